@@ -1,0 +1,139 @@
+/*
+ * prgpu.h -- C ABI of the GB300 Poisson surface reconstruction library
+ * (libprgpu.so, sm_103a).
+ *
+ * The reference (DavidXu-JJ/PoissonRecon_GPU) has no library interface: it is a
+ * single executable whose stages are host functions inside main.cu.  Each entry
+ * point below replaces one of those stages; the comment on each names the
+ * reference code it stands in for.  Conventions:
+ *   - every function returns a prgpu_status (0 = success) and never throws;
+ *   - a context owns one CUDA stream and all device buffers of one
+ *     reconstruction; it is not thread safe, distinct contexts are independent;
+ *   - host pointers are caller owned; arrays returned through prgpu_mesh are
+ *     library owned and stay valid until the next call on the same context or
+ *     prgpu_destroy().
+ */
+#ifndef PRGPU_H
+#define PRGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PRGPU_OK = 0,
+    PRGPU_ERR_ARG = 1,           /* invalid argument or call order */
+    PRGPU_ERR_CUDA = 2,          /* CUDA runtime error (see prgpu_last_error) */
+    PRGPU_ERR_NOMEM = 3,         /* device allocation failed */
+    PRGPU_ERR_LIMIT = 4,         /* input beyond a supported size */
+    PRGPU_ERR_NOT_CONVERGED = 5, /* solver hit its iteration cap (results still written) */
+    PRGPU_ERR_TIMEOUT = 6,       /* a device-side wait gave up (kernel returned early) */
+    PRGPU_ERR_IO = 7             /* file could not be read or written */
+} prgpu_status;
+
+typedef enum {
+    PRGPU_SOLVE_REFERENCE = 0,   /* CG per depth from x0=0 until float(r.r) <= tol^2 or max_iter (CG_CUDA.cuh:256-324) */
+    PRGPU_SOLVE_RELATIVE = 1     /* CG per depth until ||r|| <= tol*||b||, FP64 reductions */
+} prgpu_solve_mode;
+
+typedef struct {
+    int32_t depth;        /* maxDepth, root = depth 0 (main.cu:69); 1..15 */
+    int32_t solve_mode;   /* prgpu_solve_mode */
+    double cg_tol;        /* 1e-5 absolute (reference) or relative tolerance */
+    int32_t cg_max_iter;  /* 10000 in the reference (CG_CUDA.cuh:263) */
+    int32_t device;       /* CUDA device ordinal */
+    int32_t reserved[8];
+} prgpu_params;
+
+typedef struct {
+    int64_t n_vertices;
+    int64_t n_triangles;
+    const float* vertices;     /* 3*n_vertices, in input coordinates */
+    const int32_t* triangles;  /* 3*n_triangles vertex indices */
+} prgpu_mesh;
+
+/* Defaults: depth 8, reference CG schedule (tol 1e-5, 10000 iterations), device 0. */
+int prgpu_params_default(prgpu_params* p);
+
+/* Context lifetime.  Replaces the process-global state of main.cu:3247-3270. */
+int prgpu_create(const prgpu_params* p, void** ctx);
+int prgpu_destroy(void* ctx);
+
+/* Oriented points, 3 floats per point each, host memory.  The reference reads
+ * them from a PointStream (main.cu:516-571; PointStream.inl). */
+int prgpu_set_points(void* ctx, const float* xyz, const float* nrm, int64_t n);
+/* Same, from device memory already resident on the context's device. */
+int prgpu_set_points_device(void* ctx, const float* d_xyz, const float* d_nrm, int64_t n);
+
+/* Normalisation, Morton keys, radix sort, node arrays and 27-neighbour tables.
+ * Replaces pipelineBuildNodeArray (main.cu:511-841). */
+int prgpu_build_octree(void* ctx);
+
+/* Basis tables, vector-field splat and divergence for every depth.
+ * Replaces main.cu:3306-3462 (FunctionData tables, computeVectorField,
+ * computeEncodedFinerNodesDivergence and the coarse divergence loop). */
+int prgpu_compute_rhs(void* ctx);
+
+/* Per-depth Laplacian solve (matrix-free 27-point stencil).
+ * Replaces LaplacianIteration (main.cu:1223-1332) and solverCG_DeviceToDevice. */
+int prgpu_solve(void* ctx);
+
+/* Implicit function at the input points and the iso-value.
+ * Replaces calculatePointsImplicitFunctionValue + reduce (main.cu:1334-1381,3480-3499). */
+int prgpu_eval_points(void* ctx, float* iso_out);
+
+/* Marching cubes on the finest nodes and on subdivided coarse leaves.
+ * Replaces main.cu:3504-4561. */
+int prgpu_extract_mesh(void* ctx);
+
+/* Copies the mesh to library-owned host memory (input coordinates). */
+int prgpu_get_mesh(void* ctx, prgpu_mesh* out);
+
+/* All stages in order; equivalent to the body of main() (main.cu:3247-4573)
+ * without file I/O. */
+int prgpu_reconstruct(void* ctx, const float* xyz, const float* nrm, int64_t n, prgpu_mesh* out);
+
+/* Copy an internal array to host memory.  Names: "key","pidx","pnum","parent",
+ * "children","neighs","didx","dnum","base","count","points","normals",
+ * "point_node","vfield","divergence","x","point_value","stencil","cg_iters",
+ * "cg_rr","has_tri","has_int","dot","ddot","d2dot","center","scale","iso".
+ * Node arrays follow the reference OctNode field meaning (OctNode.cuh:8-41);
+ * "children" and "neighs" are 8 and 27 int32 per node.  *bytes receives the
+ * size; with dst == NULL only the size is returned. */
+int prgpu_get_array(void* ctx, const char* name, void* dst, int64_t max_bytes, int64_t* bytes);
+/* Replace an internal float array ("vfield","divergence","x","iso") before the
+ * next stage runs (stage-by-stage parity tests). */
+int prgpu_set_array(void* ctx, const char* name, const void* src, int64_t bytes);
+
+/* Per-stage device times, counts and solver statistics as one JSON object. */
+int prgpu_stats_json(void* ctx, char* buf, int64_t len);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or timing events after the library's. */
+int prgpu_get_stream(void* ctx, void** stream);
+
+/* Number of kernels this process has launched through the library. */
+int64_t prgpu_kernel_launches(void);
+
+/* Human-readable text of the last error on this thread. */
+const char* prgpu_last_error(void);
+
+/* Conjugate gradients on a CSR matrix in device memory, x0 = 0, stopping when
+ * float(r.r) <= tol^2 or after max_iter iterations; FP32 vectors, FP64 dots.
+ * Replaces solverCG_DeviceToDevice(N, nz, I, J, val, rhs, x) (CG_CUDA.cuh:344-509).
+ * I has N+1 row offsets.  iters / kernel_ms may be NULL. */
+int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* d_col,
+                 const float* d_val, const float* d_rhs, float* d_x, float tol, int32_t max_iter,
+                 int32_t* iters, float* kernel_ms);
+
+/* PLY I/O (PointStream.inl:160-239 input; PlyWriteTriangles plyfile.cu:2769-2836 output).
+ * prgpu_read_points returns library-owned arrays valid until the next call. */
+int prgpu_read_points(const char* path, int64_t* n, const float** xyz, const float** nrm);
+int prgpu_write_mesh_ply(const char* path, const prgpu_mesh* mesh, int32_t binary);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRGPU_H */

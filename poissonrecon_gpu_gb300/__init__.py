@@ -1,0 +1,264 @@
+"""GB300 Poisson surface reconstruction: Python host interface over libprgpu.so.
+
+The compute path is the sm_103a CUDA library built from ``csrc/``; this module
+only moves arrays across its C ABI (``include/prgpu.h``).  The stage methods
+mirror the reference's stage functions (main.cu):
+
+==========================  ==============================================
+``build_octree``            ``pipelineBuildNodeArray`` (main.cu:511)
+``compute_rhs``             basis tables, ``computeVectorField``, divergence
+``solve``                   ``LaplacianIteration`` / ``solverCG_DeviceToDevice``
+``eval_points``             ``calculatePointsImplicitFunctionValue`` + iso
+``extract_mesh``            marching cubes + coarse-leaf subdivision
+==========================  ==============================================
+
+There is no CPU fallback: constructing a :class:`Reconstructor` without the
+compiled library or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libprgpu.so")
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "size limit",
+          5: "not converged", 6: "device wait timed out", 7: "I/O error"}
+SOLVE_REFERENCE, SOLVE_RELATIVE = 0, 1
+
+# element types of the arrays behind prgpu_get_array
+ARRAY_DTYPES = {
+    "key": np.int64, "pidx": np.int32, "pnum": np.int32, "didx": np.int32, "dnum": np.int32,
+    "parent": np.int32, "children": np.int32, "neighs": np.int32, "point_node": np.int32,
+    "points": np.float32, "normals": np.float32, "sort_idx": np.uint32, "base": np.int64,
+    "count": np.int64, "center": np.float32, "scale": np.float32, "vfield": np.float32,
+    "divergence": np.float32, "stencil": np.float32, "ddot_rows": np.float32, "dot": np.float64,
+    "ddot": np.float64, "d2dot": np.float64, "x": np.float32, "cg_iters": np.int32, "cg_rr": np.float32,
+    "point_value": np.float32, "iso": np.float32, "has_tri": np.int32, "has_int": np.int32,
+    "batch_tri": np.int64, "subdivide_roots": np.int64,
+}
+
+
+class PrgpuError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = "%s failed: %s (%s)" % (where, STATUS.get(status, status), _lib().prgpu_last_error().decode())
+        super().__init__(msg)
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("depth", ctypes.c_int32), ("solve_mode", ctypes.c_int32), ("cg_tol", ctypes.c_double),
+                ("cg_max_iter", ctypes.c_int32), ("device", ctypes.c_int32), ("reserved", ctypes.c_int32 * 8)]
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("n_vertices", ctypes.c_int64), ("n_triangles", ctypes.c_int64),
+                ("vertices", ctypes.POINTER(ctypes.c_float)), ("triangles", ctypes.POINTER(ctypes.c_int32))]
+
+
+# every entry point of include/prgpu.h with its ctypes signature
+_VP, _I64, _I32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+SIGNATURES = {
+    "prgpu_params_default": (ctypes.c_int, [ctypes.POINTER(Params)]),
+    "prgpu_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(_VP)]),
+    "prgpu_destroy": (ctypes.c_int, [_VP]),
+    "prgpu_set_points": (ctypes.c_int, [_VP, _VP, _VP, _I64]),
+    "prgpu_set_points_device": (ctypes.c_int, [_VP, _VP, _VP, _I64]),
+    "prgpu_build_octree": (ctypes.c_int, [_VP]),
+    "prgpu_compute_rhs": (ctypes.c_int, [_VP]),
+    "prgpu_solve": (ctypes.c_int, [_VP]),
+    "prgpu_eval_points": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float)]),
+    "prgpu_extract_mesh": (ctypes.c_int, [_VP]),
+    "prgpu_get_mesh": (ctypes.c_int, [_VP, ctypes.POINTER(Mesh)]),
+    "prgpu_reconstruct": (ctypes.c_int, [_VP, _VP, _VP, _I64, ctypes.POINTER(Mesh)]),
+    "prgpu_get_array": (ctypes.c_int, [_VP, ctypes.c_char_p, _VP, _I64, ctypes.POINTER(_I64)]),
+    "prgpu_set_array": (ctypes.c_int, [_VP, ctypes.c_char_p, _VP, _I64]),
+    "prgpu_stats_json": (ctypes.c_int, [_VP, ctypes.c_char_p, _I64]),
+    "prgpu_last_error": (ctypes.c_char_p, []),
+    "prgpu_get_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "prgpu_kernel_launches": (ctypes.c_int64, []),
+    "prgpu_cg_csr": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32,
+                                    ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_float)]),
+    "prgpu_read_points": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_I64), ctypes.POINTER(_VP),
+                                         ctypes.POINTER(_VP)]),
+    "prgpu_write_mesh_ply": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Mesh), _I32]),
+}
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libprgpu.so is not built (run poissonrecon_gpu_gb300/builder.py); "
+                              "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _check(rc, where):
+    if rc != 0:
+        raise PrgpuError(rc, where)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Reconstructor:
+    """One reconstruction context on one GPU (its own CUDA stream)."""
+
+    def __init__(self, depth: int = 8, solve_mode: int = SOLVE_REFERENCE, cg_tol: float = 1e-5,
+                 cg_max_iter: int = 10000, device: int = 0):
+        L = _lib()
+        p = Params()
+        L.prgpu_params_default(ctypes.byref(p))
+        p.depth, p.solve_mode, p.cg_tol, p.cg_max_iter, p.device = depth, solve_mode, cg_tol, cg_max_iter, device
+        self.params = p
+        self._h = _VP()
+        _check(L.prgpu_create(ctypes.byref(p), ctypes.byref(self._h)), "prgpu_create")
+        self.depth = depth
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib().prgpu_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- stages
+    def set_points(self, xyz, nrm):
+        self._xyz, self._nrm = _f32(xyz), _f32(nrm)
+        _check(_lib().prgpu_set_points(self._h, self._xyz.ctypes.data, self._nrm.ctypes.data, len(self._xyz)),
+               "prgpu_set_points")
+
+    def set_points_device(self, xyz_ptr: int, nrm_ptr: int, n: int):
+        _check(_lib().prgpu_set_points_device(self._h, xyz_ptr, nrm_ptr, n), "prgpu_set_points_device")
+
+    def build_octree(self):
+        _check(_lib().prgpu_build_octree(self._h), "prgpu_build_octree")
+
+    def compute_rhs(self):
+        _check(_lib().prgpu_compute_rhs(self._h), "prgpu_compute_rhs")
+
+    def solve(self, allow_not_converged: bool = True):
+        rc = _lib().prgpu_solve(self._h)
+        if rc == 5 and allow_not_converged:
+            return False
+        _check(rc, "prgpu_solve")
+        return True
+
+    def eval_points(self) -> float:
+        iso = ctypes.c_float(0)
+        _check(_lib().prgpu_eval_points(self._h, ctypes.byref(iso)), "prgpu_eval_points")
+        return iso.value
+
+    def extract_mesh(self):
+        _check(_lib().prgpu_extract_mesh(self._h), "prgpu_extract_mesh")
+
+    def mesh(self):
+        m = Mesh()
+        _check(_lib().prgpu_get_mesh(self._h, ctypes.byref(m)), "prgpu_get_mesh")
+        v = np.ctypeslib.as_array(m.vertices, shape=(m.n_vertices * 3,)).reshape(-1, 3).copy() \
+            if m.n_vertices else np.zeros((0, 3), np.float32)
+        f = np.ctypeslib.as_array(m.triangles, shape=(m.n_triangles * 3,)).reshape(-1, 3).copy() \
+            if m.n_triangles else np.zeros((0, 3), np.int32)
+        return v, f
+
+    def reconstruct(self, xyz, nrm):
+        self.set_points(xyz, nrm)
+        self.build_octree()
+        self.compute_rhs()
+        self.solve()
+        self.eval_points()
+        self.extract_mesh()
+        return self.mesh()
+
+    # ---- arrays
+    def get(self, name: str) -> np.ndarray:
+        L = _lib()
+        nb = _I64(0)
+        _check(L.prgpu_get_array(self._h, name.encode(), None, 0, ctypes.byref(nb)), "prgpu_get_array(%s)" % name)
+        dt = np.dtype(ARRAY_DTYPES[name])
+        out = np.empty(nb.value // dt.itemsize, dtype=dt)
+        _check(L.prgpu_get_array(self._h, name.encode(), out.ctypes.data, nb.value, ctypes.byref(nb)),
+               "prgpu_get_array(%s)" % name)
+        return out
+
+    def set(self, name: str, arr):
+        a = _f32(arr).ravel()
+        _check(_lib().prgpu_set_array(self._h, name.encode(), a.ctypes.data, a.nbytes), "prgpu_set_array(%s)" % name)
+
+    def stream(self) -> int:
+        st = _VP()
+        _check(_lib().prgpu_get_stream(self._h, ctypes.byref(st)), "prgpu_get_stream")
+        return st.value or 0
+
+    def stats(self) -> dict:
+        buf = ctypes.create_string_buffer(1 << 16)
+        _check(_lib().prgpu_stats_json(self._h, buf, len(buf)), "prgpu_stats_json")
+        return json.loads(buf.value.decode())
+
+
+# ---- reference-named helpers -------------------------------------------------
+def pipelineBuildNodeArray(xyz, nrm, depth: int, device: int = 0):
+    """Octree of an oriented point set; returns the reference OctNode fields as arrays."""
+    r = Reconstructor(depth=depth, device=device)
+    r.set_points(xyz, nrm)
+    r.build_octree()
+    out = {k: r.get(k) for k in ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum",
+                                "base", "count", "point_node", "points", "normals", "center", "scale")}
+    r.close()
+    return out
+
+
+def solverCG_DeviceToDevice(N: int, nz: int, I: int, J: int, val: int, rhs: int, x: int, tol: float = 1e-5,
+                            max_iter: int = 10000):
+    """CG on a CSR matrix in device memory (raw device pointers), x0 = 0.  Returns (kernel ms, iterations)."""
+    it = _I32(0)
+    ms = ctypes.c_float(0)
+    rc = _lib().prgpu_cg_csr(N, nz, I, J, val, rhs, x, tol, max_iter, ctypes.byref(it), ctypes.byref(ms))
+    if rc not in (0, 5):
+        raise PrgpuError(rc, "prgpu_cg_csr")
+    return ms.value, it.value
+
+
+def kernel_launches() -> int:
+    return int(_lib().prgpu_kernel_launches())
+
+
+def read_points(path: str):
+    n = _I64(0)
+    px, pn = _VP(), _VP()
+    _check(_lib().prgpu_read_points(path.encode(), ctypes.byref(n), ctypes.byref(px), ctypes.byref(pn)),
+           "prgpu_read_points")
+    xyz = np.ctypeslib.as_array(ctypes.cast(px, ctypes.POINTER(ctypes.c_float)), shape=(n.value * 3,))
+    nrm = np.ctypeslib.as_array(ctypes.cast(pn, ctypes.POINTER(ctypes.c_float)), shape=(n.value * 3,))
+    return xyz.reshape(-1, 3).copy(), nrm.reshape(-1, 3).copy()
+
+
+def write_mesh(path: str, vertices, triangles, binary: bool = True):
+    v = _f32(vertices)
+    f = np.ascontiguousarray(triangles, dtype=np.int32)
+    m = Mesh(len(v), len(f), v.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+             f.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    _check(_lib().prgpu_write_mesh_ply(path.encode(), ctypes.byref(m), int(binary)), "prgpu_write_mesh_ply")
+
+
+def build(force: bool = False):
+    from . import builder
+    return builder.build(force=force)

@@ -1,0 +1,432 @@
+// C ABI (include/prgpu.h) and stage orchestration.
+#include <cstdarg>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "context.h"
+#include "prims.cuh"
+
+namespace prgpu {
+
+static thread_local char g_err[512] = {0};
+unsigned long long g_kernel_launches = 0;
+void set_last_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+const char* last_error() { return g_err; }
+
+void Ctx::free_nodes() {
+    cudaStream_t s = stream;
+    dfree(nodes.key, s); dfree(nodes.pidx, s); dfree(nodes.pnum, s); dfree(nodes.didx, s);
+    dfree(nodes.dnum, s); dfree(nodes.parent, s); dfree(nodes.child0, s); dfree(nodes.depth, s);
+    dfree(nodes.neigh, s);
+    nodes.M = 0;
+}
+void Ctx::free_all() {
+    cudaStream_t s = stream;
+    free_nodes();
+    dfree(in_xyz, s); dfree(in_nrm, s); dfree(pts, s); dfree(nrm, s); dfree(sort_idx, s);
+    dfree(point_node, s); dfree(basis, s); dfree(ddot_div, s); dfree(full_tables, s);
+    dfree(vfield, s); dfree(divergence, s); dfree(x, s); dfree(point_value, s);
+    dfree(d_cg_iters, s); dfree(d_cg_rr, s);
+}
+
+int cg_csr_impl(int n, const int* rowptr, const int* col, const float* val, const float* rhs, float* x, float tol,
+                int max_iter, int* iters, float* ms);
+
+// timed stage runner: CUDA events on the context stream
+template <class F>
+static void timed(Ctx& c, float& acc, F&& f) {
+    CK(cudaEventRecord(c.ev0, c.stream));
+    f();
+    CK(cudaEventRecord(c.ev1, c.stream));
+    CK(cudaEventSynchronize(c.ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    acc = ms;
+}
+
+}  // namespace prgpu
+
+using namespace prgpu;
+
+#define API_BEGIN try {
+#define API_END                                                   \
+    }                                                             \
+    catch (const prgpu::Error& e) {                               \
+        return e.status;                                          \
+    }                                                             \
+    catch (...) {                                                 \
+        prgpu::set_last_error("unexpected host exception");       \
+        return PRGPU_ERR_CUDA;                                    \
+    }
+
+static Ctx* as_ctx(void* p) { return (Ctx*)p; }
+
+extern "C" {
+
+int prgpu_params_default(prgpu_params* p) {
+    if (!p) return PRGPU_ERR_ARG;
+    memset(p, 0, sizeof *p);
+    p->depth = 8;
+    p->solve_mode = PRGPU_SOLVE_REFERENCE;
+    p->cg_tol = 1e-5;
+    p->cg_max_iter = 10000;
+    p->device = 0;
+    return PRGPU_OK;
+}
+
+const char* prgpu_last_error(void) { return prgpu::last_error(); }
+
+int prgpu_create(const prgpu_params* p, void** out) {
+    if (!p || !out) return PRGPU_ERR_ARG;
+    if (p->depth < 2 || p->depth > 15) {
+        set_last_error("depth %d outside the supported range 2..15", p->depth);
+        return PRGPU_ERR_LIMIT;
+    }
+    API_BEGIN
+    Ctx* c = new Ctx();
+    c->params = *p;
+    c->D = p->depth;
+    c->device = p->device;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    // keep freed pool memory for reuse across calls
+    cudaMemPool_t pool;
+    CK(cudaDeviceGetDefaultMemPool(&pool, c->device));
+    uint64_t thr = ~0ull;
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    upload_luts();
+    *out = c;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_destroy(void* h) {
+    Ctx* c = as_ctx(h);
+    if (!c) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    c->free_all();
+    CK(cudaStreamSynchronize(c->stream));
+    cudaEventDestroy(c->ev0);
+    cudaEventDestroy(c->ev1);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return PRGPU_OK;
+    API_END
+}
+
+static int set_points_common(Ctx* c, const float* xyz, const float* nrm, int64_t n, cudaMemcpyKind kind) {
+    if (!c || !xyz || !nrm || n <= 0) {
+        set_last_error("prgpu_set_points: empty or null input");
+        return PRGPU_ERR_ARG;
+    }
+    if (n > 0x7fffffffLL / 3) {
+        set_last_error("%lld points exceed the supported count", (long long)n);
+        return PRGPU_ERR_LIMIT;
+    }
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    dfree(c->in_xyz, s);
+    dfree(c->in_nrm, s);
+    c->N = n;
+    c->in_xyz = dalloc<float>(3 * n, s);
+    c->in_nrm = dalloc<float>(3 * n, s);
+    CK(cudaMemcpyAsync(c->in_xyz, xyz, (size_t)(3 * n) * sizeof(float), kind, s));
+    CK(cudaMemcpyAsync(c->in_nrm, nrm, (size_t)(3 * n) * sizeof(float), kind, s));
+    c->stage = 1;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_set_points(void* h, const float* xyz, const float* nrm, int64_t n) {
+    return set_points_common(as_ctx(h), xyz, nrm, n, cudaMemcpyHostToDevice);
+}
+int prgpu_set_points_device(void* h, const float* xyz, const float* nrm, int64_t n) {
+    return set_points_common(as_ctx(h), xyz, nrm, n, cudaMemcpyDeviceToDevice);
+}
+
+#define REQUIRE_STAGE(c, st)                                                  \
+    do {                                                                      \
+        if (!(c) || (c)->stage < (st)) {                                      \
+            prgpu::set_last_error("%s called before its inputs exist", __func__); \
+            return PRGPU_ERR_ARG;                                             \
+        }                                                                     \
+    } while (0)
+
+int prgpu_build_octree(void* h) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 1);
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    timed(*c, c->t.octree_ms, [&] { stage_octree(*c); });
+    c->stage = 2;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_compute_rhs(void* h) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 2);
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    timed(*c, c->t.basis_ms, [&] { stage_basis(*c); });
+    timed(*c, c->t.splat_ms, [&] { stage_splat(*c); });
+    timed(*c, c->t.divergence_ms, [&] { stage_divergence(*c); });
+    c->stage = 3;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_solve(void* h) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 3);
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    timed(*c, c->t.solve_ms, [&] { stage_solve(*c); });
+    c->stage = 4;
+    bool conv = true;
+    for (int d = 0; d <= c->D; ++d)
+        if (c->cg_iters[d] >= c->params.cg_max_iter) conv = false;
+    return conv ? PRGPU_OK : PRGPU_ERR_NOT_CONVERGED;
+    API_END
+}
+
+int prgpu_eval_points(void* h, float* iso_out) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 4);
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    timed(*c, c->t.iso_ms, [&] { stage_points(*c); });
+    if (iso_out) *iso_out = c->iso;
+    c->stage = 5;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_extract_mesh(void* h) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 5);
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    timed(*c, c->t.mesh_ms, [&] { stage_mesh(*c); });
+    c->stage = 6;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_get_mesh(void* h, prgpu_mesh* out) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 6);
+    if (!out) return PRGPU_ERR_ARG;
+    out->n_vertices = (int64_t)c->mesh_v.size() / 3;
+    out->n_triangles = (int64_t)c->mesh_f.size() / 3;
+    out->vertices = c->mesh_v.data();
+    out->triangles = c->mesh_f.data();
+    return PRGPU_OK;
+}
+
+int prgpu_reconstruct(void* h, const float* xyz, const float* nrm, int64_t n, prgpu_mesh* out) {
+    int rc = prgpu_set_points(h, xyz, nrm, n);
+    if (rc) return rc;
+    if ((rc = prgpu_build_octree(h))) return rc;
+    if ((rc = prgpu_compute_rhs(h))) return rc;
+    int solve_rc = prgpu_solve(h);
+    if (solve_rc && solve_rc != PRGPU_ERR_NOT_CONVERGED) return solve_rc;
+    if ((rc = prgpu_eval_points(h, nullptr))) return rc;
+    if ((rc = prgpu_extract_mesh(h))) return rc;
+    if (out && (rc = prgpu_get_mesh(h, out))) return rc;
+    return PRGPU_OK;
+}
+
+// ----------------------------- array access ---------------------------------
+namespace {
+__global__ void k_expand_children(const int* __restrict__ child0, i64 M, int* __restrict__ out) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (i64)gridDim.x * blockDim.x)
+        for (int k = 0; k < 8; ++k) out[8 * i + k] = child0[i] == -1 ? -1 : child0[i] + k;
+}
+__global__ void k_neigh_aos(const int* __restrict__ neigh, i64 M, int* __restrict__ out) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (i64)gridDim.x * blockDim.x)
+        for (int j = 0; j < 27; ++j) out[27 * i + j] = neigh[(i64)j * M + i];
+}
+}  // namespace
+
+static int copy_out(Ctx* c, const void* dsrc, int64_t bytes, void* dst, int64_t max_bytes, int64_t* nbytes,
+                    bool host_src = false) {
+    if (nbytes) *nbytes = bytes;
+    if (!dst) return PRGPU_OK;
+    if (max_bytes < bytes) {
+        set_last_error("destination holds %lld bytes, %lld needed", (long long)max_bytes, (long long)bytes);
+        return PRGPU_ERR_ARG;
+    }
+    if (bytes == 0) return PRGPU_OK;
+    if (host_src) { memcpy(dst, dsrc, (size_t)bytes); return PRGPU_OK; }
+    CK(cudaMemcpyAsync(dst, dsrc, (size_t)bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_get_array(void* h, const char* name, void* dst, int64_t max_bytes, int64_t* nbytes) {
+    Ctx* c = as_ctx(h);
+    if (!c || !name) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    std::string n(name);
+    const i64 M = c->nodes.M;
+    cudaStream_t s = c->stream;
+    if (c->stage >= 2) {
+        if (n == "key") {
+            // int64 copy of the u64 keys
+            return copy_out(c, c->nodes.key, M * 8, dst, max_bytes, nbytes);
+        }
+        if (n == "pidx") return copy_out(c, c->nodes.pidx, M * 4, dst, max_bytes, nbytes);
+        if (n == "pnum") return copy_out(c, c->nodes.pnum, M * 4, dst, max_bytes, nbytes);
+        if (n == "didx") return copy_out(c, c->nodes.didx, M * 4, dst, max_bytes, nbytes);
+        if (n == "dnum") return copy_out(c, c->nodes.dnum, M * 4, dst, max_bytes, nbytes);
+        if (n == "parent") return copy_out(c, c->nodes.parent, M * 4, dst, max_bytes, nbytes);
+        if (n == "point_node") return copy_out(c, c->point_node, c->N * 4, dst, max_bytes, nbytes);
+        if (n == "points") return copy_out(c, c->pts, c->N * 12, dst, max_bytes, nbytes);
+        if (n == "normals") return copy_out(c, c->nrm, c->N * 12, dst, max_bytes, nbytes);
+        if (n == "sort_idx") return copy_out(c, c->sort_idx, c->N * 4, dst, max_bytes, nbytes);
+        if (n == "base") return copy_out(c, c->base.data(), (int64_t)c->base.size() * 8, dst, max_bytes, nbytes, true);
+        if (n == "count") return copy_out(c, c->count.data(), (int64_t)c->count.size() * 8, dst, max_bytes, nbytes, true);
+        if (n == "center") return copy_out(c, c->center, 12, dst, max_bytes, nbytes, true);
+        if (n == "scale") return copy_out(c, &c->scale, 4, dst, max_bytes, nbytes, true);
+        if (n == "children" || n == "neighs") {
+            const int w = (n == "children") ? 8 : 27;
+            if (nbytes) *nbytes = M * w * 4;
+            if (!dst) return PRGPU_OK;
+            int* tmp = dalloc<int>(M * w, s);
+            if (w == 8) k_expand_children<<<grid_for(M, 256), 256, 0, s>>>(c->nodes.child0, M, tmp);
+            else k_neigh_aos<<<grid_for(M, 256), 256, 0, s>>>(c->nodes.neigh, M, tmp);
+            CK_LAUNCH();
+            int rc = copy_out(c, tmp, M * w * 4, dst, max_bytes, nbytes);
+            dfree(tmp, s);
+            return rc;
+        }
+    }
+    if (c->stage >= 3) {
+        if (n == "vfield") return copy_out(c, c->vfield, c->count[c->D] * 12, dst, max_bytes, nbytes);
+        if (n == "divergence") return copy_out(c, c->divergence, M * 4, dst, max_bytes, nbytes);
+        if (n == "stencil")
+            return copy_out(c, c->stencil.data(), (int64_t)c->stencil.size() * 4, dst, max_bytes, nbytes, true);
+        if (n == "ddot_rows")
+            return copy_out(c, c->ddot_div, c->ddot_row_start.back() * 4, dst, max_bytes, nbytes);
+        if (n == "dot" || n == "ddot" || n == "d2dot") {
+            const i64 res = (1 << (c->D + 1)) - 1, R2 = res * res;
+            if (nbytes) *nbytes = R2 * 8;
+            if (!dst) return PRGPU_OK;
+            if (!c->full_tables) stage_full_tables(*c);
+            const int which = (n == "dot") ? 0 : (n == "ddot" ? 1 : 2);
+            return copy_out(c, c->full_tables + which * R2, R2 * 8, dst, max_bytes, nbytes);
+        }
+    }
+    if (c->stage >= 4) {
+        if (n == "x") return copy_out(c, c->x, M * 4, dst, max_bytes, nbytes);
+        if (n == "cg_iters")
+            return copy_out(c, c->cg_iters.data(), (int64_t)c->cg_iters.size() * 4, dst, max_bytes, nbytes, true);
+        if (n == "cg_rr") return copy_out(c, c->cg_rr.data(), (int64_t)c->cg_rr.size() * 4, dst, max_bytes, nbytes, true);
+    }
+    if (c->stage >= 5) {
+        if (n == "point_value") return copy_out(c, c->point_value, c->N * 4, dst, max_bytes, nbytes);
+        if (n == "iso") return copy_out(c, &c->iso, 4, dst, max_bytes, nbytes, true);
+    }
+    if (c->stage >= 6) {
+        if (n == "has_tri") return copy_out(c, c->has_tri.data(), (int64_t)c->has_tri.size() * 4, dst, max_bytes, nbytes, true);
+        if (n == "has_int") return copy_out(c, c->has_int.data(), (int64_t)c->has_int.size() * 4, dst, max_bytes, nbytes, true);
+        if (n == "batch_tri")
+            return copy_out(c, c->batch_tri.data(), (int64_t)c->batch_tri.size() * 8, dst, max_bytes, nbytes, true);
+        if (n == "subdivide_roots") return copy_out(c, &c->subdivide_roots, 8, dst, max_bytes, nbytes, true);
+    }
+    set_last_error("unknown array '%s' or its stage has not run", name);
+    return PRGPU_ERR_ARG;
+    API_END
+}
+
+int prgpu_set_array(void* h, const char* name, const void* src, int64_t bytes) {
+    Ctx* c = as_ctx(h);
+    if (!c || !name || !src) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    std::string n(name);
+    const i64 M = c->nodes.M;
+    float* dst = nullptr;
+    i64 need = 0;
+    if (n == "vfield" && c->stage >= 3) { dst = c->vfield; need = c->count[c->D] * 12; }
+    else if (n == "divergence" && c->stage >= 3) { dst = c->divergence; need = M * 4; }
+    else if (n == "x" && c->stage >= 4) { dst = c->x; need = M * 4; }
+    else if (n == "iso" && c->stage >= 5) {
+        if (bytes != 4) return PRGPU_ERR_ARG;
+        memcpy(&c->iso, src, 4);
+        return PRGPU_OK;
+    }
+    if (!dst || bytes != need) {
+        set_last_error("cannot set '%s' (%lld bytes) at this stage", name, (long long)bytes);
+        return PRGPU_ERR_ARG;
+    }
+    CK(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_stats_json(void* h, char* buf, int64_t len) {
+    Ctx* c = as_ctx(h);
+    if (!c || !buf || len <= 0) return PRGPU_ERR_ARG;
+    std::string js = "{";
+    char tmp[256];
+    snprintf(tmp, sizeof tmp, "\"points\":%lld,\"depth\":%d,\"nodes\":%lld,", (long long)c->N, c->D,
+             (long long)c->nodes.M);
+    js += tmp;
+    js += "\"count\":[";
+    for (size_t d = 0; d < c->count.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%lld", d ? "," : "", (long long)c->count[d]);
+        js += tmp;
+    }
+    js += "],\"cg_iters\":[";
+    for (size_t d = 0; d < c->cg_iters.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%d", d ? "," : "", c->cg_iters[d]);
+        js += tmp;
+    }
+    snprintf(tmp, sizeof tmp,
+             "],\"ms\":{\"octree\":%.4f,\"basis\":%.4f,\"splat\":%.4f,\"divergence\":%.4f,\"solve\":%.4f,"
+             "\"iso\":%.4f,\"mesh\":%.4f},",
+             c->t.octree_ms, c->t.basis_ms, c->t.splat_ms, c->t.divergence_ms, c->t.solve_ms, c->t.iso_ms,
+             c->t.mesh_ms);
+    js += tmp;
+    snprintf(tmp, sizeof tmp, "\"iso\":%.9g,\"vertices\":%lld,\"triangles\":%lld,\"subdivide_roots\":%lld}",
+             (double)c->iso, (long long)c->mesh_v.size() / 3, (long long)c->mesh_f.size() / 3,
+             (long long)c->subdivide_roots);
+    js += tmp;
+    if ((int64_t)js.size() + 1 > len) return PRGPU_ERR_ARG;
+    memcpy(buf, js.c_str(), js.size() + 1);
+    return PRGPU_OK;
+}
+
+int prgpu_get_stream(void* h, void** stream) {
+    Ctx* c = as_ctx(h);
+    if (!c || !stream) return PRGPU_ERR_ARG;
+    *stream = (void*)c->stream;
+    return PRGPU_OK;
+}
+
+int64_t prgpu_kernel_launches(void) { return (int64_t)prgpu::g_kernel_launches; }
+
+int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* rowptr, const int32_t* col, const float* val, const float* rhs,
+                 float* x, float tol, int32_t max_iter, int32_t* iters, float* kernel_ms) {
+    (void)nz;
+    if (n <= 0 || !rowptr || !col || !val || !rhs || !x || max_iter < 0) return PRGPU_ERR_ARG;
+    API_BEGIN
+    return cg_csr_impl(n, rowptr, col, val, rhs, x, tol, max_iter, iters, kernel_ms);
+    API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,133 @@
+// Shared definitions for the sm_103a Poisson-reconstruction kernels.
+//
+// The library is compiled with --fmad=false: a*b+c never fuses implicitly, and
+// every fused multiply-add below is an explicit fmaf()/fma().  That makes the
+// rounding of each stage a property of the source, so the stages that restate
+// the reference arithmetic reproduce it bit for bit.
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "../../include/prgpu.h"
+
+namespace prgpu {
+
+typedef int64_t i64;
+typedef uint64_t u64;
+
+// ---------------------------------------------------------------------------
+// error handling: every CUDA call inside the library goes through CK()
+// ---------------------------------------------------------------------------
+struct Error {
+    int status;
+    char msg[256];
+};
+void set_last_error(const char* fmt, ...);
+const char* last_error();
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            ::prgpu::set_last_error("%s:%d %s: %s", __FILE__, __LINE__, #call,          \
+                                    cudaGetErrorString(e_));                            \
+            throw ::prgpu::Error{PRGPU_ERR_CUDA, {0}};                                  \
+        }                                                                               \
+    } while (0)
+// every kernel launch is followed by CK_LAUNCH(), which also counts it
+extern unsigned long long g_kernel_launches;
+#define CK_LAUNCH()                            \
+    do {                                       \
+        ++::prgpu::g_kernel_launches;          \
+        CK(cudaGetLastError());                \
+    } while (0)
+
+inline unsigned grid_for(i64 n, int block, i64 cap = (i64)152 * 64) {
+    i64 g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+// neighbour lookup tables (main.cu:80-99): neighbour j = 9(dx+1)+3(dy+1)+(dz+1);
+// child code = x<<2 | y<<1 | z.  The tables live in octree.cu's constant bank
+// and are filled from their definition at context creation.
+// ---------------------------------------------------------------------------
+void upload_luts();
+
+// ---------------------------------------------------------------------------
+// keys: 3 bits per level, level 1 most significant; x bit 2, y bit 1, z bit 0.
+// A node at depth d keeps its key in the full-depth layout (levels below d = 0).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline void key_coords(u64 key, int d, int D, int xyz[3]) {
+    int x = 0, y = 0, z = 0;
+    for (int l = 1; l <= d; ++l) {
+        int sh = 3 * (D - l);
+        x = (x << 1) | (int)((key >> (sh + 2)) & 1);
+        y = (y << 1) | (int)((key >> (sh + 1)) & 1);
+        z = (z << 1) | (int)((key >> sh) & 1);
+    }
+    xyz[0] = x; xyz[1] = y; xyz[2] = z;
+}
+__host__ __device__ inline u64 coords_key(int x, int y, int z, int d, int D) {
+    u64 k = 0;
+    for (int l = 1; l <= d; ++l) {
+        int b = d - l;
+        u64 g = ((u64)((x >> b) & 1) << 2) | ((u64)((y >> b) & 1) << 1) | (u64)((z >> b) & 1);
+        k |= g << (3 * (D - l));
+    }
+    return k;
+}
+
+// ---------------------------------------------------------------------------
+// piecewise polynomials in the reference's "starting polynomial" form:
+// value(x) = sum over pieces i with x > start[i] of poly_i(x)
+// ---------------------------------------------------------------------------
+struct CPoly {
+    float start[4];
+    float c[4][4];
+};
+
+// value() of ConfirmedPPolynomial (ConfirmedPPolynomial.cuh:79-91); the
+// reference's device compiler fused v += temp*c into one FMA.
+template <int DEG>
+__device__ __forceinline__ float cpoly_value(const CPoly& p, float x) {
+    float res = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (!(x > p.start[i])) break;
+        float temp = 1.f, v = 0.f;
+#pragma unroll
+        for (int j = 0; j <= DEG; ++j) {
+            v = fmaf(temp, p.c[i][j], v);
+            temp = temp * x;
+        }
+        res = res + v;
+    }
+    return res;
+}
+
+// ConfirmedPPolynomial::shift (ConfirmedPPolynomial.cuh:37-50)
+template <int DEG>
+__device__ __forceinline__ void cpoly_shift(const CPoly& p, float t, CPoly& r) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        r.start[i] = p.start[i] + t;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) r.c[i][k] = 0.f;
+#pragma unroll
+        for (int k = 0; k <= DEG; ++k) {
+            float temp = 1.f;
+#pragma unroll
+            for (int j = k; j >= 0; --j) {
+                r.c[i][j] = fmaf(p.c[i][k], temp, r.c[i][j]);
+                temp = temp * (-t * (float)j);
+                temp = temp / (float)(k - j + 1);
+            }
+        }
+    }
+}
+
+}  // namespace prgpu

@@ -1,0 +1,106 @@
+// Reconstruction context shared by the stage translation units.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace prgpu {
+
+// Node arrays in HBM, structure of arrays, global index = base[d] + slot.
+struct NodeArrays {
+    i64 M = 0;
+    u64* key = nullptr;      // full-depth key
+    int* pidx = nullptr;     // first sorted point of the node
+    int* pnum = nullptr;     // number of points
+    int* didx = nullptr;     // first finest-depth slot below the node
+    int* dnum = nullptr;     // number of finest-depth slots below the node
+    int* parent = nullptr;   // -1 for the root
+    int* child0 = nullptr;   // first of 8 contiguous children, -1 if none
+    int8_t* depth = nullptr;
+    int* neigh = nullptr;    // 27 x M, neighbour j of node i at neigh[j*M + i]
+};
+
+struct StageTimes {
+    float octree_ms = 0, basis_ms = 0, splat_ms = 0, divergence_ms = 0, solve_ms = 0, iso_ms = 0, mesh_ms = 0;
+};
+
+struct Ctx {
+    prgpu_params params;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int D = 8;
+    int res = 0;
+
+    // input
+    i64 N = 0;
+    float* in_xyz = nullptr;   // 3N raw
+    float* in_nrm = nullptr;
+    // normalised, sorted
+    float* pts = nullptr;      // 3N
+    float* nrm = nullptr;      // 3N (length 2^(D+1))
+    uint32_t* sort_idx = nullptr;
+    float center[3] = {0, 0, 0};
+    float scale = 1.f;
+
+    std::vector<i64> base, count;
+    NodeArrays nodes;
+    int* point_node = nullptr;
+
+    // basis
+    CPoly* basis = nullptr;          // res functions (degree 3 storage)
+    CPoly basis_maxdepth;            // splat kernel, degree 2
+    float* ddot_div = nullptr;       // compact inner-product rows used by the divergence
+    std::vector<i64> ddot_row_start; // per depth
+    std::vector<float> stencil;      // 27 per depth
+    double* full_tables = nullptr;   // dot, ddot, d2dot (res*res each), on demand
+
+    // rhs / solve
+    float* vfield = nullptr;         // 3 x count[D]
+    float* divergence = nullptr;     // M
+    float* x = nullptr;              // M
+    std::vector<int> cg_iters;
+    std::vector<float> cg_rr;
+    int* d_cg_iters = nullptr;
+    float* d_cg_rr = nullptr;
+
+    // iso
+    float* point_value = nullptr;
+    float iso = 0.f;
+
+    // mesh (host, input coordinates)
+    std::vector<float> mesh_v;
+    std::vector<int32_t> mesh_f;
+    std::vector<int> has_tri, has_int;
+    i64 subdivide_roots = 0;
+    std::vector<i64> batch_tri;
+
+    StageTimes t;
+    int stage = 0;   // 0 none, 1 points, 2 octree, 3 rhs, 4 solved, 5 iso, 6 mesh
+    i64 kernel_launches = 0;
+
+    void free_nodes();
+    void free_all();
+};
+
+// stage entry points (each throws prgpu::Error on failure)
+void stage_octree(Ctx& c);
+void stage_basis(Ctx& c);
+void stage_full_tables(Ctx& c);
+void stage_splat(Ctx& c);
+void stage_divergence(Ctx& c);
+void stage_solve(Ctx& c);
+void stage_points(Ctx& c);
+void stage_mesh(Ctx& c);
+
+// host-side basis setup (reference host arithmetic, unfused)
+struct HostBasis {
+    CPoly base;       // F/F(0), degree 2, 4 pieces
+    CPoly dbase;      // derivative, degree 1
+    int npieces;
+};
+HostBasis host_base_function();
+void host_stencils(int D, std::vector<float>& stencil);
+
+}  // namespace prgpu

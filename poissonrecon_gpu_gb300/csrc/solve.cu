@@ -1,0 +1,438 @@
+// Per-depth Laplacian solve.  Replaces LaplacianIteration (main.cu:1223-1332)
+// and solverCG_DeviceToDevice / gpuConjugateGradient (CG_CUDA.cuh:186-509).
+//
+// The reference assembles a CSR matrix per depth and runs one cooperative CG
+// kernel per depth, one depth after the other.  Here the matrix is never
+// stored: same-depth inner products are translation invariant, so row i of L_d
+// is the depth's 27 stencil coefficients applied through the node's neighbour
+// table (the reference's |L_ij| <= 1e-6 drop rule is applied to the stencil).
+// The depths are independent systems (each starts from x0 = 0 and never sees
+// the others), so ONE persistent cooperative launch solves all of them at
+// once: the co-resident blocks are partitioned between the depths in
+// proportion to their row counts, and each partition runs its own CG with its
+// own grid barrier.  Barriers spin with an iteration limit; on expiry the
+// kernel records PRGPU_ERR_TIMEOUT and returns.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "context.h"
+#include "prims.cuh"
+
+namespace prgpu {
+
+constexpr int CG_BLOCK = 256;
+constexpr long long SPIN_LIMIT = 1ll << 24;   // polls of ~32 ns: about half a second
+
+struct PartState {          // one per depth, in global memory, zero-initialised
+    double acc[3];
+    unsigned count;
+    unsigned gen;
+    int iters;
+    float rr;
+    int status;
+    int pad;
+};
+
+struct CgDepth {
+    i64 lo, n;              // global row range
+    int first_block, nblocks;
+    float st[27];
+    double bb;              // ||b||^2 (relative mode)
+};
+
+struct CgArgs {
+    int ndepth;
+    int mode;               // prgpu_solve_mode
+    float tol2;             // reference mode: float(tol)*float(tol)
+    double rel2;            // relative mode: tol^2
+    int max_iter;
+    i64 M;
+    const int* neigh;       // 27 x M
+    const float* b;
+    float* x;
+    float* r;
+    float* p;
+    float* q;
+    PartState* state;
+    int* err;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
+    __syncthreads();
+    return s;   // valid in thread 0
+}
+
+// barrier over the blocks of one partition; returns false after a timeout
+__device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok) {
+    __syncthreads();
+    if (nblocks > 1) {
+        if (threadIdx.x == 0) {
+            volatile unsigned* vgen = &ps->gen;
+            unsigned g = *vgen;
+            __threadfence();
+            unsigned arrived = atomicAdd(&ps->count, 1u);
+            int ok = 1;
+            if (arrived == (unsigned)nblocks - 1) {
+                atomicExch(&ps->count, 0u);
+                __threadfence();
+                atomicAdd(&ps->gen, 1u);
+            } else {
+                long long spins = 0;
+                while (*vgen == g) {
+                    if (++spins > SPIN_LIMIT || *(volatile int*)err) { ok = 0; break; }
+                    __nanosleep(32);
+                }
+            }
+            __threadfence();
+            if (!ok) atomicExch(err, PRGPU_ERR_TIMEOUT);
+            *sh_ok = ok && !*(volatile int*)err;
+        }
+    } else if (threadIdx.x == 0) {
+        __threadfence_block();
+        *sh_ok = 1;
+    }
+    __syncthreads();
+    return *sh_ok != 0;
+}
+
+__global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
+                                                     const int* __restrict__ block_depth) {
+    __shared__ double sh[CG_BLOCK / 32];
+    __shared__ int sh_ok;
+    __shared__ double sh_val;
+    const int d = block_depth[blockIdx.x];
+    const CgDepth dp = deps[d];
+    PartState* ps = &a.state[d];
+    const int rank = blockIdx.x - dp.first_block;
+    const i64 stride = (i64)dp.nblocks * blockDim.x;
+    const i64 start = (i64)rank * blockDim.x + threadIdx.x;
+    int red = 0;   // reduction counter selects the accumulator slot
+
+    // reduce a per-thread double over the partition; every thread gets the sum
+    auto preduce = [&](double v, bool& ok) -> double {
+        double s = block_sum(v, sh);
+        if (threadIdx.x == 0) atomicAdd(&ps->acc[red % 3], s);
+        ok = part_barrier(ps, dp.nblocks, a.err, &sh_ok);
+        if (threadIdx.x == 0) sh_val = *(volatile double*)&ps->acc[red % 3];
+        __syncthreads();
+        double res = sh_val;
+        if (rank == 0 && threadIdx.x == 0) ps->acc[(red + 2) % 3] = 0.0;
+        ++red;
+        return res;
+    };
+
+    // x = 0, r = b  (the host-side initialisation of CG_CUDA.cuh:435-439)
+    double loc = 0;
+    for (i64 t = start; t < dp.n; t += stride) {
+        const i64 i = dp.lo + t;
+        const float bi = a.b[i];
+        a.x[i] = 0.f;
+        a.r[i] = bi;
+        loc += (double)(bi * bi);
+    }
+    bool ok = true;
+    float r1 = (float)preduce(loc, ok);
+    float r0 = 0.f;
+    int k = 1;
+    while (ok) {
+        const bool go = (a.mode == PRGPU_SOLVE_REFERENCE) ? (r1 > a.tol2) : ((double)r1 > a.rel2 * dp.bb);
+        if (!go || k > a.max_iter) break;
+        // p = r + beta p
+        if (k > 1) {
+            const float beta = r1 / r0;
+            for (i64 t = start; t < dp.n; t += stride) {
+                const i64 i = dp.lo + t;
+                a.p[i] = fmaf(beta, a.p[i], a.r[i]);
+            }
+        } else {
+            for (i64 t = start; t < dp.n; t += stride) {
+                const i64 i = dp.lo + t;
+                a.p[i] = a.r[i];
+            }
+        }
+        if (!part_barrier(ps, dp.nblocks, a.err, &sh_ok)) break;
+        // q = A p, partial p.q
+        loc = 0;
+        for (i64 t = start; t < dp.n; t += stride) {
+            const i64 i = dp.lo + t;
+            float o = 0.f;
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                const int nb = a.neigh[(i64)j * a.M + i];
+                if (nb != -1 && dp.st[j] != 0.f) o = fmaf(dp.st[j], a.p[nb], o);
+            }
+            a.q[i] = o;
+            loc += (double)(a.p[i] * o);
+        }
+        const double pq = preduce(loc, ok);
+        if (!ok) break;
+        const float al = (float)((double)r1 / pq);
+        const float nal = -al;
+        loc = 0;
+        for (i64 t = start; t < dp.n; t += stride) {
+            const i64 i = dp.lo + t;
+            a.x[i] = fmaf(al, a.p[i], a.x[i]);
+            const float ri = fmaf(nal, a.q[i], a.r[i]);
+            a.r[i] = ri;
+            loc += (double)(ri * ri);
+        }
+        r0 = r1;
+        r1 = (float)preduce(loc, ok);
+        ++k;
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        ps->iters = k - 1;
+        ps->rr = r1;
+        ps->status = ok ? 0 : PRGPU_ERR_TIMEOUT;
+    }
+}
+
+void stage_solve(Ctx& c) {
+    cudaStream_t s = c.stream;
+    const int D = c.D;
+    const i64 M = c.nodes.M;
+    dfree(c.x, s);
+    c.x = dalloc<float>(M, s);
+    float* r = dalloc<float>(M, s);
+    float* p = dalloc<float>(M, s);
+    float* q = dalloc<float>(M, s);
+    // |b|^2 per depth for the relative criterion
+    std::vector<double> bb(D + 1, 0.0);
+    if (c.params.solve_mode == PRGPU_SOLVE_RELATIVE) {
+        std::vector<float> hb(M);
+        CK(cudaMemcpyAsync(hb.data(), c.divergence, M * sizeof(float), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int d = 0; d <= D; ++d)
+            for (i64 i = c.base[d]; i < c.base[d + 1]; ++i) bb[d] += (double)hb[i] * (double)hb[i];
+    }
+    // co-resident capacity
+    int dev = c.device, sms = 0, per_sm = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_all, CG_BLOCK, 0));
+    if (per_sm < 1) per_sm = 1;
+    const int G = sms * per_sm;
+    // partition: one block per small depth, the rest in proportion to rows
+    std::vector<CgDepth> deps(D + 1);
+    std::vector<int> nb(D + 1, 1);
+    i64 big_rows = 0;
+    const i64 small_rows = 4 * CG_BLOCK;
+    int fixed = 0;
+    for (int d = 0; d <= D; ++d) {
+        if (c.count[d] <= small_rows) ++fixed;
+        else big_rows += c.count[d];
+    }
+    int avail = std::max(0, G - fixed);
+    for (int d = 0; d <= D; ++d) {
+        if (c.count[d] > small_rows) {
+            i64 want = (i64)((double)avail * (double)c.count[d] / (double)std::max<i64>(big_rows, 1));
+            i64 cap = (c.count[d] + CG_BLOCK - 1) / CG_BLOCK;
+            nb[d] = (int)std::max<i64>(1, std::min(want, cap));
+        }
+    }
+    int total = 0;
+    for (int d = 0; d <= D; ++d) total += nb[d];
+    while (total > G) {   // trim the largest partitions
+        int dm = (int)(std::max_element(nb.begin(), nb.end()) - nb.begin());
+        if (nb[dm] <= 1) break;
+        --nb[dm];
+        --total;
+    }
+    if (total > G) {
+        set_last_error("solver needs %d co-resident blocks, device offers %d", total, G);
+        throw Error{PRGPU_ERR_LIMIT, {0}};
+    }
+    std::vector<int> block_depth;
+    for (int d = 0; d <= D; ++d) {
+        deps[d].lo = c.base[d];
+        deps[d].n = c.count[d];
+        deps[d].first_block = (int)block_depth.size();
+        deps[d].nblocks = nb[d];
+        for (int j = 0; j < 27; ++j) deps[d].st[j] = c.stencil[27 * d + j];
+        deps[d].bb = bb[d];
+        for (int k = 0; k < nb[d]; ++k) block_depth.push_back(d);
+    }
+    CgDepth* ddeps = dalloc<CgDepth>(D + 1, s);
+    int* dbd = dalloc<int>((i64)block_depth.size(), s);
+    PartState* st = dalloc<PartState>(D + 1, s);
+    int* err = dalloc<int>(1, s);
+    CK(cudaMemcpyAsync(ddeps, deps.data(), (D + 1) * sizeof(CgDepth), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dbd, block_depth.data(), block_depth.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(st, 0, (D + 1) * sizeof(PartState), s));
+    CK(cudaMemsetAsync(err, 0, sizeof(int), s));
+    CgArgs a;
+    a.ndepth = D + 1;
+    a.mode = c.params.solve_mode;
+    const float tolf = (float)c.params.cg_tol;
+    a.tol2 = tolf * tolf;
+    a.rel2 = c.params.cg_tol * c.params.cg_tol;
+    a.max_iter = c.params.cg_max_iter;
+    a.M = M;
+    a.neigh = c.nodes.neigh;
+    a.b = c.divergence;
+    a.x = c.x;
+    a.r = r;
+    a.p = p;
+    a.q = q;
+    a.state = st;
+    a.err = err;
+    void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
+    CK(cudaLaunchCooperativeKernel((void*)k_cg_all, dim3((unsigned)block_depth.size()), dim3(CG_BLOCK), kargs, 0, s));
+    ++g_kernel_launches;
+    std::vector<PartState> hs(D + 1);
+    int herr = 0;
+    CK(cudaMemcpyAsync(hs.data(), st, (D + 1) * sizeof(PartState), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    c.cg_iters.assign(D + 1, 0);
+    c.cg_rr.assign(D + 1, 0.f);
+    for (int d = 0; d <= D; ++d) { c.cg_iters[d] = hs[d].iters; c.cg_rr[d] = hs[d].rr; }
+    dfree(r, s); dfree(p, s); dfree(q, s);
+    dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(err, s);
+    if (herr) {
+        set_last_error("solver barrier timed out");
+        throw Error{PRGPU_ERR_TIMEOUT, {0}};
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CSR conjugate gradients with the reference's interface (CG_CUDA.cuh:344-509)
+// ---------------------------------------------------------------------------
+struct CsrArgs {
+    int n;
+    const int* rowptr;
+    const int* col;
+    const float* val;
+    const float* b;
+    float* x;
+    float* r;
+    float* p;
+    float* q;
+    float tol2;
+    int max_iter;
+    PartState* state;
+    int* err;
+};
+
+__global__ void __launch_bounds__(CG_BLOCK) k_cg_csr(CsrArgs a) {
+    __shared__ double sh[CG_BLOCK / 32];
+    __shared__ int sh_ok;
+    __shared__ double sh_val;
+    PartState* ps = a.state;
+    const int nblocks = gridDim.x;
+    const i64 stride = (i64)gridDim.x * blockDim.x;
+    const i64 start = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    int red = 0;
+    auto preduce = [&](double v, bool& ok) -> double {
+        double s = block_sum(v, sh);
+        if (threadIdx.x == 0) atomicAdd(&ps->acc[red % 3], s);
+        ok = part_barrier(ps, nblocks, a.err, &sh_ok);
+        if (threadIdx.x == 0) sh_val = *(volatile double*)&ps->acc[red % 3];
+        __syncthreads();
+        double res = sh_val;
+        if (blockIdx.x == 0 && threadIdx.x == 0) ps->acc[(red + 2) % 3] = 0.0;
+        ++red;
+        return res;
+    };
+    double loc = 0;
+    for (i64 i = start; i < a.n; i += stride) {
+        a.x[i] = 0.f;
+        a.r[i] = a.b[i];
+        loc += (double)(a.b[i] * a.b[i]);
+    }
+    bool ok = true;
+    float r1 = (float)preduce(loc, ok), r0 = 0.f;
+    int k = 1;
+    while (ok && r1 > a.tol2 && k <= a.max_iter) {
+        if (k > 1) {
+            const float beta = r1 / r0;
+            for (i64 i = start; i < a.n; i += stride) a.p[i] = fmaf(beta, a.p[i], a.r[i]);
+        } else {
+            for (i64 i = start; i < a.n; i += stride) a.p[i] = a.r[i];
+        }
+        if (!part_barrier(ps, nblocks, a.err, &sh_ok)) break;
+        loc = 0;
+        for (i64 i = start; i < a.n; i += stride) {
+            float o = 0.f;
+            for (int e = a.rowptr[i]; e < a.rowptr[i + 1]; ++e) o = fmaf(a.val[e], a.p[a.col[e]], o);
+            a.q[i] = o;
+            loc += (double)(a.p[i] * o);
+        }
+        const double pq = preduce(loc, ok);
+        if (!ok) break;
+        const float al = (float)((double)r1 / pq), nal = -al;
+        loc = 0;
+        for (i64 i = start; i < a.n; i += stride) {
+            a.x[i] = fmaf(al, a.p[i], a.x[i]);
+            const float ri = fmaf(nal, a.q[i], a.r[i]);
+            a.r[i] = ri;
+            loc += (double)(ri * ri);
+        }
+        r0 = r1;
+        r1 = (float)preduce(loc, ok);
+        ++k;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ps->iters = k - 1;
+        ps->rr = r1;
+    }
+}
+
+int cg_csr_impl(int n, const int* rowptr, const int* col, const float* val, const float* rhs, float* x, float tol,
+                int max_iter, int* iters, float* ms) {
+    cudaStream_t s = 0;
+    int dev = 0, sms = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_csr, CG_BLOCK, 0));
+    i64 want = ((i64)n + CG_BLOCK - 1) / CG_BLOCK;
+    int G = (int)std::max<i64>(1, std::min<i64>((i64)sms * std::max(per_sm, 1), want));
+    float *r = nullptr, *p = nullptr, *q = nullptr;
+    PartState* st = nullptr;
+    int* err = nullptr;
+    CK(cudaMalloc(&r, sizeof(float) * std::max(n, 1)));
+    CK(cudaMalloc(&p, sizeof(float) * std::max(n, 1)));
+    CK(cudaMalloc(&q, sizeof(float) * std::max(n, 1)));
+    CK(cudaMalloc(&st, sizeof(PartState)));
+    CK(cudaMalloc(&err, sizeof(int)));
+    CK(cudaMemset(st, 0, sizeof(PartState)));
+    CK(cudaMemset(err, 0, sizeof(int)));
+    CsrArgs a;
+    a.n = n; a.rowptr = rowptr; a.col = col; a.val = val; a.b = rhs; a.x = x; a.r = r; a.p = p; a.q = q;
+    a.tol2 = tol * tol;
+    a.max_iter = max_iter;
+    a.state = st;
+    a.err = err;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    void* kargs[] = {(void*)&a};
+    CK(cudaEventRecord(e0, s));
+    CK(cudaLaunchCooperativeKernel((void*)k_cg_csr, dim3(G), dim3(CG_BLOCK), kargs, 0, s));
+    ++g_kernel_launches;
+    CK(cudaEventRecord(e1, s));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    PartState hs;
+    int herr = 0;
+    CK(cudaMemcpy(&hs, st, sizeof hs, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&herr, err, sizeof herr, cudaMemcpyDeviceToHost));
+    cudaFree(r); cudaFree(p); cudaFree(q); cudaFree(st); cudaFree(err);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (iters) *iters = hs.iters;
+    if (ms) *ms = t;
+    if (herr) {
+        set_last_error("CG barrier timed out");
+        return PRGPU_ERR_TIMEOUT;
+    }
+    return hs.iters >= max_iter && hs.rr > a.tol2 ? PRGPU_ERR_NOT_CONVERGED : PRGPU_OK;
+}
+
+}  // namespace prgpu

@@ -1,0 +1,208 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Tolerances:
+  * integer stages (octree arrays, subdivision flags, triangle topology): bit-exact;
+  * stages whose arithmetic is restated operation for operation (normalised
+    points, inner-product tables, vector field, finest-depth divergence, stencil,
+    implicit values from the same solution, marching-cubes vertices): bit-exact;
+  * divergence at depths < D-1 (FP64 block reduction instead of a sequential
+    FP64 sum): |diff| <= 2 ulp of the value;
+  * CG solution (different FP64 reduction order): per depth
+    max|x_gpu - x_orc| <= 1e-4 * max|x_orc|;
+  * end to end: implicit values within 1e-4 of max|f|, iso-value within 1e-5
+    relative, symmetric Hausdorff distance <= 1e-3 of the bounding-box diagonal,
+    triangle counts within 0.5 %.
+"""
+import numpy as np
+import pytest
+
+from conftest import sphere
+
+pytestmark = pytest.mark.gpu
+
+
+def _torus(n, seed=0):
+    from poissonrecon_gpu_gb300 import shapes
+    return shapes.torus(n, seed=seed)
+
+
+NODE_FIELDS = ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum", "point_node")
+
+
+@pytest.fixture(scope="module", params=[("sphere", 5000, 6), ("torus", 30000, 7)], ids=["sphere5k-d6", "torus30k-d7"])
+def staged(request, lib_built, oracle_mod):
+    import poissonrecon_gpu_gb300 as pg
+    kind, n, depth = request.param
+    xyz, nrm = sphere(n, seed=2) if kind == "sphere" else _torus(n, seed=2)
+    g = pg.Reconstructor(depth=depth)
+    o = oracle_mod.Oracle(depth)
+    g.set_points(xyz, nrm)
+    o.set_points(xyz, nrm)
+    g.build_octree()
+    o.build_octree()
+    st = {"g": g, "o": o, "depth": depth, "xyz": xyz}
+    yield st
+    g.close()
+
+
+def test_octree_bit_exact(staged):
+    g, o = staged["g"], staged["o"]
+    assert np.array_equal(g.get("base"), o.get("base"))
+    assert np.array_equal(g.get("count"), o.get("count"))
+    for f in NODE_FIELDS:
+        assert np.array_equal(g.get(f), o.get(f)), f
+    assert np.array_equal(g.get("points"), o.get("points"))
+    assert np.array_equal(g.get("normals"), o.get("normals"))
+    assert np.array_equal(g.get("sort_idx").astype(np.int64), o.get("sort_idx"))
+    assert np.array_equal(g.get("center"), o.get("center"))
+    assert np.array_equal(g.get("scale"), o.get("scale"))
+
+
+def test_basis_tables_and_vector_field(staged):
+    g, o = staged["g"], staged["o"]
+    g.compute_rhs()
+    o.build_basis(True)
+    o.vector_field()
+    for t in ("dot", "ddot", "d2dot"):
+        assert np.array_equal(g.get(t), o.get(t)), t
+    assert np.array_equal(g.get("stencil"), o.get("stencil"))
+    assert np.array_equal(g.get("vfield"), o.get("vfield"))
+
+
+def test_divergence(staged):
+    g, o = staged["g"], staged["o"]
+    o.divergence()
+    a, b = g.get("divergence"), o.get("divergence")
+    base, D = o.get("base"), staged["depth"]
+    fine = slice(base[D - 1], base[D + 1])
+    assert np.array_equal(a[fine], b[fine])
+    coarse = slice(0, base[D - 1])
+    ulp = np.spacing(np.abs(b[coarse]).astype(np.float32))
+    assert np.all(np.abs(a[coarse] - b[coarse]) <= 2 * ulp)
+
+
+def test_solve(staged):
+    g, o = staged["g"], staged["o"]
+    o.set_f32("divergence", g.get("divergence"))
+    o.solve(0, 1e-5, 10000)
+    g.solve()
+    xg, xo = g.get("x"), o.get("x")
+    base, D = o.get("base"), staged["depth"]
+    for d in range(D + 1):
+        sl = slice(base[d], base[d + 1])
+        scale = max(np.abs(xo[sl]).max(), 1e-30)
+        assert np.abs(xg[sl] - xo[sl]).max() <= 1e-4 * scale, d
+    assert np.all(np.abs(g.get("cg_iters") - o.get("cg_iters")) <= 3)
+    assert np.all(g.get("cg_rr") <= np.float32(1e-5) * np.float32(1e-5))
+
+
+def test_point_values_bit_exact(staged):
+    g, o = staged["g"], staged["o"]
+    g.set("x", o.get("x"))
+    iso_g = g.eval_points()
+    o.point_values()
+    assert np.array_equal(g.get("point_value"), o.get("point_value"))
+    iso_o = float(o.get("iso")[0])
+    assert abs(iso_g - iso_o) <= 1e-6 * abs(iso_o)
+
+
+def test_mesh_matches_oracle(staged):
+    g, o = staged["g"], staged["o"]
+    g.set("iso", np.float32([o.get("iso")[0]]))
+    g.extract_mesh()
+    o.marching_cubes()
+    assert np.array_equal(g.get("has_tri"), o.get("has_tri")[: len(g.get("has_tri"))])
+    assert np.array_equal(g.get("has_int"), o.get("has_int")[: len(g.get("has_int"))])
+    assert int(g.get("subdivide_roots")[0]) == int(o.get("subdivide_roots")[0])
+    gv, gf = g.mesh()
+    ov = o.get("mesh_v").reshape(-1, 3)
+    of = o.get("mesh_f").reshape(-1, 3)
+    c, s = o.get("center"), o.get("scale")[0]
+    ov = (ov * s).astype(np.float32) + c
+    assert len(gf) == len(of)
+    # same triangles, compared as sets of vertex coordinates
+    tg = np.sort(gv[gf].reshape(len(gf), 9).view([("", np.float32)] * 9).ravel())
+    to = np.sort(ov[of].reshape(len(of), 9).astype(np.float32).view([("", np.float32)] * 9).ravel())
+    assert np.array_equal(tg, to)
+
+
+def _hausdorff(a, b):
+    from scipy.spatial import cKDTree
+    return max(cKDTree(b).query(a)[0].max(), cKDTree(a).query(b)[0].max())
+
+
+@pytest.mark.parametrize("n,depth", [(50000, 8)], ids=["sphere50k-d8"])
+def test_end_to_end(lib_built, oracle_mod, n, depth):
+    """Config 1 through both paths, each on its own (no shared intermediates)."""
+    import poissonrecon_gpu_gb300 as pg
+    xyz, nrm = sphere(n, seed=0)
+    g = pg.Reconstructor(depth=depth)
+    gv, gf = g.reconstruct(xyz, nrm)
+    o = oracle_mod.Oracle(depth)
+    o.set_points(xyz, nrm)
+    o.reconstruct()
+    for f in NODE_FIELDS:
+        assert np.array_equal(g.get(f), o.get(f)), f
+    fo = o.get("point_value")
+    fg = g.get("point_value")
+    assert np.abs(fg - fo).max() <= 1e-4 * np.abs(fo).max()
+    iso_o = float(o.get("iso")[0])
+    assert abs(float(g.get("iso")[0]) - iso_o) <= 1e-5 * abs(iso_o)
+    ov = o.get("mesh_v").reshape(-1, 3) * o.get("scale")[0] + o.get("center")
+    of = o.get("mesh_f").reshape(-1, 3)
+    assert abs(len(gf) - len(of)) <= 0.005 * len(of)
+    diag = np.linalg.norm(xyz.max(0) - xyz.min(0))
+    assert _hausdorff(gv[np.unique(gf)], ov[np.unique(of)]) <= 1e-3 * diag
+    g.close()
+
+
+def test_small_and_invalid_inputs(lib_built, oracle_mod):
+    import poissonrecon_gpu_gb300 as pg
+    xyz, nrm = sphere(40, seed=5)
+    g = pg.Reconstructor(depth=4)
+    v, f = g.reconstruct(xyz, nrm)
+    o = oracle_mod.Oracle(4, threads=1)
+    o.set_points(xyz, nrm)
+    o.reconstruct()
+    for fld in NODE_FIELDS:
+        assert np.array_equal(g.get(fld), o.get(fld)), fld
+    assert len(f) == len(o.get("mesh_f")) // 3
+    # empty input and out-of-order calls are rejected, the context stays usable
+    with pytest.raises(pg.PrgpuError):
+        g.set_points(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32))
+    h = pg.Reconstructor(depth=5)
+    with pytest.raises(pg.PrgpuError):
+        h.solve(allow_not_converged=False)
+    v2, f2 = g.reconstruct(xyz, nrm)
+    assert np.array_equal(f, f2) and np.array_equal(v, v2)
+    g.close()
+    h.close()
+
+
+def test_cg_csr_matches_dense_solve(lib_built):
+    torch = pytest.importorskip("torch")
+    import poissonrecon_gpu_gb300 as pg
+    n = 3000
+    rng = np.random.default_rng(0)
+    # SPD: 1-D Laplacian plus a positive diagonal
+    rows, cols, vals = [], [], []
+    for i in range(n):
+        for j, v in ((i - 1, -1.0), (i, 2.5), (i + 1, -1.0)):
+            if 0 <= j < n:
+                rows.append(i); cols.append(j); vals.append(v)
+    rowptr = np.searchsorted(rows, np.arange(n + 1)).astype(np.int32)
+    b = rng.standard_normal(n).astype(np.float32)
+    dev = torch.device("cuda:0")
+    tI = torch.tensor(rowptr, device=dev)
+    tJ = torch.tensor(np.array(cols, np.int32), device=dev)
+    tV = torch.tensor(np.array(vals, np.float32), device=dev)
+    tb = torch.tensor(b, device=dev)
+    tx = torch.zeros(n, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    ms, it = pg.solverCG_DeviceToDevice(n, len(vals), tI.data_ptr(), tJ.data_ptr(), tV.data_ptr(),
+                                        tb.data_ptr(), tx.data_ptr(), 1e-5, 10000)
+    A = np.zeros((n, n))
+    A[rows, cols] = vals
+    x = np.linalg.solve(A, b.astype(np.float64))
+    assert it > 0 and ms > 0
+    assert np.abs(tx.cpu().numpy() - x).max() <= 1e-4 * np.abs(x).max()

@@ -1,0 +1,80 @@
+"""Properties of the oracle's restatement on small inputs (CPU only)."""
+import numpy as np
+import pytest
+
+from conftest import sphere
+
+
+@pytest.fixture(scope="module")
+def small(oracle_mod):
+    xyz, nrm = sphere(4000, seed=1)
+    o = oracle_mod.Oracle(6, threads=4)
+    o.set_points(xyz, nrm)
+    o.reconstruct()
+    return o, xyz, nrm
+
+
+def test_octree_invariants(small):
+    o, xyz, _ = small
+    base, count = o.get("base"), o.get("count")
+    M = base[-1]
+    key, parent, children = o.get("key"), o.get("parent"), o.get("children").reshape(-1, 8)
+    pidx, pnum, neighs = o.get("pidx"), o.get("pnum"), o.get("neighs").reshape(-1, 27)
+    D = len(count) - 1
+    assert count[0] == 1 and all(c % 8 == 0 for c in count[1:])
+    assert pnum[0] == len(xyz)
+    for d in range(1, D + 1):
+        lo, hi = base[d], base[d + 1]
+        par = parent[lo:hi]
+        # every slot's parent lies one depth up and lists it as a child
+        assert np.all((par >= base[d - 1]) & (par < base[d]))
+        k = np.arange(lo, hi)
+        son = (key[lo:hi] >> (3 * (D - d))) & 7
+        assert np.array_equal(children[par, son], k)
+        # point ranges of the 8 siblings tile the parent's range
+        g = pnum[lo:hi].reshape(-1, 8).sum(1)
+        assert np.array_equal(g, pnum[par[::8]])
+    # neighbour 13 is the node itself; neighbour relation is symmetric
+    assert np.array_equal(neighs[:, 13], np.arange(M))
+    for j in range(27):
+        nb = neighs[:, j]
+        ok = nb >= 0
+        assert np.array_equal(neighs[nb[ok], 26 - j], np.nonzero(ok)[0])
+
+
+def test_solver_meets_reference_schedule(small):
+    o, _, _ = small
+    it = o.get("cg_iters")
+    rr = o.get("cg_rr")
+    assert np.all(it < 10000)
+    assert np.all(rr <= np.float32(1e-5) * np.float32(1e-5))
+
+
+def test_mesh_lies_on_sphere(small):
+    o, xyz, _ = small
+    v = o.get("mesh_v").reshape(-1, 3)
+    f = o.get("mesh_f").reshape(-1, 3)
+    assert len(f) > 1000
+    used = np.unique(f)
+    c, s = o.get("center"), o.get("scale")[0]
+    r = np.linalg.norm(v[used] * s + c - 0.5, axis=1)
+    assert abs(r.mean() - 0.35) < 0.005
+    assert r.min() > 0.3 and r.max() < 0.4
+
+
+def test_duplicate_points_share_leaves(oracle_mod):
+    """Repeated samples land in the same leaf; point ranges still tile the input."""
+    xyz, nrm = sphere(500, seed=4)
+    xyz2 = np.concatenate([xyz, xyz[:200]])
+    nrm2 = np.concatenate([nrm, nrm[:200]])
+    o = oracle_mod.Oracle(5, threads=2)
+    o.set_points(xyz2, nrm2)
+    o.build_octree()
+    base, pnum, pidx = o.get("base"), o.get("pnum"), o.get("pidx")
+    D = 5
+    leaf = slice(base[D], base[D + 1])
+    assert pnum[leaf].sum() == len(xyz2)
+    nz = pnum[leaf] > 0
+    starts = pidx[leaf][nz]
+    assert np.all(np.diff(starts) > 0)
+    assert np.array_equal(np.sort(o.get("sort_idx")), np.arange(len(xyz2)))
