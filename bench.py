@@ -1,0 +1,269 @@
+"""Benchmark: end-to-end Poisson reconstruction throughput (points/s) on GB300.
+
+Workload (default): the precision-study configuration -- 1,000,000 seeded
+synthetic points on a torus (R=0.3, r=0.1, density 1+7x, position noise
+sigma=0.001, von Mises-Fisher normal noise kappa=500), maxDepth 10, per-depth CG
+to relative residual 1e-6 with FP64 reductions.  One step is one complete
+reconstruction: normalise, octree, tables, splat, divergence, solve, implicit
+values + iso-value, marching cubes with subdivision, mesh to host.
+
+  value : points/s with the input already resident in HBM (prgpu_set_points_device)
+  e2e   : points/s through prgpu_reconstruct with pinned host buffers, host->device
+          copy of the points and device->host copy of the mesh inside the timed region
+Timing: CUDA events on the library's stream, per step, L2 flushed (256 MiB
+write) between steps; clocks sampled with nvidia-smi during the timed steps.
+
+--impl reference runs the reference path on the host cores: the CPU oracle
+(oracle/oracle.cpp, a restatement of the reference pipeline, OpenMP) on a
+bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+CPU_SAMPLE_POINTS = 50_000     # bounded CPU sample of the 1M-point workload
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="prgpu", choices=["prgpu", "reference"])
+    ap.add_argument("--points", type=int, default=1_000_000)
+    ap.add_argument("--depth", type=int, default=10)
+    ap.add_argument("--tol", type=float, default=1e-6)
+    return ap.parse_args()
+
+
+def workload(n):
+    from poissonrecon_gpu_gb300 import shapes
+    return shapes.torus(n, seed=0)
+
+
+def config(args, l2):
+    return {"workload": "torus %d points, maxDepth %d, CG to relative residual %g" % (args.points, args.depth, args.tol),
+            "points": args.points, "depth": args.depth, "solve": "per-depth CG, rel residual %g, FP64 dots" % args.tol,
+            "l2": l2, "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference(args, steps, warmup):
+    """The reference path on the host cores: the oracle on a bounded sample."""
+    import oracle
+    oracle.build()
+    xyz, nrm = workload(args.points)
+    rng = np.random.default_rng(1)
+    pick = np.sort(rng.choice(len(xyz), size=min(CPU_SAMPLE_POINTS, len(xyz)), replace=False))
+    sx, sn = xyz[pick], nrm[pick]
+    threads = os.cpu_count() or 1
+    times = []
+    for it in range(warmup + steps):
+        o = oracle.Oracle(args.depth, threads=threads)
+        o.set_points(sx, sn)
+        t = time.perf_counter()
+        o.reconstruct(1, args.tol, 10000)
+        dt = time.perf_counter() - t
+        if it >= warmup:
+            times.append(dt)
+        del o
+    per = float(np.mean(times))
+    return {"value": len(sx) / per, "unit": "points/s", "cores": threads, "kind": "port",
+            "sample": "CPU oracle (OpenMP restatement of the reference pipeline) on a seeded %d-point subsample of "
+                      "the same torus at maxDepth %d, same solver schedule; %.2f s per reconstruction"
+                      % (len(sx), args.depth, per)}, per
+
+
+def roofline(stats, peaks):
+    ks = stats.get("kernels", {})
+    if not ks:
+        return None
+    name, k = max(ks.items(), key=lambda kv: kv[1]["ms"])
+    per_launch_ms = k["ms"] / max(k["launches"], 1)
+    bytes_per_launch = k["bytes"] / max(k["launches"], 1)
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+            "launch_ms": round(per_launch_ms, 4), "algorithmic_bytes_per_launch": bytes_per_launch}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cpu, per = cpu_reference(args, args.steps, args.warmup)
+        out = {"metric": "points/s end-to-end", "value": cpu["value"], "unit": "points/s", "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": config(args, "n/a (host)"), "impl": "reference", "cpu_baseline": cpu,
+               "e2e": {"value": cpu["value"], "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    import torch
+    import poissonrecon_gpu_gb300 as pg
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+
+    xyz, nrm = workload(args.points)
+    n = len(xyz)
+    h_xyz = torch.from_numpy(xyz).pin_memory()
+    h_nrm = torch.from_numpy(nrm).pin_memory()
+    d_xyz = h_xyz.to(dev)
+    d_nrm = h_nrm.to(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MiB > L2
+
+    r = pg.Reconstructor(depth=args.depth, solve_mode=pg.SOLVE_RELATIVE, cg_tol=args.tol, cg_max_iter=10000,
+                         device=local)
+    stream = torch.cuda.ExternalStream(r.stream(), device=dev)
+
+    def device_step():
+        r.set_points_device(d_xyz.data_ptr(), d_nrm.data_ptr(), n)
+        r.build_octree()
+        r.compute_rhs()
+        r.solve()
+        r.eval_points()
+        r.extract_mesh()
+
+    def host_step():
+        m = pg.Mesh()
+        rc = pg._lib().prgpu_reconstruct(r._h, h_xyz.data_ptr(), h_nrm.data_ptr(), n, ctypes.byref(m))
+        if rc not in (0, 5):
+            raise pg.PrgpuError(rc, "prgpu_reconstruct")
+        return m.n_vertices, m.n_triangles
+
+    def timed(step, k):
+        ms = []
+        for _ in range(k):
+            flush.fill_(1.0)
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = step()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms, out
+
+    for _ in range(args.warmup):
+        device_step()
+        host_step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+
+    launches0 = pg.kernel_launches()
+    r.set_profiling(True)
+    with Clocks(os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else ".",
+                             "bench_clocks.csv")) as clk:
+        dev_ms, _ = timed(device_step, args.steps)
+        stats = r.stats()
+        r.set_profiling(False)
+        e2e_ms, (nv, nt) = timed(host_step, args.steps)
+    launches = pg.kernel_launches() - launches0
+    torch.cuda.synchronize(dev)
+    t_dev = float(np.mean(dev_ms))
+    t_e2e = float(np.mean(e2e_ms))
+    if world > 1:
+        t = torch.tensor([t_dev, t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev, t_e2e = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    out = {
+        "metric": "points/s end-to-end", "value": n * world / (t_dev * 1e-3), "unit": "points/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config(args, "flushed between steps (256 MiB write)"),
+        "e2e": {"value": n * world / (t_e2e * 1e-3), "unit": "points/s", "ms_per_step": t_e2e,
+                "h2d_bytes_per_step": int(24 * n), "d2h_bytes_per_step": int(12 * nv + 12 * nt)},
+        "gpu_launches": int(launches),
+        "roofline": roofline(stats, peaks),
+        "clocks": clk.summary(),
+        "stages_ms": stats.get("ms"),
+        "cg_iters": stats.get("cg_iters"),
+        "kernels": stats.get("kernels"),
+        "mesh": {"vertices": nv, "triangles": nt},
+    }
+    if os.environ.get("PRGPU_BENCH_NO_CPU") != "1":
+        cpu, _ = cpu_reference(args, 1, 0)
+        out["cpu_baseline"] = cpu
+    print(json.dumps(out))
+    r.close()
+
+
+if __name__ == "__main__":
+    main()

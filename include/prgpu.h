@@ -110,6 +110,11 @@ int prgpu_set_array(void* ctx, const char* name, const void* src, int64_t bytes)
 /* Per-stage device times, counts and solver statistics as one JSON object. */
 int prgpu_stats_json(void* ctx, char* buf, int64_t len);
 
+/* Per-kernel timing: when enabled, the main kernels are bracketed by CUDA
+ * events on the context stream and their times, launch counts and algorithmic
+ * byte counts appear under "kernels" in prgpu_stats_json.  Enabling resets them. */
+int prgpu_set_profiling(void* ctx, int32_t enable);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own
  * work or timing events after the library's. */
 int prgpu_get_stream(void* ctx, void** stream);

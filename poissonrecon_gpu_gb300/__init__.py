@@ -80,6 +80,7 @@ SIGNATURES = {
     "prgpu_stats_json": (ctypes.c_int, [_VP, ctypes.c_char_p, _I64]),
     "prgpu_last_error": (ctypes.c_char_p, []),
     "prgpu_get_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "prgpu_set_profiling": (ctypes.c_int, [_VP, _I32]),
     "prgpu_kernel_launches": (ctypes.c_int64, []),
     "prgpu_cg_csr": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32,
                                     ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_float)]),
@@ -202,6 +203,9 @@ class Reconstructor:
     def set(self, name: str, arr):
         a = _f32(arr).ravel()
         _check(_lib().prgpu_set_array(self._h, name.encode(), a.ctypes.data, a.nbytes), "prgpu_set_array(%s)" % name)
+
+    def set_profiling(self, enable: bool = True):
+        _check(_lib().prgpu_set_profiling(self._h, int(enable)), "prgpu_set_profiling")
 
     def stream(self) -> int:
         st = _VP()

@@ -35,6 +35,49 @@ void Ctx::free_all() {
     dfree(d_cg_iters, s); dfree(d_cg_rr, s);
 }
 
+int Ctx::kbegin(const char* name, double bytes) {
+    if (!profile) return -1;
+    int slot = -1;
+    for (size_t k = 0; k < ktimers.size(); ++k)
+        if (ktimers[k].name == name) slot = (int)k;
+    if (slot < 0) {
+        ktimers.push_back(KernelTimer());
+        ktimers.back().name = name;
+        slot = (int)ktimers.size() - 1;
+    }
+    while (kevents.size() < kev_next + 2) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        kevents.push_back(e);
+    }
+    PendingTimer pt;
+    pt.slot = slot;
+    pt.a = kevents[kev_next++];
+    pt.b = kevents[kev_next++];
+    pt.bytes = bytes;
+    CK(cudaEventRecord(pt.a, stream));
+    kpending.push_back(pt);
+    return (int)kpending.size() - 1;
+}
+void Ctx::kend(int h) {
+    if (h < 0) return;
+    CK(cudaEventRecord(kpending[h].b, stream));
+}
+void Ctx::kflush() {
+    if (kpending.empty()) return;
+    CK(cudaStreamSynchronize(stream));
+    for (auto& p : kpending) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, p.a, p.b));
+        KernelTimer& t = ktimers[p.slot];
+        t.ms += ms;
+        t.launches += 1;
+        t.bytes += p.bytes;
+    }
+    kpending.clear();
+    kev_next = 0;
+}
+
 int cg_csr_impl(int n, const int* rowptr, const int* col, const float* val, const float* rhs, float* x, float tol,
                 int max_iter, int* iters, float* ms);
 
@@ -45,6 +88,7 @@ static void timed(Ctx& c, float& acc, F&& f) {
     f();
     CK(cudaEventRecord(c.ev1, c.stream));
     CK(cudaEventSynchronize(c.ev1));
+    c.kflush();
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
     acc = ms;
@@ -115,6 +159,7 @@ int prgpu_destroy(void* h) {
     CK(cudaSetDevice(c->device));
     c->free_all();
     CK(cudaStreamSynchronize(c->stream));
+    for (auto e : c->kevents) cudaEventDestroy(e);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
     cudaStreamDestroy(c->stream);
@@ -391,7 +436,15 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
         snprintf(tmp, sizeof tmp, "%s%lld", d ? "," : "", (long long)c->count[d]);
         js += tmp;
     }
-    js += "],\"cg_iters\":[";
+    js += "],\"roots_per_depth\":[";
+    for (size_t d = 0; d < c->roots_per_depth.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%lld", d ? "," : "", (long long)c->roots_per_depth[d]);
+        js += tmp;
+    }
+    snprintf(tmp, sizeof tmp, "],\"virtual_cells\":%lld,\"kernel_launches\":%llu", (long long)c->virtual_cells,
+             (unsigned long long)g_kernel_launches);
+    js += tmp;
+    js += ",\"cg_iters\":[";
     for (size_t d = 0; d < c->cg_iters.size(); ++d) {
         snprintf(tmp, sizeof tmp, "%s%d", d ? "," : "", c->cg_iters[d]);
         js += tmp;
@@ -402,12 +455,28 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
              c->t.octree_ms, c->t.basis_ms, c->t.splat_ms, c->t.divergence_ms, c->t.solve_ms, c->t.iso_ms,
              c->t.mesh_ms);
     js += tmp;
+    js += "\"kernels\":{";
+    for (size_t k = 0; k < c->ktimers.size(); ++k) {
+        const KernelTimer& t = c->ktimers[k];
+        snprintf(tmp, sizeof tmp, "%s\"%s\":{\"ms\":%.5f,\"launches\":%lld,\"bytes\":%.6g}", k ? "," : "",
+                 t.name.c_str(), t.ms, t.launches, t.bytes);
+        js += tmp;
+    }
+    js += "},";
     snprintf(tmp, sizeof tmp, "\"iso\":%.9g,\"vertices\":%lld,\"triangles\":%lld,\"subdivide_roots\":%lld}",
              (double)c->iso, (long long)c->mesh_v.size() / 3, (long long)c->mesh_f.size() / 3,
              (long long)c->subdivide_roots);
     js += tmp;
     if ((int64_t)js.size() + 1 > len) return PRGPU_ERR_ARG;
     memcpy(buf, js.c_str(), js.size() + 1);
+    return PRGPU_OK;
+}
+
+int prgpu_set_profiling(void* h, int32_t enable) {
+    Ctx* c = as_ctx(h);
+    if (!c) return PRGPU_ERR_ARG;
+    c->profile = enable != 0;
+    c->ktimers.clear();
     return PRGPU_OK;
 }
 

@@ -21,6 +21,20 @@ struct NodeArrays {
     int* neigh = nullptr;    // 27 x M, neighbour j of node i at neigh[j*M + i]
 };
 
+// per-kernel device time with CUDA events on the context stream, and the
+// kernel's algorithmic (compulsory) byte count per launch
+struct KernelTimer {
+    std::string name;
+    double ms = 0;
+    long long launches = 0;
+    double bytes = 0;
+};
+struct PendingTimer {
+    int slot;
+    cudaEvent_t a, b;
+    double bytes;
+};
+
 struct StageTimes {
     float octree_ms = 0, basis_ms = 0, splat_ms = 0, divergence_ms = 0, solve_ms = 0, iso_ms = 0, mesh_ms = 0;
 };
@@ -75,8 +89,18 @@ struct Ctx {
     std::vector<int> has_tri, has_int;
     i64 subdivide_roots = 0;
     std::vector<i64> batch_tri;
+    std::vector<i64> roots_per_depth;   // subdivided leaves by depth
+    i64 virtual_cells = 0;
 
     StageTimes t;
+    bool profile = false;
+    std::vector<KernelTimer> ktimers;
+    std::vector<PendingTimer> kpending;
+    std::vector<cudaEvent_t> kevents;   // pool
+    size_t kev_next = 0;
+    int kbegin(const char* name, double bytes);   // returns a handle for kend, -1 when not profiling
+    void kend(int handle);
+    void kflush();                                // after a stream sync
     int stage = 0;   // 0 none, 1 points, 2 octree, 3 rhs, 4 solved, 5 iso, 6 mesh
     i64 kernel_launches = 0;
 

@@ -128,8 +128,10 @@ void stage_points(Ctx& c) {
     double* sum = dalloc<double>(1, s);
     CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
     EvalArgs a{c.nodes, c.D, c.basis, c.x};
+    const int kt = c.kbegin("point_values", (double)c.N * (12 + 4 + 4) + (double)c.nodes.M * (4 + 4 + 8 + 108));
     k_point_values<<<grid_for(c.N, 128, 1ll << 30), 128, 0, s>>>(a, c.pts, c.point_node, c.N, c.point_value, sum);
     CK_LAUNCH();
+    c.kend(kt);
     double h = read_scalar(sum, s);
     dfree(sum, s);
     c.iso = (float)h / (float)c.N;
@@ -355,6 +357,14 @@ __device__ float virtual_corner_value(const VArgs& v, int L, int r, const int oc
         const int sh = D - d;
         const int V[3] = {oc[0] >> sh, oc[1] >> sh, oc[2] >> sh};
         const int fb = (1 << d) - 1, lim = 1 << d;
+        // a virtual cell whose 3x3x3 block lies inside the leaf has no real neighbour
+        const int span = 1 << (d - r);
+        bool inner = true;
+        for (int ax = 0; ax < 3; ++ax) {
+            const int lo = Lc[ax] * span;
+            if (V[ax] - 1 < lo || V[ax] + 1 >= lo + span) inner = false;
+        }
+        if (inner) continue;
         float bv[3][3];
         for (int ax = 0; ax < 3; ++ax)
             for (int t = 0; t < 3; ++t) {
@@ -639,10 +649,14 @@ void stage_mesh(Ctx& c) {
     float* cell_v = dalloc<float>(8 * nD, s);
     unsigned char* cat = dalloc<unsigned char>(nD, s);
     int* ntri = dalloc<int>(nD, s);
+    int kt = c.kbegin("corner_values", (double)M * (108 + 8 + 4 + 4) + (double)nD * 8 * 4);
     k_finest_corner_values<<<grid_for(nD, 128, 1ll << 30), 128, 0, s>>>(ea, lo, M, c.iso, cval);
     CK_LAUNCH();
+    c.kend(kt);
+    kt = c.kbegin("cells", (double)nD * (8 * 4 + 108 + 8 * 4 + 1 + 4));
     k_finest_cells<<<grid_for(nD, 128, 1ll << 30), 128, 0, s>>>(nd, lo, M, cval, cell_v, cat, ntri);
     CK_LAUNCH();
+    c.kend(kt);
     dfree(cval, s);
     // ---- face marks and subdivision roots
     int* fflag = dalloc<int>(6 * M, s);
@@ -657,9 +671,11 @@ void stage_mesh(Ctx& c) {
     CK(cudaMemsetAsync(has_int, 0, nCoarse * sizeof(int), s));
     CK(cudaMemsetAsync(is_root, 0, nCoarse * sizeof(int), s));
     if (nCoarse > 1) {
+        const int kc = c.kbegin("coarse_leaves", (double)nCoarse * (4 + 108 + 8 + 3 * 4) + (double)M * 4);
         k_coarse_leaves<<<grid_for(nCoarse - 1, 128, 1ll << 30), 128, 0, s>>>(ea, 1, nCoarse, c.iso, fflag, has_tri,
                                                                              has_int, is_root);
         CK_LAUNCH();
+        c.kend(kc);
     }
     dfree(fflag, s);
     c.has_tri.assign(nCoarse, 0);
@@ -696,6 +712,8 @@ void stage_mesh(Ctx& c) {
         roots.push_back(R);
     }
     c.subdivide_roots = (i64)roots.size();
+    c.roots_per_depth.assign(D + 1, 0);
+    for (auto& R : roots) c.roots_per_depth[R.depth]++;
     const int nbatches = nb + 1;
     // ---- real cells: active list, triangle bases
     int* flags = dalloc<int>(std::max<i64>(nD, 1), s);
@@ -754,13 +772,17 @@ void stage_mesh(Ctx& c) {
         va.roots = droots;
         va.batch_root_flag = bflag;
         lat = dalloc<float>(total_lat, s);
+        const int kv = c.kbegin("virtual_corners", (double)total_lat * 4);
         k_virtual_corners<<<grid_for(total_lat, 128, 1ll << 30), 128, 0, s>>>(va, lat_prefix, total_lat, lat);
         CK_LAUNCH();
+        c.kend(kv);
         vcat = dalloc<unsigned char>(total_cells, s);
         vntri = dalloc<int>(total_cells, s);
+        const int kc2 = c.kbegin("virtual_cells", (double)total_lat * 4 + (double)total_cells * 5);
         k_virtual_cells<<<grid_for(total_cells, 256, 1ll << 30), 256, 0, s>>>(va, cell_prefix, lat_prefix, total_cells,
                                                                               lat, vcat, vntri);
         CK_LAUNCH();
+        c.kend(kc2);
         int* vf = dalloc<int>(total_cells, s);
         int* vp = dalloc<int>(total_cells + 1, s);
         k_active_flags<<<grid_for(total_cells, 256), 256, 0, s>>>(vntri, total_cells, vf);
@@ -780,6 +802,7 @@ void stage_mesh(Ctx& c) {
         dfree(tmp, s);
         ntri_virt = read_scalar(tri_virt + nact_virt, s);
     }
+    c.virtual_cells = total_cells;
     // ---- emission, sort, vertex ids
     const i64 ntri_all = ntri_real + ntri_virt;
     const i64 nem = 3 * ntri_all;
@@ -820,7 +843,9 @@ void stage_mesh(Ctx& c) {
         }
         u64* ktmp = dalloc<u64>(nem, s);
         uint32_t* stmp = dalloc<uint32_t>(nem, s);
+        const int ks = c.kbegin("edge_sort", (double)nem * 12 * 2);
         radix_sort_pairs(em.keys, em.slot, ktmp, stmp, nem, local_bits + batch_bits, s);
+        c.kend(ks);
         dfree(ktmp, s);
         dfree(stmp, s);
         int* hf = dalloc<int>(nem, s);

@@ -293,7 +293,9 @@ void stage_octree(Ctx& c) {
     k_normalise_encode<<<grid_for(N, 256), 256, 0, s>>>(c.in_xyz, c.in_nrm, N, c.center[0], c.center[1], c.center[2],
                                                          c.scale, (float)(2 << D), D, ptmp, ntmp, keys, idx);
     CK_LAUNCH();
+    const int ks = c.kbegin("point_sort", (double)N * 12 * 2);
     radix_sort_pairs(keys, idx, ktmp, itmp, N, 3 * D, s);
+    c.kend(ks);
     dfree(ktmp, s);
     dfree(itmp, s);
     dfree(c.pts, s); dfree(c.nrm, s); dfree(c.sort_idx, s);
@@ -401,10 +403,12 @@ void stage_octree(Ctx& c) {
         CK_LAUNCH();
     }
     // ---- neighbours, top-down
+    const int kn = c.kbegin("neighbours", (double)M * (108 + 8 + 4 + 4));
     for (int d = 1; d <= D; ++d) {
         k_neighbours<<<grid_for(c.count[d], 256), 256, 0, s>>>(nd, c.base[d], c.base[d + 1], 3 * (D - d));
         CK_LAUNCH();
     }
+    c.kend(kn);
     // ---- point -> leaf
     dfree(c.point_node, s);
     c.point_node = dalloc<int>(N, s);

@@ -155,9 +155,12 @@ void stage_splat(Ctx& c) {
     const i64 lo = c.base[D], hi = c.base[D + 1];
     dfree(c.vfield, s);
     c.vfield = dalloc<float>(3 * (hi - lo), s);
+    // compulsory: points+normals once, finest keys and neighbour tables, V written
+    const int kt = c.kbegin("splat", (double)c.N * 24 + (double)(hi - lo) * (8 + 108 + 12));
     k_splat<<<grid_for(hi - lo, 128, 1ll << 30), 128, 0, s>>>(c.nodes, lo, hi, D, c.basis_maxdepth, c.pts, c.nrm,
                                                                c.vfield);
     CK_LAUNCH();
+    c.kend(kt);
 }
 
 void stage_divergence(Ctx& c) {
@@ -180,6 +183,8 @@ void stage_divergence(Ctx& c) {
     a.row_start = rs;
     // depths D and D-1: at most 27 and 216 terms per node
     const int split = D >= 1 ? D - 1 : 0;
+    // compulsory: every node's key, depth, neighbours and b; V and coordinates of the finest slots
+    const int kt = c.kbegin("divergence", (double)M * (8 + 1 + 108 + 4) + (double)nD * (12 + 8));
     k_div_thread<<<grid_for(M - c.base[split], 128, 1ll << 30), 128, 0, s>>>(c.nodes, a, c.base[split], M,
                                                                              c.divergence);
     CK_LAUNCH();
@@ -187,6 +192,7 @@ void stage_divergence(Ctx& c) {
         k_div_block<<<(unsigned)c.base[split], DIV_BLOCK, 0, s>>>(c.nodes, a, 0, c.divergence);
         CK_LAUNCH();
     }
+    c.kend(kt);
     dfree(fc, s);
     dfree(rs, s);
 }

@@ -283,8 +283,10 @@ void stage_solve(Ctx& c) {
     a.state = st;
     a.err = err;
     void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
+    const int kt = c.kbegin("cg", 0.0);
     CK(cudaLaunchCooperativeKernel((void*)k_cg_all, dim3((unsigned)block_depth.size()), dim3(CG_BLOCK), kargs, 0, s));
     ++g_kernel_launches;
+    c.kend(kt);
     std::vector<PartState> hs(D + 1);
     int herr = 0;
     CK(cudaMemcpyAsync(hs.data(), st, (D + 1) * sizeof(PartState), cudaMemcpyDeviceToHost, s));
@@ -293,6 +295,13 @@ void stage_solve(Ctx& c) {
     c.cg_iters.assign(D + 1, 0);
     c.cg_rr.assign(D + 1, 0.f);
     for (int d = 0; d <= D; ++d) { c.cg_iters[d] = hs[d].iters; c.cg_rr[d] = hs[d].rr; }
+    if (kt >= 0) {
+        // compulsory per row and iteration: 27 neighbour indices, p gathered once, p/q/x/r
+        // streams (read p,r,q,x; write p,q,x,r: 7 words)
+        double bytes = 0;
+        for (int d = 0; d <= D; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (108.0 + 7 * 4);
+        c.kpending[kt].bytes = bytes;
+    }
     dfree(r, s); dfree(p, s); dfree(q, s);
     dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(err, s);
     if (herr) {
