@@ -133,6 +133,21 @@ int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* 
                  const float* d_val, const float* d_rhs, float* d_x, float tol, int32_t max_iter,
                  int32_t* iters, float* kernel_ms);
 
+/* The same solver for callers that cannot allocate device memory at solve time
+ * (a framework's caching allocator owns the device memory, cudaFree's implicit
+ * synchronisation is not affordable, or the host forbids allocation after
+ * start-up).  No counterpart in the reference.  It allocates nothing: the
+ * scratch vectors and solver state live in one static device array of the
+ * library (about 3 MiB per GPU that loads the library, held until exit), so n
+ * is limited to 262144 rows (PRGPU_ERR_LIMIT beyond).  All calls share that
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  The first call on a device looks up the array's address; make it
+ * before any stream capture.  Runs on 'stream' (a cudaStream_t, NULL = legacy
+ * default stream) and returns after the solve has finished. */
+int prgpu_cg_csr_noalloc(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* d_col,
+                         const float* d_val, const float* d_rhs, float* d_x, float tol, int32_t max_iter,
+                         void* stream, int32_t* iters);
+
 /* PLY I/O (PointStream.inl:160-239 input; PlyWriteTriangles plyfile.cu:2769-2836 output).
  * prgpu_read_points returns library-owned arrays valid until the next call. */
 int prgpu_read_points(const char* path, int64_t* n, const float** xyz, const float** nrm);

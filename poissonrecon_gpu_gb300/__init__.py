@@ -84,6 +84,8 @@ SIGNATURES = {
     "prgpu_kernel_launches": (ctypes.c_int64, []),
     "prgpu_cg_csr": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32,
                                     ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_float)]),
+    "prgpu_cg_csr_noalloc": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32, _VP,
+                                            ctypes.POINTER(_I32)]),
     "prgpu_read_points": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_I64), ctypes.POINTER(_VP),
                                          ctypes.POINTER(_VP)]),
     "prgpu_write_mesh_ply": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Mesh), _I32]),
