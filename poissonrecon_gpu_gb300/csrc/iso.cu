@@ -301,6 +301,7 @@ struct VRoot {
     int pad;
     i64 lattice_base;  // first corner value of this root
     i64 cell_base;     // first virtual cell of this root
+    i64 brick_base;    // first brick of this root, -1 for small roots (lattice edge <= 8)
 };
 
 struct VArgs {
@@ -394,18 +395,19 @@ __device__ float virtual_corner_value(const VArgs& v, int L, int r, const int oc
 
 __device__ __forceinline__ u64 cell_key_D(const int c[3], int D) { return coords_key(c[0], c[1], c[2], D, D); }
 
-// one thread per lattice corner of every root
-__global__ void k_virtual_corners(VArgs v, const i64* __restrict__ lat_prefix, i64 total, float* __restrict__ lat) {
+// one thread per lattice corner of the listed roots (the small ones)
+__global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i64* __restrict__ list_prefix,
+                                  int nlist, i64 total, const i64* __restrict__ lat_prefix, float* __restrict__ lat) {
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
-        // root by binary search over the lattice prefix
-        int lo = 0, hi = v.nroots - 1;
+        int lo = 0, hi = nlist - 1;
         while (lo < hi) {
             int mid = (lo + hi + 1) >> 1;
-            if (lat_prefix[mid] <= e) lo = mid; else hi = mid - 1;
+            if (list_prefix[mid] <= e) lo = mid; else hi = mid - 1;
         }
-        const VRoot R = v.roots[lo];
+        const int ri = list[lo];
+        const VRoot R = v.roots[ri];
         const int D = v.e.D, S = 1 << (D - R.depth), S1 = S + 1;
-        const i64 loc = e - lat_prefix[lo];
+        const i64 loc = e - list_prefix[lo];
         const int u = (int)(loc / ((i64)S1 * S1)), w = (int)((loc / S1) % S1), z = (int)(loc % S1);
         int Lc[3];
         key_coords(v.e.nd.key[R.node], R.depth, D, Lc);
@@ -420,13 +422,287 @@ __global__ void k_virtual_corners(VArgs v, const i64* __restrict__ lat_prefix, i
             const u64 kk = cell_key_D(cell, D);
             if (kk < best) { best = kk; own_root = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
         }
-        lat[e] = virtual_corner_value(v, own_root, R.depth, oc, qc) - v.iso;
+        lat[lat_prefix[ri] + loc] = virtual_corner_value(v, own_root, R.depth, oc, qc) - v.iso;
+    }
+}
+
+// ---- large subdivided leaves (lattice edge >= 16): bricks of 8^3 cells.
+//
+// Most corners of a large subdivided leaf lie far from the surface.  A brick is
+// culled when every corner value it contains provably has the same sign as
+// (value - iso) -- then none of its cells carries a triangle and its corners
+// are never read.  The proof uses the exact quantities the evaluation would
+// use: each term of a corner value is x_n * B_x(q_x) * B_y(q_y) * B_z(q_z)
+// with B the single-precision basis values, so the brick's range of each term
+// is an interval product over the brick's lattice coordinates, and the
+// difference between the FMA chain and the exact sum of its terms is at most
+// (K + 4) u sum|term| for K terms (u = 2^-24).  Terms that only some corners
+// include (neighbours of exposed virtual cells) get intervals widened to 0.
+// Bricks that touch the leaf's lower faces are not culled (their corners may
+// be owned by cells outside the leaf).  Every corner of a non-culled brick is
+// evaluated exactly as virtual_corner_value does, so culling changes no value.
+constexpr int BR = 8;              // brick edge (cells); corners per axis BR+1
+constexpr int BR_BLOCK = 128;
+
+struct VBrick {
+    int root;                      // index into roots
+    int bu, bv, bw;
+};
+struct BrickIndex {                // bricks of the large roots, numbered root by root
+    const int* big;                // root indices of the large roots
+    const i64* prefix;             // first brick of each large root
+    int nbig;
+};
+__device__ __forceinline__ VBrick brick_of(const VArgs& v, const BrickIndex& bx, i64 g) {
+    int lo = 0, hi = bx.nbig - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (bx.prefix[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    VBrick b;
+    b.root = bx.big[lo];
+    const int nb = (1 << (v.e.D - v.roots[b.root].depth)) / BR;
+    const i64 l = g - bx.prefix[lo];
+    b.bu = (int)(l / ((i64)nb * nb));
+    b.bv = (int)((l / nb) % nb);
+    b.bw = (int)(l % nb);
+    return b;
+}
+
+__device__ __forceinline__ float x_or_zero(const EvalArgs& a, int node) { return node < 0 ? 0.f : a.x[node]; }
+
+// real node at depth d with coordinates N near leaf L (depth r, coords Lc), or -1 (none, or inside L)
+__device__ i64 shell_node(const VArgs& v, int L, int r, const int Lc[3], int d, const int N[3]) {
+    const NodeArrays& nd = v.e.nd;
+    const int lim = 1 << d;
+    if (N[0] < 0 || N[1] < 0 || N[2] < 0 || N[0] >= lim || N[1] >= lim || N[2] >= lim) return -1;
+    const int s2 = d - r;
+    const int dx = (N[0] >> s2) - Lc[0], dy = (N[1] >> s2) - Lc[1], dz = (N[2] >> s2) - Lc[2];
+    if (!dx && !dy && !dz) return -1;
+    const int an = nd.neigh[(i64)(9 * (dx + 1) + 3 * (dy + 1) + (dz + 1)) * nd.M + L];
+    if (an == -1) return -1;
+    return descend(nd, an, r, d, N);
+}
+
+// min/max over the brick's lattice coordinates along one axis of basis function fi
+__device__ __forceinline__ void basis_range(const EvalArgs& a, int fi, int g0, float inv, float& mn, float& mx) {
+    mn = 3.4e38f;
+    mx = -3.4e38f;
+    for (int k = 0; k <= BR; ++k) {
+        const float q = (float)(g0 + k) * inv;
+        const float b = cpoly_value<3>(a.basis[fi], q);
+        mn = fminf(mn, b);
+        mx = fmaxf(mx, b);
+    }
+}
+
+// interval of x * X * Y * Z (X, Y, Z intervals), in double
+__device__ __forceinline__ void term_interval(double x, const float* lo, const float* hi, double& tlo, double& thi) {
+    double a = x, b = x;
+    for (int ax = 0; ax < 3; ++ax) {
+        const double c0 = a * lo[ax], c1 = a * hi[ax], c2 = b * lo[ax], c3 = b * hi[ax];
+        a = fmin(fmin(c0, c1), fmin(c2, c3));
+        b = fmax(fmax(c0, c1), fmax(c2, c3));
+    }
+    tlo = a;
+    thi = b;
+}
+
+__global__ void __launch_bounds__(BR_BLOCK) k_brick_bounds(VArgs v, BrickIndex bix, i64 nbricks,
+                                                           unsigned char* __restrict__ culled) {
+    __shared__ double red[4][BR_BLOCK / 32];
+    const EvalArgs& a = v.e;
+    const NodeArrays& nd = a.nd;
+    const int D = a.D;
+    const float inv = 1.0f / (float)(1 << D);
+    for (i64 bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
+        const VBrick B = brick_of(v, bix, bi);
+        const VRoot R = v.roots[B.root];
+        const int r = R.depth, S = 1 << (D - r), L = R.node;
+        if (B.bu == 0 || B.bv == 0 || B.bw == 0) {   // touches the lower faces: evaluate
+            if (threadIdx.x == 0) culled[bi] = 0;
+            continue;
+        }
+        int Lc[3];
+        key_coords(nd.key[L], r, D, Lc);
+        const int c0[3] = {B.bu * BR, B.bv * BR, B.bw * BR};
+        const int g0[3] = {Lc[0] * S + c0[0], Lc[1] * S + c0[1], Lc[2] * S + c0[2]};   // first corner (global)
+        double lo = 0, hi = 0, amax = 0, cnt = 0;
+        // (a) the leaf and its ancestors: 27 (r+1) terms every corner has
+        for (int t = threadIdx.x; t < 27 * (r + 1); t += blockDim.x) {
+            const int l = r - t / 27, j = t % 27;
+            int node = L;
+            for (int q = r; q > l; --q) node = nd.parent[node];
+            const int nb = nd.neigh[(i64)j * nd.M + node];
+            if (nb == -1) continue;
+            const int off[3] = {j / 9 - 1, (j / 3) % 3 - 1, j % 3 - 1};
+            float blo[3], bhi[3];
+            for (int ax = 0; ax < 3; ++ax) {
+                const int fi = (1 << l) - 1 + (Lc[ax] >> (r - l)) + off[ax];
+                basis_range(a, fi, g0[ax], inv, blo[ax], bhi[ax]);
+            }
+            double tl, th;
+            term_interval((double)a.x[nb], blo, bhi, tl, th);
+            lo += tl; hi += th;
+            amax += fmax(fabs(tl), fabs(th));
+            cnt += 1;
+        }
+        // (b) real nodes around the virtual cells the brick's owners pass through
+        for (int d = r + 1; d <= D; ++d) {
+            const int sh = D - d, span = 1 << (d - r);
+            int Vlo[3], Vhi[3], ext[3];
+            bool inner = true;
+            for (int ax = 0; ax < 3; ++ax) {
+                Vlo[ax] = (g0[ax] - 1) >> sh;
+                Vhi[ax] = (g0[ax] + BR - 1) >> sh;
+                const int llo = Lc[ax] * span;
+                if (Vlo[ax] - 1 < llo || Vhi[ax] + 1 >= llo + span) inner = false;
+                ext[ax] = Vhi[ax] - Vlo[ax] + 3;
+            }
+            if (inner) continue;   // every neighbour lies inside the leaf
+            const int ncell = ext[0] * ext[1] * ext[2];
+            for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+                const int N[3] = {Vlo[0] - 1 + t / (ext[1] * ext[2]), Vlo[1] - 1 + (t / ext[2]) % ext[1],
+                                  Vlo[2] - 1 + t % ext[2]};
+                const i64 node = shell_node(v, L, r, Lc, d, N);
+                if (node < 0) continue;
+                float blo[3], bhi[3];
+                for (int ax = 0; ax < 3; ++ax) {
+                    basis_range(a, (1 << d) - 1 + N[ax], g0[ax], inv, blo[ax], bhi[ax]);
+                    blo[ax] = fminf(blo[ax], 0.f);   // not every corner has this term
+                    bhi[ax] = fmaxf(bhi[ax], 0.f);
+                }
+                double tl, th;
+                term_interval((double)a.x[node], blo, bhi, tl, th);
+                lo += tl; hi += th;
+                amax += fmax(fabs(tl), fabs(th));
+                cnt += 1;
+            }
+        }
+        // block reduction
+        double vals[4] = {lo, hi, amax, cnt};
+        for (int k = 0; k < 4; ++k) {
+            double x = vals[k];
+            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum[4] = {0, 0, 0, 0};
+            for (int k = 0; k < 4; ++k)
+                for (int w = 0; w < BR_BLOCK / 32; ++w) sum[k] += red[k][w];
+            const double u = 5.9604644775390625e-08;   // 2^-24
+            const double iso = (double)v.iso;
+            const double margin = (sum[3] + 4.0) * u * sum[2] + 2.0 * u * (fabs(sum[0]) + fabs(sum[1]) + 2.0 * fabs(iso)) +
+                                  1e-12 * (sum[2] + fabs(iso));
+            const bool above = sum[0] - margin > iso, below = sum[1] + margin < iso;
+            culled[bi] = (above || below) ? 1 : 0;
+        }
+        __syncthreads();
+    }
+}
+
+// exact corner values of a non-culled brick; corners on the leaf's lower faces
+// go through the owner search, the others take the interior path
+__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const i64* __restrict__ list,
+                                                         i64 nlist,
+                                                         const i64* __restrict__ lat_prefix, float* __restrict__ lat) {
+    __shared__ float xL[16 * 27];
+    __shared__ float Bt[16 * 9 * (BR + 1)];
+    const EvalArgs& a = v.e;
+    const NodeArrays& nd = a.nd;
+    const int D = a.D;
+    const float inv = 1.0f / (float)(1 << D);
+    for (i64 li = blockIdx.x; li < nlist; li += gridDim.x) {
+        const VBrick B = brick_of(v, bix, list[li]);
+        const VRoot R = v.roots[B.root];
+        const int r = R.depth, S = 1 << (D - r), S1 = S + 1, L = R.node;
+        int Lc[3];
+        key_coords(nd.key[L], r, D, Lc);
+        const int c0[3] = {B.bu * BR, B.bv * BR, B.bw * BR};
+        __syncthreads();
+        if (threadIdx.x <= r) {
+            int node = L;
+            for (int l = r; l > (int)threadIdx.x; --l) node = nd.parent[node];
+            for (int j = 0; j < 27; ++j) xL[27 * threadIdx.x + j] = x_or_zero(a, nd.neigh[(i64)j * nd.M + node]);
+        }
+        for (int e = threadIdx.x; e < (D + 1) * 9 * (BR + 1); e += blockDim.x) {
+            const int k = e % (BR + 1), t = (e / (BR + 1)) % 3, ax = (e / (3 * (BR + 1))) % 3, d = e / (9 * (BR + 1));
+            const int u = c0[ax] + k;
+            int cidx;
+            if (d <= r) cidx = (Lc[ax] >> (r - d)) + t - 1;
+            else cidx = ((Lc[ax] * S + u - 1) >> (D - d)) + t - 1;
+            float val = 0.f;
+            if (cidx >= 0 && cidx < (1 << d)) val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(Lc[ax] * S + u) * inv);
+            Bt[((d * 3 + ax) * 3 + t) * (BR + 1) + k] = val;
+        }
+        __syncthreads();
+        const int nc = (BR + 1) * (BR + 1) * (BR + 1);
+        // interior corners
+        for (int e = threadIdx.x; e < nc; e += blockDim.x) {
+            const int ku = e / ((BR + 1) * (BR + 1)), kv = (e / (BR + 1)) % (BR + 1), kw = e % (BR + 1);
+            const int u = c0[0] + ku, w = c0[1] + kv, z = c0[2] + kw;
+            if (u == 0 || w == 0 || z == 0) continue;
+            const int o[3] = {Lc[0] * S + u - 1, Lc[1] * S + w - 1, Lc[2] * S + z - 1};
+            float val = 0.f;
+            for (int d = D; d > r; --d) {
+                const int sh = D - d, span = 1 << (d - r);
+                const int V[3] = {o[0] >> sh, o[1] >> sh, o[2] >> sh};
+                bool inner = true;
+                for (int ax = 0; ax < 3; ++ax) {
+                    const int lo = Lc[ax] * span;
+                    if (V[ax] - 1 < lo || V[ax] + 1 >= lo + span) inner = false;
+                }
+                if (inner) continue;
+                const float* bx = Bt + ((d * 3 + 0) * 3) * (BR + 1) + ku;
+                const float* by = Bt + ((d * 3 + 1) * 3) * (BR + 1) + kv;
+                const float* bz = Bt + ((d * 3 + 2) * 3) * (BR + 1) + kw;
+                for (int j = 0; j < 27; ++j) {
+                    const int jx = j / 9, jy = (j / 3) % 3, jz = j % 3;
+                    const int N[3] = {V[0] + jx - 1, V[1] + jy - 1, V[2] + jz - 1};
+                    if ((N[0] >> (d - r)) == Lc[0] && (N[1] >> (d - r)) == Lc[1] && (N[2] >> (d - r)) == Lc[2]) continue;
+                    const i64 node = shell_node(v, L, r, Lc, d, N);
+                    const float xn = node < 0 ? 0.f : a.x[node];
+                    val = fmaf(xn * bx[jx * (BR + 1)] * by[jy * (BR + 1)], bz[jz * (BR + 1)], val);
+                }
+            }
+            for (int l = r; l >= 0; --l) {
+                const float* xs = xL + 27 * l;
+                const float* bx = Bt + ((l * 3 + 0) * 3) * (BR + 1) + ku;
+                const float* by = Bt + ((l * 3 + 1) * 3) * (BR + 1) + kv;
+                const float* bz = Bt + ((l * 3 + 2) * 3) * (BR + 1) + kw;
+#pragma unroll
+                for (int j = 0; j < 27; ++j)
+                    val = fmaf(xs[j] * bx[(j / 9) * (BR + 1)] * by[((j / 3) % 3) * (BR + 1)], bz[(j % 3) * (BR + 1)], val);
+            }
+            lat[lat_prefix[B.root] + ((i64)u * S1 + w) * S1 + z] = val - v.iso;
+        }
+        // corners on the leaf's lower faces
+        if (B.bu == 0 || B.bv == 0 || B.bw == 0) {
+            for (int e = threadIdx.x; e < nc; e += blockDim.x) {
+                const int ku = e / ((BR + 1) * (BR + 1)), kv = (e / (BR + 1)) % (BR + 1), kw = e % (BR + 1);
+                const int u = c0[0] + ku, w = c0[1] + kv, z = c0[2] + kw;
+                if (!(u == 0 || w == 0 || z == 0)) continue;
+                const int qc[3] = {Lc[0] * S + u, Lc[1] * S + w, Lc[2] * S + z};
+                u64 best = ~0ull;
+                int own_root = -1, oc[3] = {0, 0, 0};
+                for (int eo = 0; eo < 8; ++eo) {
+                    const int cell[3] = {qc[0] - (eo & 1), qc[1] - ((eo >> 1) & 1), qc[2] - ((eo >> 2) & 1)};
+                    const int m = batch_member(v, R, Lc, cell);
+                    if (m < 0) continue;
+                    const u64 kk = cell_key_D(cell, D);
+                    if (kk < best) { best = kk; own_root = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
+                }
+                lat[lat_prefix[B.root] + ((i64)u * S1 + w) * S1 + z] =
+                    virtual_corner_value(v, own_root, r, oc, qc) - v.iso;
+            }
+        }
     }
 }
 
 __global__ void k_virtual_cells(VArgs v, const i64* __restrict__ cell_prefix, const i64* __restrict__ lat_prefix,
-                                i64 total, const float* __restrict__ lat, unsigned char* __restrict__ cat,
-                                int* __restrict__ ntri) {
+                                i64 total, const float* __restrict__ lat, const unsigned char* __restrict__ culled,
+                                unsigned char* __restrict__ cat, int* __restrict__ ntri) {
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
         int lo = 0, hi = v.nroots - 1;
         while (lo < hi) {
@@ -437,6 +713,14 @@ __global__ void k_virtual_cells(VArgs v, const i64* __restrict__ cell_prefix, co
         const int S = 1 << (v.e.D - R.depth), S1 = S + 1;
         const i64 loc = e - cell_prefix[lo];
         const int u = (int)(loc / ((i64)S * S)), w = (int)((loc / S) % S), z = (int)(loc % S);
+        if (R.brick_base >= 0) {
+            const int nb = S / BR;
+            if (culled[R.brick_base + ((i64)(u / BR) * nb + (w / BR)) * nb + (z / BR)]) {
+                cat[e] = 0;
+                ntri[e] = 0;
+                continue;
+            }
+        }
         const float* L = lat + lat_prefix[lo];
         int cc = 0;
         for (int kind = 0; kind < 8; ++kind) {
@@ -613,6 +897,11 @@ __global__ void k_vertex_ids(const u64* __restrict__ keys, const uint32_t* __res
         }
     }
 }
+// live (not culled) flag per brick
+__global__ void k_flags_from_bytes(const unsigned char* __restrict__ culled, i64 n, int* __restrict__ f) {
+    for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        f[k] = culled[k] ? 0 : 1;
+}
 __global__ void k_key_heads(const u64* __restrict__ keys, i64 n, int* __restrict__ f) {
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
         f[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1 : 0;
@@ -738,10 +1027,13 @@ void stage_mesh(Ctx& c) {
     dfree(fpos, s);
     // ---- virtual cells
     i64 ntri_virt = 0, nact_virt = 0, total_cells = 0, total_lat = 0;
+    c.total_bricks = 0;
+    c.live_bricks = 0;
     VRoot* droots = nullptr;
     i64 *cell_prefix = nullptr, *lat_prefix = nullptr, *act_virt = nullptr, *tri_virt = nullptr;
     float* lat = nullptr;
     unsigned char* vcat = nullptr;
+    unsigned char* culled = nullptr;
     int* vntri = nullptr;
     int* bflag = nullptr;
     VArgs va;
@@ -750,12 +1042,15 @@ void stage_mesh(Ctx& c) {
     va.nroots = (int)roots.size();
     if (!roots.empty()) {
         std::vector<i64> hcp(roots.size()), hlp(roots.size());
+        i64 brick_run = 0;
         for (size_t k = 0; k < roots.size(); ++k) {
             const i64 S = 1ll << (D - roots[k].depth);
             hcp[k] = total_cells;
             hlp[k] = total_lat;
             roots[k].cell_base = total_cells;
             roots[k].lattice_base = total_lat;
+            roots[k].brick_base = (S > BR) ? brick_run : -1;
+            if (S > BR) brick_run += (S / BR) * (S / BR) * (S / BR);
             total_cells += S * S * S;
             total_lat += (S + 1) * (S + 1) * (S + 1);
         }
@@ -772,15 +1067,75 @@ void stage_mesh(Ctx& c) {
         va.roots = droots;
         va.batch_root_flag = bflag;
         lat = dalloc<float>(total_lat, s);
-        const int kv = c.kbegin("virtual_corners", (double)total_lat * 4);
-        k_virtual_corners<<<grid_for(total_lat, 128, 1ll << 30), 128, 0, s>>>(va, lat_prefix, total_lat, lat);
-        CK_LAUNCH();
-        c.kend(kv);
+        // small leaves (lattice edge <= 8): one thread per corner; large ones: 8^3-cell bricks
+        std::vector<int> small_list, big_list;
+        std::vector<i64> small_prefix, brick_prefix;
+        i64 small_total = 0, nbricks = 0;
+        for (size_t k = 0; k < roots.size(); ++k) {
+            const int S = 1 << (D - roots[k].depth);
+            if (S <= BR) {
+                small_list.push_back((int)k);
+                small_prefix.push_back(small_total);
+                small_total += (i64)(S + 1) * (S + 1) * (S + 1);
+            } else {
+                big_list.push_back((int)k);
+                brick_prefix.push_back(nbricks);
+                nbricks += (i64)(S / BR) * (S / BR) * (S / BR);
+            }
+        }
+        if (small_total > 0) {
+            const int kvs = c.kbegin("virtual_small", (double)small_total * 4);
+            int* dlist = dalloc<int>((i64)small_list.size(), s);
+            i64* dpre = dalloc<i64>((i64)small_prefix.size(), s);
+            CK(cudaMemcpyAsync(dlist, small_list.data(), small_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dpre, small_prefix.data(), small_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+            k_virtual_corners<<<grid_for(small_total, 128, 1ll << 30), 128, 0, s>>>(
+                va, dlist, dpre, (int)small_list.size(), small_total, lat_prefix, lat);
+            CK_LAUNCH();
+            c.kend(kvs);
+            dfree(dlist, s);
+            dfree(dpre, s);
+        }
+        culled = dalloc<unsigned char>(std::max<i64>(nbricks, 1), s);
+        if (nbricks > 0) {
+            int* dbig = dalloc<int>((i64)big_list.size(), s);
+            i64* dbpre = dalloc<i64>((i64)brick_prefix.size(), s);
+            CK(cudaMemcpyAsync(dbig, big_list.data(), big_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(dbpre, brick_prefix.data(), brick_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+            BrickIndex bix{dbig, dbpre, (int)big_list.size()};
+            const int kb = c.kbegin("brick_bounds", (double)nbricks * 1);
+            k_brick_bounds<<<grid_for(nbricks, 1, 152 * 64), BR_BLOCK, 0, s>>>(va, bix, nbricks, culled);
+            CK_LAUNCH();
+            c.kend(kb);
+            // non-culled bricks
+            int* bf = dalloc<int>(nbricks, s);
+            int* bp = dalloc<int>(nbricks + 1, s);
+            k_flags_from_bytes<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
+            CK_LAUNCH();
+            exclusive_scan<int, int>(bf, bp, nbricks, bp + nbricks, s);
+            const i64 nlive = read_scalar(bp + nbricks, s);
+            c.live_bricks = nlive;
+            c.total_bricks = nbricks;
+            if (nlive > 0) {
+                i64* live = dalloc<i64>(nlive, s);
+                k_compact_idx<i64><<<grid_for(nbricks, 256), 256, 0, s>>>(bf, bp, nbricks, live);
+                CK_LAUNCH();
+                const int ke = c.kbegin("brick_eval", (double)nlive * (BR + 1) * (BR + 1) * (BR + 1) * 4);
+                k_brick_eval<<<grid_for(nlive, 1, 152 * 64), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_prefix, lat);
+                CK_LAUNCH();
+                c.kend(ke);
+                dfree(live, s);
+            }
+            dfree(bf, s);
+            dfree(bp, s);
+            dfree(dbig, s);
+            dfree(dbpre, s);
+        }
         vcat = dalloc<unsigned char>(total_cells, s);
         vntri = dalloc<int>(total_cells, s);
         const int kc2 = c.kbegin("virtual_cells", (double)total_lat * 4 + (double)total_cells * 5);
         k_virtual_cells<<<grid_for(total_cells, 256, 1ll << 30), 256, 0, s>>>(va, cell_prefix, lat_prefix, total_cells,
-                                                                              lat, vcat, vntri);
+                                                                              lat, culled, vcat, vntri);
         CK_LAUNCH();
         c.kend(kc2);
         int* vf = dalloc<int>(total_cells, s);
@@ -869,7 +1224,7 @@ void stage_mesh(Ctx& c) {
     dfree(act_real, s);
     dfree(tri_real, s);
     dfree(droots, s); dfree(cell_prefix, s); dfree(lat_prefix, s); dfree(act_virt, s); dfree(tri_virt, s);
-    dfree(lat, s); dfree(vcat, s); dfree(vntri, s); dfree(bflag, s);
+    dfree(lat, s); dfree(vcat, s); dfree(vntri, s); dfree(bflag, s); dfree(culled, s);
     dfree(cell_v, s);
     dfree(cat, s);
     dfree(ntri, s);
