@@ -139,6 +139,7 @@ int prgpu_create(const prgpu_params* p, void** out) {
     c->device = p->device;
     CK(cudaSetDevice(c->device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device));
     CK(cudaEventCreate(&c->ev0));
     CK(cudaEventCreate(&c->ev1));
     // keep freed pool memory for reuse across calls

@@ -43,6 +43,7 @@ struct Ctx {
     prgpu_params params;
     int device = 0;
     cudaStream_t stream = nullptr;
+    int sms = 152;                      // multiprocessors of the device
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int D = 8;
     int res = 0;

@@ -428,21 +428,33 @@ __global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i
 
 // ---- large subdivided leaves (lattice edge >= 16): bricks of 8^3 cells.
 //
-// Most corners of a large subdivided leaf lie far from the surface.  A brick is
-// culled when every corner value it contains provably has the same sign as
-// (value - iso) -- then none of its cells carries a triangle and its corners
-// are never read.  The proof uses the exact quantities the evaluation would
-// use: each term of a corner value is x_n * B_x(q_x) * B_y(q_y) * B_z(q_z)
-// with B the single-precision basis values, so the brick's range of each term
-// is an interval product over the brick's lattice coordinates, and the
-// difference between the FMA chain and the exact sum of its terms is at most
-// (K + 4) u sum|term| for K terms (u = 2^-24).  Terms that only some corners
-// include (neighbours of exposed virtual cells) get intervals widened to 0.
-// Bricks that touch the leaf's lower faces are not culled (their corners may
-// be owned by cells outside the leaf).  Every corner of a non-culled brick is
-// evaluated exactly as virtual_corner_value does, so culling changes no value.
+// Most corners of a large subdivided leaf lie far from the surface.  One block
+// takes one brick (8^3 cells, 9^3 corners) at a time:
+//   1. it gathers into shared memory every coefficient the brick's corners can
+//      read: the 27 neighbours of the leaf and of each ancestor, and at every
+//      virtual depth the window of cells around the brick's owner cells (real
+//      nodes outside the leaf, 0 where there is none);
+//   2. it bounds the brick's corner values: each term is x_n * B_x * B_y * B_z
+//      with the single-precision basis values the evaluation uses, so the range
+//      of a term over the corners that include it is an interval product, and
+//      the rounding of the FMA chain is at most (K + 4) u sum|term| for K terms
+//      (u = 2^-24); terms only some corners include get intervals widened to 0;
+//   3. if the bound proves that every corner value has the same sign as
+//      (value - iso), the brick is culled: none of its cells carries a triangle
+//      and its corners are never read;
+//   4. otherwise every corner is evaluated from the shared window in the order
+//      of virtual_corner_value, so culling changes no value.
+// Corners on the leaf's lower faces may be owned by a cell of another leaf of
+// the same depth batch: those go through virtual_corner_value, and a brick with
+// such a corner is never culled.
 constexpr int BR = 8;              // brick edge (cells); corners per axis BR+1
+constexpr int BR1 = BR + 1;
 constexpr int BR_BLOCK = 128;
+constexpr int BR_LEVELS = 16;      // depths 0..15
+constexpr int BR_WEXT = BR + 3;    // window edge at the finest depth
+// window cells over all virtual depths of a brick whose first corner is a
+// multiple of 8: 11^3 + 7^3 + 5^3 + 12 * 4^3 = 2567
+constexpr int BR_XW = 2600;
 
 struct VBrick {
     int root;                      // index into roots
@@ -484,18 +496,6 @@ __device__ i64 shell_node(const VArgs& v, int L, int r, const int Lc[3], int d, 
     return descend(nd, an, r, d, N);
 }
 
-// min/max over the brick's lattice coordinates along one axis of basis function fi
-__device__ __forceinline__ void basis_range(const EvalArgs& a, int fi, int g0, float inv, float& mn, float& mx) {
-    mn = 3.4e38f;
-    mx = -3.4e38f;
-    for (int k = 0; k <= BR; ++k) {
-        const float q = (float)(g0 + k) * inv;
-        const float b = cpoly_value<3>(a.basis[fi], q);
-        mn = fminf(mn, b);
-        mx = fmaxf(mx, b);
-    }
-}
-
 // interval of x * X * Y * Z (X, Y, Z intervals), in double
 __device__ __forceinline__ void term_interval(double x, const float* lo, const float* hi, double& tlo, double& thi) {
     double a = x, b = x;
@@ -508,194 +508,279 @@ __device__ __forceinline__ void term_interval(double x, const float* lo, const f
     thi = b;
 }
 
-__global__ void __launch_bounds__(BR_BLOCK) k_brick_bounds(VArgs v, BrickIndex bix, i64 nbricks,
-                                                           unsigned char* __restrict__ culled) {
-    __shared__ double red[4][BR_BLOCK / 32];
-    const EvalArgs& a = v.e;
-    const NodeArrays& nd = a.nd;
-    const int D = a.D;
-    const float inv = 1.0f / (float)(1 << D);
-    for (i64 bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
-        const VBrick B = brick_of(v, bix, bi);
-        const VRoot R = v.roots[B.root];
-        const int r = R.depth, S = 1 << (D - r), L = R.node;
-        if (B.bu == 0 || B.bv == 0 || B.bw == 0) {   // touches the lower faces: evaluate
-            if (threadIdx.x == 0) culled[bi] = 0;
-            continue;
-        }
-        int Lc[3];
-        key_coords(nd.key[L], r, D, Lc);
-        const int c0[3] = {B.bu * BR, B.bv * BR, B.bw * BR};
-        const int g0[3] = {Lc[0] * S + c0[0], Lc[1] * S + c0[1], Lc[2] * S + c0[2]};   // first corner (global)
-        double lo = 0, hi = 0, amax = 0, cnt = 0;
-        // (a) the leaf and its ancestors: 27 (r+1) terms every corner has
-        for (int t = threadIdx.x; t < 27 * (r + 1); t += blockDim.x) {
-            const int l = r - t / 27, j = t % 27;
-            int node = L;
-            for (int q = r; q > l; --q) node = nd.parent[node];
-            const int nb = nd.neigh[(i64)j * nd.M + node];
-            if (nb == -1) continue;
-            const int off[3] = {j / 9 - 1, (j / 3) % 3 - 1, j % 3 - 1};
-            float blo[3], bhi[3];
-            for (int ax = 0; ax < 3; ++ax) {
-                const int fi = (1 << l) - 1 + (Lc[ax] >> (r - l)) + off[ax];
-                basis_range(a, fi, g0[ax], inv, blo[ax], bhi[ax]);
-            }
-            double tl, th;
-            term_interval((double)a.x[nb], blo, bhi, tl, th);
-            lo += tl; hi += th;
-            amax += fmax(fabs(tl), fabs(th));
-            cnt += 1;
-        }
-        // (b) real nodes around the virtual cells the brick's owners pass through
-        for (int d = r + 1; d <= D; ++d) {
-            const int sh = D - d, span = 1 << (d - r);
-            int Vlo[3], Vhi[3], ext[3];
-            bool inner = true;
-            for (int ax = 0; ax < 3; ++ax) {
-                Vlo[ax] = (g0[ax] - 1) >> sh;
-                Vhi[ax] = (g0[ax] + BR - 1) >> sh;
-                const int llo = Lc[ax] * span;
-                if (Vlo[ax] - 1 < llo || Vhi[ax] + 1 >= llo + span) inner = false;
-                ext[ax] = Vhi[ax] - Vlo[ax] + 3;
-            }
-            if (inner) continue;   // every neighbour lies inside the leaf
-            const int ncell = ext[0] * ext[1] * ext[2];
-            for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-                const int N[3] = {Vlo[0] - 1 + t / (ext[1] * ext[2]), Vlo[1] - 1 + (t / ext[2]) % ext[1],
-                                  Vlo[2] - 1 + t % ext[2]};
-                const i64 node = shell_node(v, L, r, Lc, d, N);
-                if (node < 0) continue;
-                float blo[3], bhi[3];
-                for (int ax = 0; ax < 3; ++ax) {
-                    basis_range(a, (1 << d) - 1 + N[ax], g0[ax], inv, blo[ax], bhi[ax]);
-                    blo[ax] = fminf(blo[ax], 0.f);   // not every corner has this term
-                    bhi[ax] = fmaxf(bhi[ax], 0.f);
-                }
-                double tl, th;
-                term_interval((double)a.x[node], blo, bhi, tl, th);
-                lo += tl; hi += th;
-                amax += fmax(fabs(tl), fabs(th));
-                cnt += 1;
-            }
-        }
-        // block reduction
-        double vals[4] = {lo, hi, amax, cnt};
-        for (int k = 0; k < 4; ++k) {
-            double x = vals[k];
-            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = x;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double sum[4] = {0, 0, 0, 0};
-            for (int k = 0; k < 4; ++k)
-                for (int w = 0; w < BR_BLOCK / 32; ++w) sum[k] += red[k][w];
-            const double u = 5.9604644775390625e-08;   // 2^-24
-            const double iso = (double)v.iso;
-            const double margin = (sum[3] + 4.0) * u * sum[2] + 2.0 * u * (fabs(sum[0]) + fabs(sum[1]) + 2.0 * fabs(iso)) +
-                                  1e-12 * (sum[2] + fabs(iso));
-            const bool above = sum[0] - margin > iso, below = sum[1] + margin < iso;
-            culled[bi] = (above || below) ? 1 : 0;
-        }
-        __syncthreads();
+struct BrickShared {
+    float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
+    float Bt[BR_LEVELS * 9 * BR1];            // [depth][axis][t][k]: basis value of owner cell + t - 1 at corner k
+    float Xw[BR_XW];                          // window coefficients, virtual depths
+    float Wlo[BR_LEVELS * 3 * BR_WEXT];       // per window coordinate: basis range over the corners using it
+    float Whi[BR_LEVELS * 3 * BR_WEXT];
+    int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
+    int wext[BR_LEVELS][3];
+    int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
+    double red[4][BR_BLOCK / 32];
+    int foreign;                              // a lower-face corner is owned by another leaf
+    int cull;
+};
+
+// owner of a lower-face corner (min key among batch cells sharing it)
+__device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, const int Lc[3], const int qc[3],
+                                                int oc[3]) {
+    u64 best = ~0ull;
+    int own = -1;
+    for (int eo = 0; eo < 8; ++eo) {
+        const int cell[3] = {qc[0] - (eo & 1), qc[1] - ((eo >> 1) & 1), qc[2] - ((eo >> 2) & 1)};
+        const int m = batch_member(v, R, Lc, cell);
+        if (m < 0) continue;
+        const u64 kk = cell_key_D(cell, v.e.D);
+        if (kk < best) { best = kk; own = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
     }
+    return own;
 }
 
-// exact corner values of a non-culled brick; corners on the leaf's lower faces
-// go through the owner search, the others take the interior path
-__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const i64* __restrict__ list,
-                                                         i64 nlist,
-                                                         const i64* __restrict__ lat_prefix, float* __restrict__ lat) {
-    __shared__ float xL[16 * 27];
-    __shared__ float Bt[16 * 9 * (BR + 1)];
+// value of corner k (brick-local kk[], global qc[]) owned by the brick's leaf
+// through owner cell oc[], from the shared window; 'interior' means oc = qc - 1
+// so the tabulated basis values apply
+__device__ __forceinline__ float brick_corner(const BrickShared& sm, const EvalArgs& a, int r, const int Lc[3],
+                                              const int oc[3], const int qc[3], const int kk[3], bool interior) {
+    const int D = a.D;
+    const float inv = 1.0f / (float)(1 << D);
+    float val = 0.f;
+    for (int d = D; d > r; --d) {
+        const int off = sm.woff[d];
+        if (off < 0) continue;
+        const int sh = D - d, span = 1 << (d - r);
+        const int V[3] = {oc[0] >> sh, oc[1] >> sh, oc[2] >> sh};
+        bool inner = true;
+        for (int ax = 0; ax < 3; ++ax) {
+            const int lo = Lc[ax] * span;
+            if (V[ax] - 1 < lo || V[ax] + 1 >= lo + span) inner = false;
+        }
+        if (inner) continue;
+        float bv[3][3];
+        if (interior) {
+            for (int ax = 0; ax < 3; ++ax)
+                for (int t = 0; t < 3; ++t) bv[ax][t] = sm.Bt[((d * 3 + ax) * 3 + t) * BR1 + kk[ax]];
+        } else {
+            const int fb = (1 << d) - 1, lim = 1 << d;
+            for (int ax = 0; ax < 3; ++ax)
+                for (int t = 0; t < 3; ++t) {
+                    const int cc = V[ax] + t - 1;
+                    bv[ax][t] = (cc >= 0 && cc < lim) ? cpoly_value<3>(a.basis[fb + cc], (float)qc[ax] * inv) : 0.f;
+                }
+        }
+        const int e1 = sm.wext[d][1], e2 = sm.wext[d][2];
+        const int b0 = V[0] - 1 - sm.wlo[d][0], b1 = V[1] - 1 - sm.wlo[d][1], b2 = V[2] - 1 - sm.wlo[d][2];
+        const int s2 = d - r;
+        for (int j = 0; j < 27; ++j) {
+            const int jx = j / 9, jy = (j / 3) % 3, jz = j % 3;
+            if (((V[0] + jx - 1) >> s2) == Lc[0] && ((V[1] + jy - 1) >> s2) == Lc[1] && ((V[2] + jz - 1) >> s2) == Lc[2])
+                continue;                                     // inside the subdivided leaf: no coefficient
+            const float xn = sm.Xw[off + ((b0 + jx) * e1 + (b1 + jy)) * e2 + (b2 + jz)];
+            val = fmaf(xn * bv[0][jx] * bv[1][jy], bv[2][jz], val);
+        }
+    }
+    // the leaf itself and its real ancestors (walk_up with absent neighbours as 0)
+    for (int l = r; l >= 0; --l) {
+        const float* xs = sm.xL + 27 * l;
+        const float* bx = sm.Bt + ((l * 3 + 0) * 3) * BR1 + kk[0];
+        const float* by = sm.Bt + ((l * 3 + 1) * 3) * BR1 + kk[1];
+        const float* bz = sm.Bt + ((l * 3 + 2) * 3) * BR1 + kk[2];
+#pragma unroll
+        for (int j = 0; j < 27; ++j)
+            val = fmaf(xs[j] * bx[(j / 9) * BR1] * by[((j / 3) % 3) * BR1], bz[(j % 3) * BR1], val);
+    }
+    return val;
+}
+
+// one brick at a time per block, taken from a work counter
+__global__ void __launch_bounds__(BR_BLOCK) k_bricks(VArgs v, BrickIndex bix, i64 nbricks,
+                                                     unsigned long long* __restrict__ work,
+                                                     unsigned long long* __restrict__ live,
+                                                     unsigned char* __restrict__ culled,
+                                                     const i64* __restrict__ lat_prefix, float* __restrict__ lat,
+                                                     int* __restrict__ err) {
+    __shared__ BrickShared sm;
+    __shared__ long long sh_bi;
     const EvalArgs& a = v.e;
     const NodeArrays& nd = a.nd;
     const int D = a.D;
     const float inv = 1.0f / (float)(1 << D);
-    for (i64 li = blockIdx.x; li < nlist; li += gridDim.x) {
-        const VBrick B = brick_of(v, bix, list[li]);
+    const double u = 5.9604644775390625e-08;   // 2^-24
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) sh_bi = (long long)atomicAdd(work, 1ull);
+        __syncthreads();
+        const i64 bi = sh_bi;
+        if (bi >= nbricks) break;
+        const VBrick B = brick_of(v, bix, bi);
         const VRoot R = v.roots[B.root];
         const int r = R.depth, S = 1 << (D - r), S1 = S + 1, L = R.node;
         int Lc[3];
         key_coords(nd.key[L], r, D, Lc);
         const int c0[3] = {B.bu * BR, B.bv * BR, B.bw * BR};
-        __syncthreads();
-        if (threadIdx.x <= r) {
-            int node = L;
-            for (int l = r; l > (int)threadIdx.x; --l) node = nd.parent[node];
-            for (int j = 0; j < 27; ++j) xL[27 * threadIdx.x + j] = x_or_zero(a, nd.neigh[(i64)j * nd.M + node]);
-        }
-        for (int e = threadIdx.x; e < (D + 1) * 9 * (BR + 1); e += blockDim.x) {
-            const int k = e % (BR + 1), t = (e / (BR + 1)) % 3, ax = (e / (3 * (BR + 1))) % 3, d = e / (9 * (BR + 1));
-            const int u = c0[ax] + k;
-            int cidx;
-            if (d <= r) cidx = (Lc[ax] >> (r - d)) + t - 1;
-            else cidx = ((Lc[ax] * S + u - 1) >> (D - d)) + t - 1;
-            float val = 0.f;
-            if (cidx >= 0 && cidx < (1 << d)) val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(Lc[ax] * S + u) * inv);
-            Bt[((d * 3 + ax) * 3 + t) * (BR + 1) + k] = val;
-        }
-        __syncthreads();
-        const int nc = (BR + 1) * (BR + 1) * (BR + 1);
-        // interior corners
-        for (int e = threadIdx.x; e < nc; e += blockDim.x) {
-            const int ku = e / ((BR + 1) * (BR + 1)), kv = (e / (BR + 1)) % (BR + 1), kw = e % (BR + 1);
-            const int u = c0[0] + ku, w = c0[1] + kv, z = c0[2] + kw;
-            if (u == 0 || w == 0 || z == 0) continue;
-            const int o[3] = {Lc[0] * S + u - 1, Lc[1] * S + w - 1, Lc[2] * S + z - 1};
-            float val = 0.f;
-            for (int d = D; d > r; --d) {
+        const int g0[3] = {Lc[0] * S + c0[0], Lc[1] * S + c0[1], Lc[2] * S + c0[2]};   // first corner (global)
+        const bool lower = (B.bu == 0 || B.bv == 0 || B.bw == 0);
+        // ---- 1. window layout, leaf coefficients, basis table
+        if (threadIdx.x == 0) {
+            int off = 0;
+            for (int d = r + 1; d <= D; ++d) {
                 const int sh = D - d, span = 1 << (d - r);
-                const int V[3] = {o[0] >> sh, o[1] >> sh, o[2] >> sh};
                 bool inner = true;
                 for (int ax = 0; ax < 3; ++ax) {
-                    const int lo = Lc[ax] * span;
-                    if (V[ax] - 1 < lo || V[ax] + 1 >= lo + span) inner = false;
+                    const int Vlo = (g0[ax] - 1) >> sh, Vhi = (g0[ax] + BR - 1) >> sh;
+                    const int llo = Lc[ax] * span;
+                    if (Vlo - 1 < llo || Vhi + 1 >= llo + span) inner = false;
+                    sm.wlo[d][ax] = Vlo - 1;
+                    sm.wext[d][ax] = Vhi - Vlo + 3;
                 }
-                if (inner) continue;
-                const float* bx = Bt + ((d * 3 + 0) * 3) * (BR + 1) + ku;
-                const float* by = Bt + ((d * 3 + 1) * 3) * (BR + 1) + kv;
-                const float* bz = Bt + ((d * 3 + 2) * 3) * (BR + 1) + kw;
-                for (int j = 0; j < 27; ++j) {
-                    const int jx = j / 9, jy = (j / 3) % 3, jz = j % 3;
-                    const int N[3] = {V[0] + jx - 1, V[1] + jy - 1, V[2] + jz - 1};
-                    if ((N[0] >> (d - r)) == Lc[0] && (N[1] >> (d - r)) == Lc[1] && (N[2] >> (d - r)) == Lc[2]) continue;
-                    const i64 node = shell_node(v, L, r, Lc, d, N);
-                    const float xn = node < 0 ? 0.f : a.x[node];
-                    val = fmaf(xn * bx[jx * (BR + 1)] * by[jy * (BR + 1)], bz[jz * (BR + 1)], val);
+                if (inner) {
+                    sm.woff[d] = -1;
+                } else {
+                    sm.woff[d] = off;
+                    off += sm.wext[d][0] * sm.wext[d][1] * sm.wext[d][2];
                 }
             }
-            for (int l = r; l >= 0; --l) {
-                const float* xs = xL + 27 * l;
-                const float* bx = Bt + ((l * 3 + 0) * 3) * (BR + 1) + ku;
-                const float* by = Bt + ((l * 3 + 1) * 3) * (BR + 1) + kv;
-                const float* bz = Bt + ((l * 3 + 2) * 3) * (BR + 1) + kw;
-#pragma unroll
-                for (int j = 0; j < 27; ++j)
-                    val = fmaf(xs[j] * bx[(j / 9) * (BR + 1)] * by[((j / 3) % 3) * (BR + 1)], bz[(j % 3) * (BR + 1)], val);
+            sm.foreign = 0;
+            sm.cull = 0;
+            if (off > BR_XW) {                        // cannot happen for 8-aligned bricks
+                atomicExch(err, 1);
+                for (int d = r + 1; d <= D; ++d) sm.woff[d] = -2;
             }
-            lat[lat_prefix[B.root] + ((i64)u * S1 + w) * S1 + z] = val - v.iso;
         }
-        // corners on the leaf's lower faces
-        if (B.bu == 0 || B.bv == 0 || B.bw == 0) {
-            for (int e = threadIdx.x; e < nc; e += blockDim.x) {
-                const int ku = e / ((BR + 1) * (BR + 1)), kv = (e / (BR + 1)) % (BR + 1), kw = e % (BR + 1);
-                const int u = c0[0] + ku, w = c0[1] + kv, z = c0[2] + kw;
-                if (!(u == 0 || w == 0 || z == 0)) continue;
-                const int qc[3] = {Lc[0] * S + u, Lc[1] * S + w, Lc[2] * S + z};
-                u64 best = ~0ull;
-                int own_root = -1, oc[3] = {0, 0, 0};
-                for (int eo = 0; eo < 8; ++eo) {
-                    const int cell[3] = {qc[0] - (eo & 1), qc[1] - ((eo >> 1) & 1), qc[2] - ((eo >> 2) & 1)};
-                    const int m = batch_member(v, R, Lc, cell);
-                    if (m < 0) continue;
-                    const u64 kk = cell_key_D(cell, D);
-                    if (kk < best) { best = kk; own_root = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
+        if ((int)threadIdx.x <= r) {
+            int node = L;
+            for (int l = r; l > (int)threadIdx.x; --l) node = nd.parent[node];
+            for (int j = 0; j < 27; ++j) sm.xL[27 * threadIdx.x + j] = x_or_zero(a, nd.neigh[(i64)j * nd.M + node]);
+        }
+        for (int e = threadIdx.x; e < (D + 1) * 9 * BR1; e += blockDim.x) {
+            const int k = e % BR1, t = (e / BR1) % 3, ax = (e / (3 * BR1)) % 3, d = e / (9 * BR1);
+            const int uu = c0[ax] + k;
+            int cidx;
+            if (d <= r) cidx = (Lc[ax] >> (r - d)) + t - 1;
+            else cidx = ((Lc[ax] * S + uu - 1) >> (D - d)) + t - 1;
+            float val = 0.f;
+            if (cidx >= 0 && cidx < (1 << d))
+                val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(Lc[ax] * S + uu) * inv);
+            sm.Bt[((d * 3 + ax) * 3 + t) * BR1 + k] = val;
+        }
+        __syncthreads();
+        if (sm.woff[D] == -2) continue;              // layout overflow (reported through err)
+        // ---- 2a. basis ranges per window coordinate: corners k whose owner cell is within 1 of it
+        for (int e = threadIdx.x; e < (D - r) * 3 * BR_WEXT; e += blockDim.x) {
+            const int n = e % BR_WEXT, ax = (e / BR_WEXT) % 3, d = r + 1 + e / (3 * BR_WEXT);
+            if (sm.woff[d] < 0 || n >= sm.wext[d][ax]) continue;
+            const int sh = D - d, lim = 1 << d;
+            const int N = sm.wlo[d][ax] + n;
+            float mn = 0.f, mx = 0.f;                 // 0: corners without this term
+            if (N >= 0 && N < lim) {
+                for (int k = 0; k <= BR; ++k) {
+                    const int Va = (g0[ax] + k - 1) >> sh;
+                    const int Vb = (k == 0 && c0[ax] == 0) ? (g0[ax] >> sh) : Va;   // lower-face owner cell
+                    if (N < Va - 1 || N > Vb + 1) continue;
+                    const float b = cpoly_value<3>(a.basis[lim - 1 + N], (float)(g0[ax] + k) * inv);
+                    mn = fminf(mn, b);
+                    mx = fmaxf(mx, b);
                 }
-                lat[lat_prefix[B.root] + ((i64)u * S1 + w) * S1 + z] =
-                    virtual_corner_value(v, own_root, r, oc, qc) - v.iso;
             }
+            sm.Wlo[(d * 3 + ax) * BR_WEXT + n] = mn;
+            sm.Whi[(d * 3 + ax) * BR_WEXT + n] = mx;
+        }
+        __syncthreads();
+        // ---- 2b. window coefficients and the bound
+        double lo = 0, hi = 0, amax = 0, cnt = 0;
+        for (int t = threadIdx.x; t < 27 * (r + 1); t += blockDim.x) {
+            const int l = r - t / 27, j = t % 27;
+            const float x = sm.xL[27 * l + j];
+            if (x == 0.f) continue;
+            const int tt[3] = {j / 9, (j / 3) % 3, j % 3};
+            float blo[3], bhi[3];
+            for (int ax = 0; ax < 3; ++ax) {
+                const float* row = sm.Bt + ((l * 3 + ax) * 3 + tt[ax]) * BR1;
+                float mn = row[0], mx = row[0];
+                for (int k = 1; k <= BR; ++k) { mn = fminf(mn, row[k]); mx = fmaxf(mx, row[k]); }
+                blo[ax] = mn;
+                bhi[ax] = mx;
+            }
+            double tl, th;
+            term_interval((double)x, blo, bhi, tl, th);
+            lo += tl; hi += th;
+            amax += fmax(fabs(tl), fabs(th));
+            cnt += 1;
+        }
+        for (int d = r + 1; d <= D; ++d) {
+            const int off = sm.woff[d];
+            if (off < 0) continue;
+            const int e0 = sm.wext[d][0], e1 = sm.wext[d][1], e2 = sm.wext[d][2];
+            for (int t = threadIdx.x; t < e0 * e1 * e2; t += blockDim.x) {
+                const int n[3] = {t / (e1 * e2), (t / e2) % e1, t % e2};
+                const int N[3] = {sm.wlo[d][0] + n[0], sm.wlo[d][1] + n[1], sm.wlo[d][2] + n[2]};
+                const i64 node = shell_node(v, L, r, Lc, d, N);
+                const float x = node < 0 ? 0.f : a.x[node];
+                sm.Xw[off + t] = x;
+                if (node < 0) continue;
+                float blo[3], bhi[3];
+                for (int ax = 0; ax < 3; ++ax) {
+                    blo[ax] = sm.Wlo[(d * 3 + ax) * BR_WEXT + n[ax]];
+                    bhi[ax] = sm.Whi[(d * 3 + ax) * BR_WEXT + n[ax]];
+                }
+                double tl, th;
+                term_interval((double)x, blo, bhi, tl, th);
+                lo += tl; hi += th;
+                amax += fmax(fabs(tl), fabs(th));
+                cnt += 1;
+            }
+        }
+        // lower-face corners owned by another leaf of the batch
+        if (lower && r >= 3) {
+            for (int e = threadIdx.x; e < BR1 * BR1 * BR1; e += blockDim.x) {
+                const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
+                const int uu = c0[0] + kk[0], ww = c0[1] + kk[1], zz = c0[2] + kk[2];
+                if (!(uu == 0 || ww == 0 || zz == 0)) continue;
+                const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
+                int oc[3];
+                if (lower_face_owner(v, R, Lc, qc, oc) != L) atomicOr(&sm.foreign, 1);
+            }
+        }
+        {
+            double vals[4] = {lo, hi, amax, cnt};
+            for (int k = 0; k < 4; ++k) {
+                double x = vals[k];
+                for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if ((threadIdx.x & 31) == 0) sm.red[k][threadIdx.x >> 5] = x;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum[4] = {0, 0, 0, 0};
+            for (int k = 0; k < 4; ++k)
+                for (int w = 0; w < BR_BLOCK / 32; ++w) sum[k] += sm.red[k][w];
+            const double iso = (double)v.iso;
+            const double margin = (sum[3] + 4.0) * u * sum[2] + 2.0 * u * (fabs(sum[0]) + fabs(sum[1]) + 2.0 * fabs(iso)) +
+                                  1e-12 * (sum[2] + fabs(iso));
+            const bool above = sum[0] - margin > iso, below = sum[1] + margin < iso;
+            sm.cull = (!sm.foreign && (above || below)) ? 1 : 0;
+            culled[bi] = (unsigned char)sm.cull;
+            if (!sm.cull) atomicAdd(live, 1ull);
+        }
+        __syncthreads();
+        if (sm.cull) continue;
+        // ---- 4. exact corner values
+        float* out = lat + lat_prefix[B.root];
+        for (int e = threadIdx.x; e < BR1 * BR1 * BR1; e += blockDim.x) {
+            const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
+            const int uu = c0[0] + kk[0], ww = c0[1] + kk[1], zz = c0[2] + kk[2];
+            const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
+            float val;
+            if (uu && ww && zz) {
+                const int oc[3] = {qc[0] - 1, qc[1] - 1, qc[2] - 1};
+                val = brick_corner(sm, a, r, Lc, oc, qc, kk, true);
+            } else {
+                int oc[3] = {0, 0, 0};
+                const int own = lower_face_owner(v, R, Lc, qc, oc);
+                val = (own == L) ? brick_corner(sm, a, r, Lc, oc, qc, kk, false)
+                                 : virtual_corner_value(v, own, r, oc, qc);
+            }
+            out[((i64)uu * S1 + ww) * S1 + zz] = val - v.iso;
         }
     }
 }
@@ -896,11 +981,6 @@ __global__ void k_vertex_ids(const u64* __restrict__ keys, const uint32_t* __res
             vpos[3 * (i64)vid + 2] = epos[3 * (i64)sl + 2];
         }
     }
-}
-// live (not culled) flag per brick
-__global__ void k_flags_from_bytes(const unsigned char* __restrict__ culled, i64 n, int* __restrict__ f) {
-    for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
-        f[k] = culled[k] ? 0 : 1;
 }
 __global__ void k_key_heads(const u64* __restrict__ keys, i64 n, int* __restrict__ f) {
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
@@ -1103,31 +1183,28 @@ void stage_mesh(Ctx& c) {
             CK(cudaMemcpyAsync(dbig, big_list.data(), big_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
             CK(cudaMemcpyAsync(dbpre, brick_prefix.data(), brick_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
             BrickIndex bix{dbig, dbpre, (int)big_list.size()};
-            const int kb = c.kbegin("brick_bounds", (double)nbricks * 1);
-            k_brick_bounds<<<grid_for(nbricks, 1, 152 * 64), BR_BLOCK, 0, s>>>(va, bix, nbricks, culled);
+            // work counter, live-brick count, layout error flag
+            unsigned long long* wk = dalloc<unsigned long long>(3, s);
+            CK(cudaMemsetAsync(wk, 0, 3 * sizeof(unsigned long long), s));
+            int per_sm = 0;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bricks, BR_BLOCK, 0));
+            const i64 grid = std::min<i64>(nbricks, (i64)c.sms * std::max(per_sm, 1));
+            // compulsory: the brick's lattice corners written once
+            const int kb = c.kbegin("bricks", (double)nbricks * BR1 * BR1 * BR1 * 4);
+            k_bricks<<<(unsigned)grid, BR_BLOCK, 0, s>>>(va, bix, nbricks, wk, wk + 1, culled, lat_prefix, lat,
+                                                          (int*)(wk + 2));
             CK_LAUNCH();
             c.kend(kb);
-            // non-culled bricks
-            int* bf = dalloc<int>(nbricks, s);
-            int* bp = dalloc<int>(nbricks + 1, s);
-            k_flags_from_bytes<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
-            CK_LAUNCH();
-            exclusive_scan<int, int>(bf, bp, nbricks, bp + nbricks, s);
-            const i64 nlive = read_scalar(bp + nbricks, s);
-            c.live_bricks = nlive;
-            c.total_bricks = nbricks;
-            if (nlive > 0) {
-                i64* live = dalloc<i64>(nlive, s);
-                k_compact_idx<i64><<<grid_for(nbricks, 256), 256, 0, s>>>(bf, bp, nbricks, live);
-                CK_LAUNCH();
-                const int ke = c.kbegin("brick_eval", (double)nlive * (BR + 1) * (BR + 1) * (BR + 1) * 4);
-                k_brick_eval<<<grid_for(nlive, 1, 152 * 64), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_prefix, lat);
-                CK_LAUNCH();
-                c.kend(ke);
-                dfree(live, s);
+            unsigned long long hw[3];
+            CK(cudaMemcpyAsync(hw, wk, sizeof hw, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            dfree(wk, s);
+            c.live_bricks = (i64)hw[1];
+            if (hw[2]) {
+                set_last_error("brick window layout overflow");
+                throw Error{PRGPU_ERR_LIMIT, {0}};
             }
-            dfree(bf, s);
-            dfree(bp, s);
+            c.total_bricks = nbricks;
             dfree(dbig, s);
             dfree(dbpre, s);
         }
