@@ -39,6 +39,36 @@ struct StageTimes {
     float octree_ms = 0, basis_ms = 0, splat_ms = 0, divergence_ms = 0, solve_ms = 0, iso_ms = 0, mesh_ms = 0;
 };
 
+// page-locked host array that grows and keeps its capacity (mesh output)
+template <class T>
+struct PinnedBuf {
+    T* ptr = nullptr;
+    i64 n = 0, cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() {
+        if (ptr) cudaFreeHost(ptr);
+    }
+    void resize(i64 m) {
+        if (m > cap) {
+            if (ptr) cudaFreeHost(ptr);
+            ptr = nullptr;
+            cap = 0;
+            n = 0;
+            const i64 want = std::max<i64>(m, cap + cap / 4);
+            CK(cudaMallocHost((void**)&ptr, (size_t)want * sizeof(T)));
+            cap = want;
+        }
+        n = m;
+    }
+    void clear() { n = 0; }
+    i64 size() const { return n; }
+    T* data() { return ptr; }
+    const T* data() const { return ptr; }
+    T& operator[](i64 k) { return ptr[k]; }
+};
+
 struct Ctx {
     prgpu_params params;
     int device = 0;
@@ -85,8 +115,8 @@ struct Ctx {
     float iso = 0.f;
 
     // mesh (host, input coordinates)
-    std::vector<float> mesh_v;
-    std::vector<int32_t> mesh_f;
+    PinnedBuf<float> mesh_v;
+    PinnedBuf<int32_t> mesh_f;
     std::vector<int> has_tri, has_int;
     i64 subdivide_roots = 0;
     std::vector<i64> batch_tri;

@@ -299,9 +299,6 @@ struct VRoot {
     int depth;         // r
     int batch;         // vertex-sharing batch id (1-based)
     int pad;
-    i64 lattice_base;  // first corner value of this root
-    i64 cell_base;     // first virtual cell of this root
-    i64 brick_base;    // first brick of this root, -1 for small roots (lattice edge <= 8)
 };
 
 struct VArgs {
@@ -397,7 +394,7 @@ __device__ __forceinline__ u64 cell_key_D(const int c[3], int D) { return coords
 
 // one thread per lattice corner of the listed roots (the small ones)
 __global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i64* __restrict__ list_prefix,
-                                  int nlist, i64 total, const i64* __restrict__ lat_prefix, float* __restrict__ lat) {
+                                  int nlist, i64 total, float* __restrict__ lat) {
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
         int lo = 0, hi = nlist - 1;
         while (lo < hi) {
@@ -422,48 +419,64 @@ __global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i
             const u64 kk = cell_key_D(cell, D);
             if (kk < best) { best = kk; own_root = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
         }
-        lat[lat_prefix[ri] + loc] = virtual_corner_value(v, own_root, R.depth, oc, qc) - v.iso;
+        lat[e] = virtual_corner_value(v, own_root, R.depth, oc, qc) - v.iso;
     }
 }
 
 // ---- large subdivided leaves (lattice edge >= 16): bricks of 8^3 cells.
 //
-// Most corners of a large subdivided leaf lie far from the surface.  One block
-// takes one brick (8^3 cells, 9^3 corners) at a time:
-//   1. it gathers into shared memory every coefficient the brick's corners can
-//      read: the 27 neighbours of the leaf and of each ancestor, and at every
-//      virtual depth the window of cells around the brick's owner cells (real
-//      nodes outside the leaf, 0 where there is none);
-//   2. it bounds the brick's corner values: each term is x_n * B_x * B_y * B_z
-//      with the single-precision basis values the evaluation uses, so the range
-//      of a term over the corners that include it is an interval product, and
-//      the rounding of the FMA chain is at most (K + 4) u sum|term| for K terms
-//      (u = 2^-24); terms only some corners include get intervals widened to 0;
-//   3. if the bound proves that every corner value has the same sign as
-//      (value - iso), the brick is culled: none of its cells carries a triangle
-//      and its corners are never read;
-//   4. otherwise every corner is evaluated from the shared window in the order
-//      of virtual_corner_value, so culling changes no value.
-// Corners on the leaf's lower faces may be owned by a cell of another leaf of
-// the same depth batch: those go through virtual_corner_value, and a brick with
-// such a corner is never culled.
+// Most corners of a large subdivided leaf lie far from the surface.  The leaf
+// is cut into bricks of 8^3 cells (9^3 corners) and each brick is bounded
+// before any of its corners is evaluated:
+//   * every term of a corner value is x_n * B_x * B_y * B_z with the
+//     single-precision basis values the evaluation uses, so the range of a term
+//     over the corners that include it is an interval product; terms that only
+//     some corners include get intervals widened to 0;
+//   * the rounding of the FMA chain is at most (K + 4) u sum|term| for K terms
+//     (u = 2^-24);
+//   * a brick whose bound proves that every corner value has the same sign as
+//     (value - iso) is culled: none of its cells carries a triangle and its
+//     corners are never read.
+// The surviving ("live") bricks are evaluated exactly, in the order of
+// virtual_corner_value, so culling changes no value.  Corners on the leaf's
+// lower faces may be owned by a cell of another leaf of the same depth batch:
+// those go through virtual_corner_value, and a brick with such a corner is
+// never culled.
+//
+// Everything a brick needs along one axis depends only on the leaf, the axis
+// and the brick's index along it (a "brick row"), so it is tabulated once per
+// row by k_brick_rows:
+//   BT[d][t][k]   basis value at corner k of the function of cell V_k + t - 1
+//                 (depth d > r, V_k the owner cell of corner k) or of ancestor
+//                 cell + t - 1 (depth d <= r)
+//   RA[l][t]      range over k of BT[l][t][k], l <= r
+//   RW[d][n]      range (with 0) of the depth-d function of window cell n over
+//                 the corners whose owner cell is within one cell of it
 constexpr int BR = 8;              // brick edge (cells); corners per axis BR+1
 constexpr int BR1 = BR + 1;
+constexpr int BR_CORNERS = BR1 * BR1 * BR1;
+constexpr int BR_CELLS = BR * BR * BR;
 constexpr int BR_BLOCK = 128;
 constexpr int BR_LEVELS = 16;      // depths 0..15
 constexpr int BR_WEXT = BR + 3;    // window edge at the finest depth
 // window cells over all virtual depths of a brick whose first corner is a
 // multiple of 8: 11^3 + 7^3 + 5^3 + 12 * 4^3 = 2567
 constexpr int BR_XW = 2600;
+// brick-row table: BT (27 per depth), RA (6 per depth), RW (22 per depth)
+constexpr int ROW_BT = 0, ROW_RA = 27, ROW_RW = 33, ROW_PER_DEPTH = 55;
 
-struct VBrick {
-    int root;                      // index into roots
-    int bu, bv, bw;
-};
 struct BrickIndex {                // bricks of the large roots, numbered root by root
     const int* big;                // root indices of the large roots
     const i64* prefix;             // first brick of each large root
+    const i64* row_prefix;         // first brick row of each large root (3 * bricks per edge rows each)
     int nbig;
+    const float* rows;             // brick-row tables, 55 (D+1) floats each
+    const float* xl;               // per large root: x of the 27 neighbours of each ancestor, 16 x 27
+};
+struct VBrick {
+    int root;                      // index into roots
+    int big;                       // index into the large roots
+    int b[3];                      // brick coordinates in the leaf
 };
 __device__ __forceinline__ VBrick brick_of(const VArgs& v, const BrickIndex& bx, i64 g) {
     int lo = 0, hi = bx.nbig - 1;
@@ -472,13 +485,17 @@ __device__ __forceinline__ VBrick brick_of(const VArgs& v, const BrickIndex& bx,
         if (bx.prefix[mid] <= g) lo = mid; else hi = mid - 1;
     }
     VBrick b;
+    b.big = lo;
     b.root = bx.big[lo];
     const int nb = (1 << (v.e.D - v.roots[b.root].depth)) / BR;
     const i64 l = g - bx.prefix[lo];
-    b.bu = (int)(l / ((i64)nb * nb));
-    b.bv = (int)((l / nb) % nb);
-    b.bw = (int)(l % nb);
+    b.b[0] = (int)(l / ((i64)nb * nb));
+    b.b[1] = (int)((l / nb) % nb);
+    b.b[2] = (int)(l % nb);
     return b;
+}
+__device__ __forceinline__ const float* brick_row(const BrickIndex& bx, int D, int big, int nb, int ax, int b) {
+    return bx.rows + (bx.row_prefix[big] + (i64)ax * nb + b) * (i64)(ROW_PER_DEPTH * (D + 1));
 }
 
 __device__ __forceinline__ float x_or_zero(const EvalArgs& a, int node) { return node < 0 ? 0.f : a.x[node]; }
@@ -508,19 +525,90 @@ __device__ __forceinline__ void term_interval(double x, const float* lo, const f
     thi = b;
 }
 
-struct BrickShared {
-    float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
-    float Bt[BR_LEVELS * 9 * BR1];            // [depth][axis][t][k]: basis value of owner cell + t - 1 at corner k
-    float Xw[BR_XW];                          // window coefficients, virtual depths
-    float Wlo[BR_LEVELS * 3 * BR_WEXT];       // per window coordinate: basis range over the corners using it
-    float Whi[BR_LEVELS * 3 * BR_WEXT];
-    int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
-    int wext[BR_LEVELS][3];
-    int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
-    double red[4][BR_BLOCK / 32];
-    int foreign;                              // a lower-face corner is owned by another leaf
-    int cull;
-};
+// window of depth d around a brick along one axis: origin and extent of the
+// cells the brick's owner cells can reach; 'cross' when that reaches outside the leaf
+__device__ __forceinline__ void window_axis(int g0, int Lc_ax, int r, int d, int D, int& wlo, int& ext, bool& cross) {
+    const int sh = D - d, span = 1 << (d - r);
+    const int Vlo = (g0 - 1) >> sh, Vhi = (g0 + BR - 1) >> sh;
+    const int llo = Lc_ax * span;
+    cross = (Vlo - 1 < llo || Vhi + 1 >= llo + span);
+    wlo = Vlo - 1;
+    ext = Vhi - Vlo + 3;
+}
+
+// one thread per (brick row, depth)
+__global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrows, float* __restrict__ rows) {
+    const EvalArgs& a = v.e;
+    const int D = a.D;
+    const float inv = 1.0f / (float)(1 << D);
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < nrows * (D + 1); e += (i64)gridDim.x * blockDim.x) {
+        const i64 row = e / (D + 1);
+        const int d = (int)(e % (D + 1));
+        const int4 rd = rowdesc[row];             // root, axis, brick index
+        const VRoot R = v.roots[rd.x];
+        const int ax = rd.y, r = R.depth, S = 1 << (D - r);
+        int Lc[3];
+        key_coords(a.nd.key[R.node], r, D, Lc);
+        const int g0 = Lc[ax] * S + rd.z * BR;
+        const int c0 = rd.z * BR;
+        float* out = rows + row * (i64)(ROW_PER_DEPTH * (D + 1));
+        float bt[3][BR1];
+        for (int t = 0; t < 3; ++t)
+            for (int k = 0; k <= BR; ++k) {
+                const int cidx = (d <= r) ? (Lc[ax] >> (r - d)) + t - 1 : ((g0 + k - 1) >> (D - d)) + t - 1;
+                float val = 0.f;
+                if (cidx >= 0 && cidx < (1 << d)) val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(g0 + k) * inv);
+                bt[t][k] = val;
+                out[ROW_BT * (D + 1) + (d * 3 + t) * BR1 + k] = val;
+            }
+        if (d <= r) {
+            for (int t = 0; t < 3; ++t) {
+                float mn = bt[t][0], mx = bt[t][0];
+                for (int k = 1; k <= BR; ++k) { mn = fminf(mn, bt[t][k]); mx = fmaxf(mx, bt[t][k]); }
+                out[ROW_RA * (D + 1) + (d * 3 + t) * 2] = mn;
+                out[ROW_RA * (D + 1) + (d * 3 + t) * 2 + 1] = mx;
+            }
+        } else {
+            int wlo, ext;
+            bool cross;
+            window_axis(g0, Lc[ax], r, d, D, wlo, ext, cross);
+            const int sh = D - d, lim = 1 << d;
+            for (int n = 0; n < BR_WEXT; ++n) {
+                const int N = wlo + n;
+                float mn = 0.f, mx = 0.f;             // 0: corners without this term
+                if (n < ext && N >= 0 && N < lim) {
+                    for (int k = 0; k <= BR; ++k) {
+                        const int Va = (g0 + k - 1) >> sh;
+                        const int Vb = (k == 0 && c0 == 0) ? (g0 >> sh) : Va;   // lower-face owner cell
+                        if (N < Va - 1 || N > Vb + 1) continue;
+                        const float b = cpoly_value<3>(a.basis[lim - 1 + N], (float)(g0 + k) * inv);
+                        mn = fminf(mn, b);
+                        mx = fmaxf(mx, b);
+                    }
+                }
+                out[ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2] = mn;
+                out[ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2 + 1] = mx;
+            }
+        }
+    }
+}
+
+// x of the 27 neighbours of each ancestor of a large root (0: no neighbour)
+__global__ void k_brick_xl(VArgs v, const int* __restrict__ big, int nbig, float* __restrict__ xl) {
+    const NodeArrays& nd = v.e.nd;
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < (i64)nbig * BR_LEVELS * 27;
+         e += (i64)gridDim.x * blockDim.x) {
+        const int bi = (int)(e / (BR_LEVELS * 27)), l = (int)((e / 27) % BR_LEVELS), j = (int)(e % 27);
+        const VRoot R = v.roots[big[bi]];
+        float x = 0.f;
+        if (l <= R.depth) {
+            int node = R.node;
+            for (int q = R.depth; q > l; --q) node = nd.parent[node];
+            x = x_or_zero(v.e, nd.neigh[(i64)j * nd.M + node]);
+        }
+        xl[e] = x;
+    }
+}
 
 // owner of a lower-face corner (min key among batch cells sharing it)
 __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, const int Lc[3], const int qc[3],
@@ -537,9 +625,115 @@ __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, 
     return own;
 }
 
-// value of corner k (brick-local kk[], global qc[]) owned by the brick's leaf
-// through owner cell oc[], from the shared window; 'interior' means oc = qc - 1
-// so the tabulated basis values apply
+// one warp per brick: the bound, and the culled flag
+constexpr int BB_BLOCK = 256;
+__global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bix, i64 nbricks,
+                                                          unsigned char* __restrict__ culled) {
+    const EvalArgs& a = v.e;
+    const int D = a.D;
+    const int lane = threadIdx.x & 31;
+    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    const double u = 5.9604644775390625e-08;   // 2^-24
+    for (i64 bi = warp; bi < nbricks; bi += nwarps) {
+        const VBrick B = brick_of(v, bix, bi);
+        const VRoot R = v.roots[B.root];
+        const int r = R.depth, S = 1 << (D - r), L = R.node, nb = S / BR;
+        int Lc[3];
+        key_coords(a.nd.key[L], r, D, Lc);
+        const int g0[3] = {Lc[0] * S + B.b[0] * BR, Lc[1] * S + B.b[1] * BR, Lc[2] * S + B.b[2] * BR};
+        const float* row[3];
+        for (int ax = 0; ax < 3; ++ax) row[ax] = brick_row(bix, D, B.big, nb, ax, B.b[ax]);
+        const float* xl = bix.xl + (i64)B.big * BR_LEVELS * 27;
+        double lo = 0, hi = 0, amax = 0, cnt = 0;
+        // the leaf and its ancestors
+        for (int t = lane; t < 27 * (r + 1); t += 32) {
+            const int l = r - t / 27, j = t % 27;
+            const float x = xl[27 * l + j];
+            if (x == 0.f) continue;
+            const int tt[3] = {j / 9, (j / 3) % 3, j % 3};
+            float blo[3], bhi[3];
+            for (int ax = 0; ax < 3; ++ax) {
+                blo[ax] = row[ax][ROW_RA * (D + 1) + (l * 3 + tt[ax]) * 2];
+                bhi[ax] = row[ax][ROW_RA * (D + 1) + (l * 3 + tt[ax]) * 2 + 1];
+            }
+            double tl, th;
+            term_interval((double)x, blo, bhi, tl, th);
+            lo += tl; hi += th;
+            amax += fmax(fabs(tl), fabs(th));
+            cnt += 1;
+        }
+        // real nodes around the leaf, at the virtual depths
+        for (int d = r + 1; d <= D; ++d) {
+            int wlo[3], ext[3];
+            bool cross = false;
+            for (int ax = 0; ax < 3; ++ax) {
+                bool c;
+                window_axis(g0[ax], Lc[ax], r, d, D, wlo[ax], ext[ax], c);
+                cross |= c;
+            }
+            if (!cross) continue;
+            const int ncell = ext[0] * ext[1] * ext[2];
+            for (int t = lane; t < ncell; t += 32) {
+                const int n[3] = {t / (ext[1] * ext[2]), (t / ext[2]) % ext[1], t % ext[2]};
+                const int N[3] = {wlo[0] + n[0], wlo[1] + n[1], wlo[2] + n[2]};
+                const i64 node = shell_node(v, L, r, Lc, d, N);
+                if (node < 0) continue;
+                float blo[3], bhi[3];
+                for (int ax = 0; ax < 3; ++ax) {
+                    blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n[ax]) * 2];
+                    bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n[ax]) * 2 + 1];
+                }
+                double tl, th;
+                term_interval((double)a.x[node], blo, bhi, tl, th);
+                lo += tl; hi += th;
+                amax += fmax(fabs(tl), fabs(th));
+                cnt += 1;
+            }
+        }
+        // lower-face corners owned by another leaf of the batch
+        int foreign = 0;
+        if (r >= 3 && (B.b[0] == 0 || B.b[1] == 0 || B.b[2] == 0)) {
+            for (int e = lane; e < BR_CORNERS; e += 32) {
+                const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
+                const int uu = B.b[0] * BR + kk[0], ww = B.b[1] * BR + kk[1], zz = B.b[2] * BR + kk[2];
+                if (uu && ww && zz) continue;
+                const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
+                int oc[3];
+                if (lower_face_owner(v, R, Lc, qc, oc) != L) foreign = 1;
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            lo += __shfl_xor_sync(0xffffffffu, lo, o);
+            hi += __shfl_xor_sync(0xffffffffu, hi, o);
+            amax += __shfl_xor_sync(0xffffffffu, amax, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            foreign |= __shfl_xor_sync(0xffffffffu, foreign, o);
+        }
+        if (lane == 0) {
+            const double iso = (double)v.iso;
+            const double margin = (cnt + 4.0) * u * amax + 2.0 * u * (fabs(lo) + fabs(hi) + 2.0 * fabs(iso)) +
+                                  1e-12 * (amax + fabs(iso));
+            const bool above = lo - margin > iso, below = hi + margin < iso;
+            culled[bi] = (!foreign && (above || below)) ? 1 : 0;
+        }
+    }
+}
+
+struct BrickShared {
+    float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
+    float Bt[3 * BR_LEVELS * 27];             // [axis][depth][t][k], from the brick-row tables
+    float Xw[BR_XW];                          // window coefficients, virtual depths
+    int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
+    int wext[BR_LEVELS][3];
+    int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
+};
+__device__ __forceinline__ float bt_at(const BrickShared& sm, int ax, int d, int t, int k) {
+    return sm.Bt[(ax * BR_LEVELS + d) * 27 + t * BR1 + k];
+}
+
+// value of a corner owned by the brick's leaf through owner cell oc[], from the
+// shared window; 'interior' means oc = qc - 1 so the tabulated basis values apply
 __device__ __forceinline__ float brick_corner(const BrickShared& sm, const EvalArgs& a, int r, const int Lc[3],
                                               const int oc[3], const int qc[3], const int kk[3], bool interior) {
     const int D = a.D;
@@ -559,7 +753,7 @@ __device__ __forceinline__ float brick_corner(const BrickShared& sm, const EvalA
         float bv[3][3];
         if (interior) {
             for (int ax = 0; ax < 3; ++ax)
-                for (int t = 0; t < 3; ++t) bv[ax][t] = sm.Bt[((d * 3 + ax) * 3 + t) * BR1 + kk[ax]];
+                for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, d, t, kk[ax]);
         } else {
             const int fb = (1 << d) - 1, lim = 1 << d;
             for (int ax = 0; ax < 3; ++ax)
@@ -582,193 +776,81 @@ __device__ __forceinline__ float brick_corner(const BrickShared& sm, const EvalA
     // the leaf itself and its real ancestors (walk_up with absent neighbours as 0)
     for (int l = r; l >= 0; --l) {
         const float* xs = sm.xL + 27 * l;
-        const float* bx = sm.Bt + ((l * 3 + 0) * 3) * BR1 + kk[0];
-        const float* by = sm.Bt + ((l * 3 + 1) * 3) * BR1 + kk[1];
-        const float* bz = sm.Bt + ((l * 3 + 2) * 3) * BR1 + kk[2];
-#pragma unroll
         for (int j = 0; j < 27; ++j)
-            val = fmaf(xs[j] * bx[(j / 9) * BR1] * by[((j / 3) % 3) * BR1], bz[(j % 3) * BR1], val);
+            val = fmaf(xs[j] * bt_at(sm, 0, l, j / 9, kk[0]) * bt_at(sm, 1, l, (j / 3) % 3, kk[1]),
+                       bt_at(sm, 2, l, j % 3, kk[2]), val);
     }
     return val;
 }
 
-// one brick at a time per block, taken from a work counter
-__global__ void __launch_bounds__(BR_BLOCK) k_bricks(VArgs v, BrickIndex bix, i64 nbricks,
-                                                     unsigned long long* __restrict__ work,
-                                                     unsigned long long* __restrict__ live,
-                                                     unsigned char* __restrict__ culled,
-                                                     const i64* __restrict__ lat_prefix, float* __restrict__ lat,
-                                                     int* __restrict__ err) {
+__device__ __noinline__ float foreign_corner_value(const VArgs& v, int own, int r, const int oc[3], const int qc[3]) {
+    return virtual_corner_value(v, own, r, oc, qc);
+}
+
+// one block per live brick: exact corner values into the brick's 9^3 slot
+__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const int4* __restrict__ live,
+                                                         i64 nlive, float* __restrict__ blat) {
     __shared__ BrickShared sm;
-    __shared__ long long sh_bi;
     const EvalArgs& a = v.e;
-    const NodeArrays& nd = a.nd;
     const int D = a.D;
-    const float inv = 1.0f / (float)(1 << D);
-    const double u = 5.9604644775390625e-08;   // 2^-24
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) sh_bi = (long long)atomicAdd(work, 1ull);
-        __syncthreads();
-        const i64 bi = sh_bi;
-        if (bi >= nbricks) break;
-        const VBrick B = brick_of(v, bix, bi);
-        const VRoot R = v.roots[B.root];
-        const int r = R.depth, S = 1 << (D - r), S1 = S + 1, L = R.node;
+    for (i64 li = blockIdx.x; li < nlive; li += gridDim.x) {
+        const int4 ld = live[li];                  // root, brick coordinates
+        const VRoot R = v.roots[ld.x];
+        const int r = R.depth, S = 1 << (D - r), L = R.node, nb = S / BR;
+        const int bb[3] = {ld.y, ld.z, ld.w};
         int Lc[3];
-        key_coords(nd.key[L], r, D, Lc);
-        const int c0[3] = {B.bu * BR, B.bv * BR, B.bw * BR};
-        const int g0[3] = {Lc[0] * S + c0[0], Lc[1] * S + c0[1], Lc[2] * S + c0[2]};   // first corner (global)
-        const bool lower = (B.bu == 0 || B.bv == 0 || B.bw == 0);
-        // ---- 1. window layout, leaf coefficients, basis table
+        key_coords(a.nd.key[L], r, D, Lc);
+        const int g0[3] = {Lc[0] * S + bb[0] * BR, Lc[1] * S + bb[1] * BR, Lc[2] * S + bb[2] * BR};
+        // the large-root index of this root (for the tables)
+        int big = 0;
+        {
+            int lo = 0, hi = bix.nbig - 1;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (bix.big[mid] < ld.x) lo = mid + 1; else hi = mid;
+            }
+            big = lo;
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
             int off = 0;
             for (int d = r + 1; d <= D; ++d) {
-                const int sh = D - d, span = 1 << (d - r);
-                bool inner = true;
+                bool cross = false;
                 for (int ax = 0; ax < 3; ++ax) {
-                    const int Vlo = (g0[ax] - 1) >> sh, Vhi = (g0[ax] + BR - 1) >> sh;
-                    const int llo = Lc[ax] * span;
-                    if (Vlo - 1 < llo || Vhi + 1 >= llo + span) inner = false;
-                    sm.wlo[d][ax] = Vlo - 1;
-                    sm.wext[d][ax] = Vhi - Vlo + 3;
+                    bool c;
+                    window_axis(g0[ax], Lc[ax], r, d, D, sm.wlo[d][ax], sm.wext[d][ax], c);
+                    cross |= c;
                 }
-                if (inner) {
-                    sm.woff[d] = -1;
-                } else {
+                if (cross) {
                     sm.woff[d] = off;
                     off += sm.wext[d][0] * sm.wext[d][1] * sm.wext[d][2];
+                } else {
+                    sm.woff[d] = -1;
                 }
             }
-            sm.foreign = 0;
-            sm.cull = 0;
-            if (off > BR_XW) {                        // cannot happen for 8-aligned bricks
-                atomicExch(err, 1);
-                for (int d = r + 1; d <= D; ++d) sm.woff[d] = -2;
-            }
         }
-        if ((int)threadIdx.x <= r) {
-            int node = L;
-            for (int l = r; l > (int)threadIdx.x; --l) node = nd.parent[node];
-            for (int j = 0; j < 27; ++j) sm.xL[27 * threadIdx.x + j] = x_or_zero(a, nd.neigh[(i64)j * nd.M + node]);
-        }
-        for (int e = threadIdx.x; e < (D + 1) * 9 * BR1; e += blockDim.x) {
-            const int k = e % BR1, t = (e / BR1) % 3, ax = (e / (3 * BR1)) % 3, d = e / (9 * BR1);
-            const int uu = c0[ax] + k;
-            int cidx;
-            if (d <= r) cidx = (Lc[ax] >> (r - d)) + t - 1;
-            else cidx = ((Lc[ax] * S + uu - 1) >> (D - d)) + t - 1;
-            float val = 0.f;
-            if (cidx >= 0 && cidx < (1 << d))
-                val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(Lc[ax] * S + uu) * inv);
-            sm.Bt[((d * 3 + ax) * 3 + t) * BR1 + k] = val;
+        for (int e = threadIdx.x; e < 27 * (r + 1); e += blockDim.x)
+            sm.xL[e] = bix.xl[(i64)big * BR_LEVELS * 27 + e];
+        for (int e = threadIdx.x; e < 3 * 27 * (D + 1); e += blockDim.x) {
+            const int ax = e / (27 * (D + 1)), q = e % (27 * (D + 1));
+            sm.Bt[ax * BR_LEVELS * 27 + q] = brick_row(bix, D, big, nb, ax, bb[ax])[ROW_BT * (D + 1) + q];
         }
         __syncthreads();
-        if (sm.woff[D] == -2) continue;              // layout overflow (reported through err)
-        // ---- 2a. basis ranges per window coordinate: corners k whose owner cell is within 1 of it
-        for (int e = threadIdx.x; e < (D - r) * 3 * BR_WEXT; e += blockDim.x) {
-            const int n = e % BR_WEXT, ax = (e / BR_WEXT) % 3, d = r + 1 + e / (3 * BR_WEXT);
-            if (sm.woff[d] < 0 || n >= sm.wext[d][ax]) continue;
-            const int sh = D - d, lim = 1 << d;
-            const int N = sm.wlo[d][ax] + n;
-            float mn = 0.f, mx = 0.f;                 // 0: corners without this term
-            if (N >= 0 && N < lim) {
-                for (int k = 0; k <= BR; ++k) {
-                    const int Va = (g0[ax] + k - 1) >> sh;
-                    const int Vb = (k == 0 && c0[ax] == 0) ? (g0[ax] >> sh) : Va;   // lower-face owner cell
-                    if (N < Va - 1 || N > Vb + 1) continue;
-                    const float b = cpoly_value<3>(a.basis[lim - 1 + N], (float)(g0[ax] + k) * inv);
-                    mn = fminf(mn, b);
-                    mx = fmaxf(mx, b);
-                }
-            }
-            sm.Wlo[(d * 3 + ax) * BR_WEXT + n] = mn;
-            sm.Whi[(d * 3 + ax) * BR_WEXT + n] = mx;
-        }
-        __syncthreads();
-        // ---- 2b. window coefficients and the bound
-        double lo = 0, hi = 0, amax = 0, cnt = 0;
-        for (int t = threadIdx.x; t < 27 * (r + 1); t += blockDim.x) {
-            const int l = r - t / 27, j = t % 27;
-            const float x = sm.xL[27 * l + j];
-            if (x == 0.f) continue;
-            const int tt[3] = {j / 9, (j / 3) % 3, j % 3};
-            float blo[3], bhi[3];
-            for (int ax = 0; ax < 3; ++ax) {
-                const float* row = sm.Bt + ((l * 3 + ax) * 3 + tt[ax]) * BR1;
-                float mn = row[0], mx = row[0];
-                for (int k = 1; k <= BR; ++k) { mn = fminf(mn, row[k]); mx = fmaxf(mx, row[k]); }
-                blo[ax] = mn;
-                bhi[ax] = mx;
-            }
-            double tl, th;
-            term_interval((double)x, blo, bhi, tl, th);
-            lo += tl; hi += th;
-            amax += fmax(fabs(tl), fabs(th));
-            cnt += 1;
-        }
         for (int d = r + 1; d <= D; ++d) {
             const int off = sm.woff[d];
             if (off < 0) continue;
             const int e0 = sm.wext[d][0], e1 = sm.wext[d][1], e2 = sm.wext[d][2];
             for (int t = threadIdx.x; t < e0 * e1 * e2; t += blockDim.x) {
-                const int n[3] = {t / (e1 * e2), (t / e2) % e1, t % e2};
-                const int N[3] = {sm.wlo[d][0] + n[0], sm.wlo[d][1] + n[1], sm.wlo[d][2] + n[2]};
+                const int N[3] = {sm.wlo[d][0] + t / (e1 * e2), sm.wlo[d][1] + (t / e2) % e1, sm.wlo[d][2] + t % e2};
                 const i64 node = shell_node(v, L, r, Lc, d, N);
-                const float x = node < 0 ? 0.f : a.x[node];
-                sm.Xw[off + t] = x;
-                if (node < 0) continue;
-                float blo[3], bhi[3];
-                for (int ax = 0; ax < 3; ++ax) {
-                    blo[ax] = sm.Wlo[(d * 3 + ax) * BR_WEXT + n[ax]];
-                    bhi[ax] = sm.Whi[(d * 3 + ax) * BR_WEXT + n[ax]];
-                }
-                double tl, th;
-                term_interval((double)x, blo, bhi, tl, th);
-                lo += tl; hi += th;
-                amax += fmax(fabs(tl), fabs(th));
-                cnt += 1;
-            }
-        }
-        // lower-face corners owned by another leaf of the batch
-        if (lower && r >= 3) {
-            for (int e = threadIdx.x; e < BR1 * BR1 * BR1; e += blockDim.x) {
-                const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
-                const int uu = c0[0] + kk[0], ww = c0[1] + kk[1], zz = c0[2] + kk[2];
-                if (!(uu == 0 || ww == 0 || zz == 0)) continue;
-                const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
-                int oc[3];
-                if (lower_face_owner(v, R, Lc, qc, oc) != L) atomicOr(&sm.foreign, 1);
-            }
-        }
-        {
-            double vals[4] = {lo, hi, amax, cnt};
-            for (int k = 0; k < 4; ++k) {
-                double x = vals[k];
-                for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-                if ((threadIdx.x & 31) == 0) sm.red[k][threadIdx.x >> 5] = x;
+                sm.Xw[off + t] = node < 0 ? 0.f : a.x[node];
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double sum[4] = {0, 0, 0, 0};
-            for (int k = 0; k < 4; ++k)
-                for (int w = 0; w < BR_BLOCK / 32; ++w) sum[k] += sm.red[k][w];
-            const double iso = (double)v.iso;
-            const double margin = (sum[3] + 4.0) * u * sum[2] + 2.0 * u * (fabs(sum[0]) + fabs(sum[1]) + 2.0 * fabs(iso)) +
-                                  1e-12 * (sum[2] + fabs(iso));
-            const bool above = sum[0] - margin > iso, below = sum[1] + margin < iso;
-            sm.cull = (!sm.foreign && (above || below)) ? 1 : 0;
-            culled[bi] = (unsigned char)sm.cull;
-            if (!sm.cull) atomicAdd(live, 1ull);
-        }
-        __syncthreads();
-        if (sm.cull) continue;
-        // ---- 4. exact corner values
-        float* out = lat + lat_prefix[B.root];
-        for (int e = threadIdx.x; e < BR1 * BR1 * BR1; e += blockDim.x) {
+        float* out = blat + li * BR_CORNERS;
+        for (int e = threadIdx.x; e < BR_CORNERS; e += blockDim.x) {
             const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
-            const int uu = c0[0] + kk[0], ww = c0[1] + kk[1], zz = c0[2] + kk[2];
+            const int uu = bb[0] * BR + kk[0], ww = bb[1] * BR + kk[1], zz = bb[2] * BR + kk[2];
             const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
             float val;
             if (uu && ww && zz) {
@@ -778,40 +860,82 @@ __global__ void __launch_bounds__(BR_BLOCK) k_bricks(VArgs v, BrickIndex bix, i6
                 int oc[3] = {0, 0, 0};
                 const int own = lower_face_owner(v, R, Lc, qc, oc);
                 val = (own == L) ? brick_corner(sm, a, r, Lc, oc, qc, kk, false)
-                                 : virtual_corner_value(v, own, r, oc, qc);
+                                 : foreign_corner_value(v, own, r, oc, qc);
             }
-            out[((i64)uu * S1 + ww) * S1 + zz] = val - v.iso;
+            out[e] = val - v.iso;
         }
     }
 }
 
-__global__ void k_virtual_cells(VArgs v, const i64* __restrict__ cell_prefix, const i64* __restrict__ lat_prefix,
-                                i64 total, const float* __restrict__ lat, const unsigned char* __restrict__ culled,
-                                unsigned char* __restrict__ cat, int* __restrict__ ntri) {
-    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
-        int lo = 0, hi = v.nroots - 1;
+// live bricks in brick order: root and brick coordinates
+__global__ void k_live_bricks(VArgs v, BrickIndex bix, const unsigned char* __restrict__ culled,
+                              const int* __restrict__ pos, i64 nbricks, int4* __restrict__ live) {
+    for (i64 bi = (i64)blockIdx.x * blockDim.x + threadIdx.x; bi < nbricks; bi += (i64)gridDim.x * blockDim.x) {
+        if (culled[bi]) continue;
+        const VBrick B = brick_of(v, bix, bi);
+        live[pos[bi]] = make_int4(B.root, B.b[0], B.b[1], B.b[2]);
+    }
+}
+__global__ void k_live_flags(const unsigned char* __restrict__ culled, i64 n, int* __restrict__ f) {
+    for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        f[k] = culled[k] ? 0 : 1;
+}
+
+// ---- virtual cells: the small leaves' lattices, then the live bricks
+struct VirtCells {
+    const int* small;              // root indices of the small leaves
+    const i64* small_cells;        // first cell of each small leaf
+    const i64* small_lat;          // first corner of each small leaf
+    int nsmall;
+    i64 cells_small;               // cells of all small leaves
+    const float* lat_small;        // corner values (minus iso) of the small leaves
+    const int4* live;              // live bricks: root, brick coordinates
+    const float* lat_brick;        // 9^3 corner values (minus iso) per live brick
+};
+
+// root, cell coordinates in the root's lattice and the 8 corner values of virtual cell e
+__device__ __forceinline__ int virt_cell(const VirtCells& vc, const VArgs& v, i64 e, int cu[3], float cv[8]) {
+    const int D = v.e.D;
+    if (e < vc.cells_small) {
+        int lo = 0, hi = vc.nsmall - 1;
         while (lo < hi) {
             int mid = (lo + hi + 1) >> 1;
-            if (cell_prefix[mid] <= e) lo = mid; else hi = mid - 1;
+            if (vc.small_cells[mid] <= e) lo = mid; else hi = mid - 1;
         }
-        const VRoot R = v.roots[lo];
-        const int S = 1 << (v.e.D - R.depth), S1 = S + 1;
-        const i64 loc = e - cell_prefix[lo];
-        const int u = (int)(loc / ((i64)S * S)), w = (int)((loc / S) % S), z = (int)(loc % S);
-        if (R.brick_base >= 0) {
-            const int nb = S / BR;
-            if (culled[R.brick_base + ((i64)(u / BR) * nb + (w / BR)) * nb + (z / BR)]) {
-                cat[e] = 0;
-                ntri[e] = 0;
-                continue;
-            }
-        }
-        const float* L = lat + lat_prefix[lo];
+        const int root = vc.small[lo];
+        const int S = 1 << (D - v.roots[root].depth), S1 = S + 1;
+        const i64 loc = e - vc.small_cells[lo];
+        cu[0] = (int)(loc / ((i64)S * S));
+        cu[1] = (int)((loc / S) % S);
+        cu[2] = (int)(loc % S);
+        const float* L = vc.lat_small + vc.small_lat[lo];
+        for (int kind = 0; kind < 8; ++kind)
+            cv[kind] = L[((i64)(cu[0] + (kind & 1)) * S1 + (cu[1] + ((kind >> 1) & 1))) * S1 + (cu[2] + ((kind >> 2) & 1))];
+        return root;
+    }
+    const i64 be = e - vc.cells_small;
+    const i64 li = be / BR_CELLS;
+    const int loc = (int)(be % BR_CELLS);
+    const int l3[3] = {loc / (BR * BR), (loc / BR) % BR, loc % BR};
+    const int4 ld = vc.live[li];
+    cu[0] = ld.y * BR + l3[0];
+    cu[1] = ld.z * BR + l3[1];
+    cu[2] = ld.w * BR + l3[2];
+    const float* L = vc.lat_brick + li * BR_CORNERS;
+    for (int kind = 0; kind < 8; ++kind)
+        cv[kind] = L[((l3[0] + (kind & 1)) * BR1 + (l3[1] + ((kind >> 1) & 1))) * BR1 + (l3[2] + ((kind >> 2) & 1))];
+    return ld.x;
+}
+
+__global__ void k_virtual_cells(VArgs v, VirtCells vc, i64 total, unsigned char* __restrict__ cat,
+                                int* __restrict__ ntri) {
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+        int cu[3];
+        float cv[8];
+        virt_cell(vc, v, e, cu, cv);
         int cc = 0;
-        for (int kind = 0; kind < 8; ++kind) {
-            const i64 idx = ((i64)(u + (kind & 1)) * S1 + (w + ((kind >> 1) & 1))) * S1 + (z + ((kind >> 2) & 1));
-            if (L[idx] < 0.f) cc |= 1 << c_vid[kind];
-        }
+        for (int kind = 0; kind < 8; ++kind)
+            if (cv[kind] < 0.f) cc |= 1 << c_vid[kind];
         cat[e] = (unsigned char)cc;
         ntri[e] = c_tri_count[cc];
     }
@@ -910,29 +1034,18 @@ __global__ void k_emit_real(NodeArrays nd, EmitArgs em, i64 lo, const int* __res
     }
 }
 
-__global__ void k_emit_virtual(VArgs v, EmitArgs em, const i64* __restrict__ cell_prefix,
-                               const i64* __restrict__ lat_prefix, const i64* __restrict__ active, i64 nactive,
-                               const unsigned char* __restrict__ cat, const i64* __restrict__ tri_base,
-                               const float* __restrict__ lat) {
+__global__ void k_emit_virtual(VArgs v, EmitArgs em, VirtCells vc, const i64* __restrict__ active, i64 nactive,
+                               const unsigned char* __restrict__ cat, const i64* __restrict__ tri_base) {
     const int D = em.D;
     for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < nactive; t += (i64)gridDim.x * blockDim.x) {
         const i64 e = active[t];
-        int lo = 0, hi = v.nroots - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (cell_prefix[mid] <= e) lo = mid; else hi = mid - 1;
-        }
-        const VRoot R = v.roots[lo];
-        const int S = 1 << (D - R.depth), S1 = S + 1;
-        const i64 loc = e - cell_prefix[lo];
-        const int u = (int)(loc / ((i64)S * S)), w = (int)((loc / S) % S), z = (int)(loc % S);
+        int cu[3];
+        float cv[8];
+        const VRoot R = v.roots[virt_cell(vc, v, e, cu, cv)];
+        const int S = 1 << (D - R.depth);
         int Lc[3];
         key_coords(v.e.nd.key[R.node], R.depth, D, Lc);
-        const int c[3] = {Lc[0] * S + u, Lc[1] * S + w, Lc[2] * S + z};
-        const float* L = lat + lat_prefix[lo];
-        float cv[8];
-        for (int kind = 0; kind < 8; ++kind)
-            cv[kind] = L[((i64)(u + (kind & 1)) * S1 + (w + ((kind >> 1) & 1))) * S1 + (z + ((kind >> 2) & 1))];
+        const int c[3] = {Lc[0] * S + cu[0], Lc[1] * S + cu[1], Lc[2] * S + cu[2]};
         const int cc = cat[e];
         const int nt = c_tri_count[cc];
         const i64 tb = em.tri_offset + tri_base[t];
@@ -968,17 +1081,18 @@ __global__ void k_emit_virtual(VArgs v, EmitArgs em, const i64* __restrict__ cel
 
 // after sorting: vertex id per sorted element, positions of the first element
 __global__ void k_vertex_ids(const u64* __restrict__ keys, const uint32_t* __restrict__ slot, i64 n,
-                             const int* __restrict__ pos_scan, const float* __restrict__ epos,
-                             int32_t* __restrict__ tri_vid, float* __restrict__ vpos) {
+                             const int* __restrict__ pos_scan, const float* __restrict__ epos, float scale,
+                             float3 center, int32_t* __restrict__ tri_vid, float* __restrict__ vpos) {
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
         const bool head = (k == 0) || keys[k] != keys[k - 1];
         const int vid = pos_scan[k] + (head ? 1 : 0) - 1;
         tri_vid[slot[k]] = vid;
         if (head) {
+            // input coordinates: p*scale + centre (PlyWriteTriangles plyfile.cu:2801-2812), unfused
             const uint32_t sl = slot[k];
-            vpos[3 * (i64)vid] = epos[3 * (i64)sl];
-            vpos[3 * (i64)vid + 1] = epos[3 * (i64)sl + 1];
-            vpos[3 * (i64)vid + 2] = epos[3 * (i64)sl + 2];
+            vpos[3 * (i64)vid] = __fadd_rn(__fmul_rn(epos[3 * (i64)sl], scale), center.x);
+            vpos[3 * (i64)vid + 1] = __fadd_rn(__fmul_rn(epos[3 * (i64)sl + 1], scale), center.y);
+            vpos[3 * (i64)vid + 2] = __fadd_rn(__fmul_rn(epos[3 * (i64)sl + 2], scale), center.z);
         }
     }
 }
@@ -1105,134 +1219,162 @@ void stage_mesh(Ctx& c) {
     const i64 ntri_real = read_scalar(tri_real + nact_real, s);
     dfree(flags, s);
     dfree(fpos, s);
-    // ---- virtual cells
-    i64 ntri_virt = 0, nact_virt = 0, total_cells = 0, total_lat = 0;
+    // ---- virtual cells: small leaves (lattice edge <= 8) one thread per corner,
+    // large leaves in bricks of 8^3 cells, bounded and culled before evaluation
+    i64 ntri_virt = 0, nact_virt = 0, total_cells = 0;
     c.total_bricks = 0;
     c.live_bricks = 0;
     VRoot* droots = nullptr;
-    i64 *cell_prefix = nullptr, *lat_prefix = nullptr, *act_virt = nullptr, *tri_virt = nullptr;
-    float* lat = nullptr;
+    i64 *act_virt = nullptr, *tri_virt = nullptr;
     unsigned char* vcat = nullptr;
-    unsigned char* culled = nullptr;
     int* vntri = nullptr;
     int* bflag = nullptr;
+    int* d_small = nullptr;
+    i64 *d_small_cells = nullptr, *d_small_lat = nullptr;
+    float *lat_small = nullptr, *lat_brick = nullptr;
+    int4* live = nullptr;
     VArgs va;
     va.e = ea;
     va.iso = c.iso;
     va.nroots = (int)roots.size();
+    VirtCells vc{};
     if (!roots.empty()) {
-        std::vector<i64> hcp(roots.size()), hlp(roots.size());
-        i64 brick_run = 0;
-        for (size_t k = 0; k < roots.size(); ++k) {
-            const i64 S = 1ll << (D - roots[k].depth);
-            hcp[k] = total_cells;
-            hlp[k] = total_lat;
-            roots[k].cell_base = total_cells;
-            roots[k].lattice_base = total_lat;
-            roots[k].brick_base = (S > BR) ? brick_run : -1;
-            if (S > BR) brick_run += (S / BR) * (S / BR) * (S / BR);
-            total_cells += S * S * S;
-            total_lat += (S + 1) * (S + 1) * (S + 1);
-        }
         bflag_host.assign(M, 0);
         for (auto& R : roots) if (R.depth >= 3) bflag_host[R.node] = R.batch;
         droots = dalloc<VRoot>((i64)roots.size(), s);
-        cell_prefix = dalloc<i64>((i64)roots.size(), s);
-        lat_prefix = dalloc<i64>((i64)roots.size(), s);
         bflag = dalloc<int>(M, s);
         CK(cudaMemcpyAsync(droots, roots.data(), roots.size() * sizeof(VRoot), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(cell_prefix, hcp.data(), hcp.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(lat_prefix, hlp.data(), hlp.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(bflag, bflag_host.data(), M * sizeof(int), cudaMemcpyHostToDevice, s));
         va.roots = droots;
         va.batch_root_flag = bflag;
-        lat = dalloc<float>(total_lat, s);
-        // small leaves (lattice edge <= 8): one thread per corner; large ones: 8^3-cell bricks
         std::vector<int> small_list, big_list;
-        std::vector<i64> small_prefix, brick_prefix;
-        i64 small_total = 0, nbricks = 0;
+        std::vector<i64> small_lat, small_cells, brick_prefix, row_prefix;
+        std::vector<int4> rowdesc;
+        i64 lat_total = 0, cells_small = 0, nbricks = 0;
         for (size_t k = 0; k < roots.size(); ++k) {
             const int S = 1 << (D - roots[k].depth);
             if (S <= BR) {
                 small_list.push_back((int)k);
-                small_prefix.push_back(small_total);
-                small_total += (i64)(S + 1) * (S + 1) * (S + 1);
+                small_lat.push_back(lat_total);
+                small_cells.push_back(cells_small);
+                lat_total += (i64)(S + 1) * (S + 1) * (S + 1);
+                cells_small += (i64)S * S * S;
             } else {
+                const int nb = S / BR;
                 big_list.push_back((int)k);
                 brick_prefix.push_back(nbricks);
-                nbricks += (i64)(S / BR) * (S / BR) * (S / BR);
+                row_prefix.push_back((i64)rowdesc.size());
+                nbricks += (i64)nb * nb * nb;
+                for (int ax = 0; ax < 3; ++ax)
+                    for (int b = 0; b < nb; ++b) rowdesc.push_back(make_int4((int)k, ax, b, 0));
             }
         }
-        if (small_total > 0) {
-            const int kvs = c.kbegin("virtual_small", (double)small_total * 4);
-            int* dlist = dalloc<int>((i64)small_list.size(), s);
-            i64* dpre = dalloc<i64>((i64)small_prefix.size(), s);
-            CK(cudaMemcpyAsync(dlist, small_list.data(), small_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(dpre, small_prefix.data(), small_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
-            k_virtual_corners<<<grid_for(small_total, 128, 1ll << 30), 128, 0, s>>>(
-                va, dlist, dpre, (int)small_list.size(), small_total, lat_prefix, lat);
+        vc.nsmall = (int)small_list.size();
+        vc.cells_small = cells_small;
+        if (!small_list.empty()) {
+            d_small = dalloc<int>((i64)small_list.size(), s);
+            d_small_cells = dalloc<i64>((i64)small_list.size(), s);
+            d_small_lat = dalloc<i64>((i64)small_list.size(), s);
+            lat_small = dalloc<float>(lat_total, s);
+            CK(cudaMemcpyAsync(d_small, small_list.data(), small_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_small_cells, small_cells.data(), small_cells.size() * sizeof(i64),
+                               cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_small_lat, small_lat.data(), small_lat.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+            const int kvs = c.kbegin("virtual_small", (double)lat_total * 4);
+            k_virtual_corners<<<grid_for(lat_total, 128, 1ll << 30), 128, 0, s>>>(
+                va, d_small, d_small_lat, (int)small_list.size(), lat_total, lat_small);
             CK_LAUNCH();
             c.kend(kvs);
-            dfree(dlist, s);
-            dfree(dpre, s);
         }
-        culled = dalloc<unsigned char>(std::max<i64>(nbricks, 1), s);
+        vc.small = d_small;
+        vc.small_cells = d_small_cells;
+        vc.small_lat = d_small_lat;
+        vc.lat_small = lat_small;
+        i64 nlive = 0;
         if (nbricks > 0) {
+            const i64 nrows = (i64)rowdesc.size();
             int* dbig = dalloc<int>((i64)big_list.size(), s);
             i64* dbpre = dalloc<i64>((i64)brick_prefix.size(), s);
+            i64* drpre = dalloc<i64>((i64)row_prefix.size(), s);
+            int4* drd = dalloc<int4>(nrows, s);
+            float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
+            float* xl = dalloc<float>((i64)big_list.size() * BR_LEVELS * 27, s);
             CK(cudaMemcpyAsync(dbig, big_list.data(), big_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
             CK(cudaMemcpyAsync(dbpre, brick_prefix.data(), brick_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
-            BrickIndex bix{dbig, dbpre, (int)big_list.size()};
-            // work counter, live-brick count, layout error flag
-            unsigned long long* wk = dalloc<unsigned long long>(3, s);
-            CK(cudaMemsetAsync(wk, 0, 3 * sizeof(unsigned long long), s));
-            int per_sm = 0;
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bricks, BR_BLOCK, 0));
-            const i64 grid = std::min<i64>(nbricks, (i64)c.sms * std::max(per_sm, 1));
-            // compulsory: the brick's lattice corners written once
-            const int kb = c.kbegin("bricks", (double)nbricks * BR1 * BR1 * BR1 * 4);
-            k_bricks<<<(unsigned)grid, BR_BLOCK, 0, s>>>(va, bix, nbricks, wk, wk + 1, culled, lat_prefix, lat,
-                                                          (int*)(wk + 2));
+            CK(cudaMemcpyAsync(drpre, row_prefix.data(), row_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(drd, rowdesc.data(), nrows * sizeof(int4), cudaMemcpyHostToDevice, s));
+            BrickIndex bix{dbig, dbpre, drpre, (int)big_list.size(), rows, xl};
+            const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
+            k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drd, nrows, rows);
+            CK_LAUNCH();
+            k_brick_xl<<<grid_for((i64)big_list.size() * BR_LEVELS * 27, 256), 256, 0, s>>>(
+                va, dbig, (int)big_list.size(), xl);
+            CK_LAUNCH();
+            c.kend(kr);
+            unsigned char* culled = dalloc<unsigned char>(nbricks, s);
+            // compulsory: each brick's three rows and its culled flag
+            const int kb = c.kbegin("brick_bound", (double)nbricks * (3.0 * 33 * (D + 1) * 4 + 1));
+            k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks,
+                                                                                                culled);
             CK_LAUNCH();
             c.kend(kb);
-            unsigned long long hw[3];
-            CK(cudaMemcpyAsync(hw, wk, sizeof hw, cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            dfree(wk, s);
-            c.live_bricks = (i64)hw[1];
-            if (hw[2]) {
-                set_last_error("brick window layout overflow");
-                throw Error{PRGPU_ERR_LIMIT, {0}};
-            }
+            int* bf = dalloc<int>(nbricks, s);
+            int* bp = dalloc<int>(nbricks + 1, s);
+            k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
+            CK_LAUNCH();
+            exclusive_scan<int, int>(bf, bp, nbricks, bp + nbricks, s);
+            nlive = read_scalar(bp + nbricks, s);
             c.total_bricks = nbricks;
+            c.live_bricks = nlive;
+            if (nlive > 0) {
+                live = dalloc<int4>(nlive, s);
+                k_live_bricks<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, culled, bp, nbricks, live);
+                CK_LAUNCH();
+                lat_brick = dalloc<float>(nlive * BR_CORNERS, s);
+                const int ke = c.kbegin("brick_eval", (double)nlive * BR_CORNERS * 4);
+                k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_brick);
+                CK_LAUNCH();
+                c.kend(ke);
+            }
+            dfree(bf, s);
+            dfree(bp, s);
+            dfree(culled, s);
             dfree(dbig, s);
             dfree(dbpre, s);
+            dfree(drpre, s);
+            dfree(drd, s);
+            dfree(rows, s);
+            dfree(xl, s);
         }
-        vcat = dalloc<unsigned char>(total_cells, s);
-        vntri = dalloc<int>(total_cells, s);
-        const int kc2 = c.kbegin("virtual_cells", (double)total_lat * 4 + (double)total_cells * 5);
-        k_virtual_cells<<<grid_for(total_cells, 256, 1ll << 30), 256, 0, s>>>(va, cell_prefix, lat_prefix, total_cells,
-                                                                              lat, culled, vcat, vntri);
-        CK_LAUNCH();
-        c.kend(kc2);
-        int* vf = dalloc<int>(total_cells, s);
-        int* vp = dalloc<int>(total_cells + 1, s);
-        k_active_flags<<<grid_for(total_cells, 256), 256, 0, s>>>(vntri, total_cells, vf);
-        CK_LAUNCH();
-        exclusive_scan<int, int>(vf, vp, total_cells, vp + total_cells, s);
-        nact_virt = read_scalar(vp + total_cells, s);
-        act_virt = dalloc<i64>(std::max<i64>(nact_virt, 1), s);
-        k_compact_idx<i64><<<grid_for(total_cells, 256), 256, 0, s>>>(vf, vp, total_cells, act_virt);
-        CK_LAUNCH();
-        dfree(vf, s);
-        dfree(vp, s);
-        tri_virt = dalloc<i64>(nact_virt + 1, s);
-        i64* tmp = dalloc<i64>(std::max<i64>(nact_virt, 1), s);
-        k_gather_ntri<<<grid_for(nact_virt, 256), 256, 0, s>>>(vntri, act_virt, nact_virt, tmp);
-        CK_LAUNCH();
-        exclusive_scan<i64, i64>(tmp, tri_virt, nact_virt, tri_virt + nact_virt, s);
-        dfree(tmp, s);
-        ntri_virt = read_scalar(tri_virt + nact_virt, s);
+        vc.live = live;
+        vc.lat_brick = lat_brick;
+        total_cells = cells_small + nlive * BR_CELLS;
+        if (total_cells > 0) {
+            vcat = dalloc<unsigned char>(total_cells, s);
+            vntri = dalloc<int>(total_cells, s);
+            const int kc2 = c.kbegin("virtual_cells", (double)(lat_total + nlive * BR_CORNERS) * 4 + (double)total_cells * 5);
+            k_virtual_cells<<<grid_for(total_cells, 256, 1ll << 30), 256, 0, s>>>(va, vc, total_cells, vcat, vntri);
+            CK_LAUNCH();
+            c.kend(kc2);
+            int* vf = dalloc<int>(total_cells, s);
+            int* vp = dalloc<int>(total_cells + 1, s);
+            k_active_flags<<<grid_for(total_cells, 256), 256, 0, s>>>(vntri, total_cells, vf);
+            CK_LAUNCH();
+            exclusive_scan<int, int>(vf, vp, total_cells, vp + total_cells, s);
+            nact_virt = read_scalar(vp + total_cells, s);
+            act_virt = dalloc<i64>(std::max<i64>(nact_virt, 1), s);
+            k_compact_idx<i64><<<grid_for(total_cells, 256), 256, 0, s>>>(vf, vp, total_cells, act_virt);
+            CK_LAUNCH();
+            dfree(vf, s);
+            dfree(vp, s);
+            tri_virt = dalloc<i64>(nact_virt + 1, s);
+            i64* tmp = dalloc<i64>(std::max<i64>(nact_virt, 1), s);
+            k_gather_ntri<<<grid_for(nact_virt, 256), 256, 0, s>>>(vntri, act_virt, nact_virt, tmp);
+            CK_LAUNCH();
+            exclusive_scan<i64, i64>(tmp, tri_virt, nact_virt, tri_virt + nact_virt, s);
+            dfree(tmp, s);
+            ntri_virt = read_scalar(tri_virt + nact_virt, s);
+        }
     }
     c.virtual_cells = total_cells;
     // ---- emission, sort, vertex ids
@@ -1269,8 +1411,8 @@ void stage_mesh(Ctx& c) {
         if (nact_virt > 0) {
             EmitArgs ev = em;
             ev.tri_offset = ntri_real;
-            k_emit_virtual<<<grid_for(nact_virt, 128, 1ll << 30), 128, 0, s>>>(va, ev, cell_prefix, lat_prefix, act_virt,
-                                                                               nact_virt, vcat, tri_virt, lat);
+            k_emit_virtual<<<grid_for(nact_virt, 128, 1ll << 30), 128, 0, s>>>(va, ev, vc, act_virt, nact_virt, vcat,
+                                                                               tri_virt);
             CK_LAUNCH();
         }
         u64* ktmp = dalloc<u64>(nem, s);
@@ -1288,7 +1430,9 @@ void stage_mesh(Ctx& c) {
         const i64 nvert = read_scalar(hp + nem, s);
         int32_t* tri_vid = dalloc<int32_t>(nem, s);
         float* vpos = dalloc<float>(3 * std::max<i64>(nvert, 1), s);
-        k_vertex_ids<<<grid_for(nem, 256), 256, 0, s>>>(em.keys, em.slot, nem, hp, em.pos, tri_vid, vpos);
+        k_vertex_ids<<<grid_for(nem, 256), 256, 0, s>>>(em.keys, em.slot, nem, hp, em.pos, c.scale,
+                                                        make_float3(c.center[0], c.center[1], c.center[2]),
+                                                        tri_vid, vpos);
         CK_LAUNCH();
         c.mesh_v.resize(3 * nvert);
         c.mesh_f.resize(nem);
@@ -1300,18 +1444,13 @@ void stage_mesh(Ctx& c) {
     }
     dfree(act_real, s);
     dfree(tri_real, s);
-    dfree(droots, s); dfree(cell_prefix, s); dfree(lat_prefix, s); dfree(act_virt, s); dfree(tri_virt, s);
-    dfree(lat, s); dfree(vcat, s); dfree(vntri, s); dfree(bflag, s); dfree(culled, s);
+    dfree(droots, s); dfree(act_virt, s); dfree(tri_virt, s);
+    dfree(vcat, s); dfree(vntri, s); dfree(bflag, s);
+    dfree(d_small, s); dfree(d_small_cells, s); dfree(d_small_lat, s);
+    dfree(lat_small, s); dfree(lat_brick, s); dfree(live, s);
     dfree(cell_v, s);
     dfree(cat, s);
     dfree(ntri, s);
-    // input coordinates: p*scale + centre (PlyWriteTriangles plyfile.cu:2801-2812), unfused
-    const i64 nv = (i64)c.mesh_v.size() / 3;
-    for (i64 k = 0; k < nv; ++k)
-        for (int a = 0; a < 3; ++a) {
-            volatile float prod = c.mesh_v[3 * k + a] * c.scale;
-            c.mesh_v[3 * k + a] = prod + c.center[a];
-        }
 }
 
 }  // namespace prgpu
