@@ -447,8 +447,9 @@ __global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i
 // and the brick's index along it (a "brick row"), so it is tabulated once per
 // row by k_brick_rows:
 //   BT[d][t][k]   basis value at corner k of the function of cell V_k + t - 1
-//                 (depth d > r, V_k the owner cell of corner k) or of ancestor
-//                 cell + t - 1 (depth d <= r)
+//                 (depth d > r, V_k the owner cell of corner k, t = 0..3; t = 3
+//                 serves corners on the leaf's lower faces, whose owner cell is
+//                 V_k + 1) or of ancestor cell + t - 1 (depth d <= r)
 //   RA[l][t]      range over k of BT[l][t][k], l <= r
 //   RW[d][n]      range (with 0) of the depth-d function of window cell n over
 //                 the corners whose owner cell is within one cell of it
@@ -463,14 +464,14 @@ constexpr int BR_WEXT = BR + 3;    // window edge at the finest depth
 // multiple of 8: 11^3 + 7^3 + 5^3 + 12 * 4^3 = 2567
 constexpr int BR_XW = 2600;
 // brick-row table: BT (27 per depth), RA (6 per depth), RW (22 per depth)
-constexpr int ROW_BT = 0, ROW_RA = 27, ROW_RW = 33, ROW_PER_DEPTH = 55;
+constexpr int ROW_BT = 0, ROW_RA = 36, ROW_RW = 42, ROW_PER_DEPTH = 64;
 
 struct BrickIndex {                // bricks of the large roots, numbered root by root
     const int* big;                // root indices of the large roots
     const i64* prefix;             // first brick of each large root
     const i64* row_prefix;         // first brick row of each large root (3 * bricks per edge rows each)
     int nbig;
-    const float* rows;             // brick-row tables, 55 (D+1) floats each
+    const float* rows;             // brick-row tables, 64 (D+1) floats each
     const float* xl;               // per large root: x of the 27 neighbours of each ancestor, 16 x 27
 };
 struct VBrick {
@@ -513,16 +514,32 @@ __device__ i64 shell_node(const VArgs& v, int L, int r, const int Lc[3], int d, 
     return descend(nd, an, r, d, N);
 }
 
-// interval of x * X * Y * Z (X, Y, Z intervals), in double
-__device__ __forceinline__ void term_interval(double x, const float* lo, const float* hi, double& tlo, double& thi) {
-    double a = x, b = x;
+// interval of x * X * Y * Z (X, Y, Z intervals), in float: each end is within
+// 3u of the exact product's end
+__device__ __forceinline__ void term_interval(float x, const float* lo, const float* hi, float& tlo, float& thi) {
+    float a = x, b = x;
     for (int ax = 0; ax < 3; ++ax) {
-        const double c0 = a * lo[ax], c1 = a * hi[ax], c2 = b * lo[ax], c3 = b * hi[ax];
-        a = fmin(fmin(c0, c1), fmin(c2, c3));
-        b = fmax(fmax(c0, c1), fmax(c2, c3));
+        const float c0 = a * lo[ax], c1 = a * hi[ax], c2 = b * lo[ax], c3 = b * hi[ax];
+        a = fminf(fminf(c0, c1), fminf(c2, c3));
+        b = fmaxf(fmaxf(c0, c1), fmaxf(c2, c3));
     }
     tlo = a;
     thi = b;
+}
+
+// can a lower-face corner of brick b[] be owned by a cell of another leaf of
+// the batch?  Only if a lower neighbour across a face the brick touches is a
+// root of the same batch (batch_member's rule)
+__device__ __forceinline__ bool brick_foreign_possible(const VArgs& v, const VRoot& R, const int b[3]) {
+    if (R.depth < 3 || (b[0] && b[1] && b[2])) return false;
+    const NodeArrays& nd = v.e.nd;
+    for (int m = 1; m < 8; ++m) {
+        const int dx = (m & 1) ? -1 : 0, dy = (m & 2) ? -1 : 0, dz = (m & 4) ? -1 : 0;
+        if ((dx && b[0]) || (dy && b[1]) || (dz && b[2])) continue;
+        const int nb = nd.neigh[(i64)(9 * (dx + 1) + 3 * (dy + 1) + (dz + 1)) * nd.M + R.node];
+        if (nb != -1 && v.batch_root_flag[nb] == R.batch) return true;
+    }
+    return false;
 }
 
 // window of depth d around a brick along one axis: origin and extent of the
@@ -552,14 +569,14 @@ __global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrow
         const int g0 = Lc[ax] * S + rd.z * BR;
         const int c0 = rd.z * BR;
         float* out = rows + row * (i64)(ROW_PER_DEPTH * (D + 1));
-        float bt[3][BR1];
-        for (int t = 0; t < 3; ++t)
+        float bt[4][BR1];
+        for (int t = 0; t < 4; ++t)
             for (int k = 0; k <= BR; ++k) {
                 const int cidx = (d <= r) ? (Lc[ax] >> (r - d)) + t - 1 : ((g0 + k - 1) >> (D - d)) + t - 1;
                 float val = 0.f;
                 if (cidx >= 0 && cidx < (1 << d)) val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(g0 + k) * inv);
                 bt[t][k] = val;
-                out[ROW_BT * (D + 1) + (d * 3 + t) * BR1 + k] = val;
+                out[ROW_BT * (D + 1) + (d * 4 + t) * BR1 + k] = val;
             }
         if (d <= r) {
             for (int t = 0; t < 3; ++t) {
@@ -638,6 +655,10 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
     for (i64 bi = warp; bi < nbricks; bi += nwarps) {
         const VBrick B = brick_of(v, bix, bi);
         const VRoot R = v.roots[B.root];
+        if (brick_foreign_possible(v, R, B.b)) {   // never culled
+            if (lane == 0) culled[bi] = 0;
+            continue;
+        }
         const int r = R.depth, S = 1 << (D - r), L = R.node, nb = S / BR;
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
@@ -645,7 +666,8 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
         const float* row[3];
         for (int ax = 0; ax < 3; ++ax) row[ax] = brick_row(bix, D, B.big, nb, ax, B.b[ax]);
         const float* xl = bix.xl + (i64)B.big * BR_LEVELS * 27;
-        double lo = 0, hi = 0, amax = 0, cnt = 0;
+        float lo = 0.f, hi = 0.f, amax = 0.f;
+        int cnt = 0;
         // the leaf and its ancestors
         for (int t = lane; t < 27 * (r + 1); t += 32) {
             const int l = r - t / 27, j = t % 27;
@@ -657,11 +679,11 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
                 blo[ax] = row[ax][ROW_RA * (D + 1) + (l * 3 + tt[ax]) * 2];
                 bhi[ax] = row[ax][ROW_RA * (D + 1) + (l * 3 + tt[ax]) * 2 + 1];
             }
-            double tl, th;
-            term_interval((double)x, blo, bhi, tl, th);
+            float tl, th;
+            term_interval(x, blo, bhi, tl, th);
             lo += tl; hi += th;
-            amax += fmax(fabs(tl), fabs(th));
-            cnt += 1;
+            amax += fmaxf(fabsf(tl), fabsf(th));
+            ++cnt;
         }
         // real nodes around the leaf, at the virtual depths
         for (int d = r + 1; d <= D; ++d) {
@@ -684,23 +706,11 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
                     blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n[ax]) * 2];
                     bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n[ax]) * 2 + 1];
                 }
-                double tl, th;
-                term_interval((double)a.x[node], blo, bhi, tl, th);
+                float tl, th;
+                term_interval(a.x[node], blo, bhi, tl, th);
                 lo += tl; hi += th;
-                amax += fmax(fabs(tl), fabs(th));
-                cnt += 1;
-            }
-        }
-        // lower-face corners owned by another leaf of the batch
-        int foreign = 0;
-        if (r >= 3 && (B.b[0] == 0 || B.b[1] == 0 || B.b[2] == 0)) {
-            for (int e = lane; e < BR_CORNERS; e += 32) {
-                const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
-                const int uu = B.b[0] * BR + kk[0], ww = B.b[1] * BR + kk[1], zz = B.b[2] * BR + kk[2];
-                if (uu && ww && zz) continue;
-                const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
-                int oc[3];
-                if (lower_face_owner(v, R, Lc, qc, oc) != L) foreign = 1;
+                amax += fmaxf(fabsf(tl), fabsf(th));
+                ++cnt;
             }
         }
         for (int o = 16; o; o >>= 1) {
@@ -708,77 +718,70 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             hi += __shfl_xor_sync(0xffffffffu, hi, o);
             amax += __shfl_xor_sync(0xffffffffu, amax, o);
             cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-            foreign |= __shfl_xor_sync(0xffffffffu, foreign, o);
         }
         if (lane == 0) {
-            const double iso = (double)v.iso;
-            const double margin = (cnt + 4.0) * u * amax + 2.0 * u * (fabs(lo) + fabs(hi) + 2.0 * fabs(iso)) +
-                                  1e-12 * (amax + fabs(iso));
-            const bool above = lo - margin > iso, below = hi + margin < iso;
-            culled[bi] = (!foreign && (above || below)) ? 1 : 0;
+            // rounding of the evaluation's FMA chain, (cnt + 4) u sum|term|, plus that of
+            // this bound's own float products and sums, (cnt + 3) u sum|term|
+            const double iso = (double)v.iso, A = (double)amax * 1.01;
+            const double margin = (2.0 * cnt + 8.0) * u * A + 4.0 * u * (fabs((double)lo) + fabs((double)hi) + 2.0 * fabs(iso)) +
+                                  1e-30;
+            const bool above = (double)lo - margin > iso, below = (double)hi + margin < iso;
+            culled[bi] = (above || below) ? 1 : 0;
         }
     }
 }
 
 struct BrickShared {
     float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
-    float Bt[3 * BR_LEVELS * 27];             // [axis][depth][t][k], from the brick-row tables
-    float Xw[BR_XW];                          // window coefficients, virtual depths
+    float Bt[3 * BR_LEVELS * 36];             // [axis][depth][t][k], from the brick-row tables
+    float Xw[BR_XW];                          // window coefficients, virtual depths (0: none or inside the leaf)
     int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
     int wext[BR_LEVELS][3];
     int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
+    int nforeign;
+    short foreign[3 * BR1 * BR1];             // lower-face corners owned by another leaf
 };
 __device__ __forceinline__ float bt_at(const BrickShared& sm, int ax, int d, int t, int k) {
-    return sm.Bt[(ax * BR_LEVELS + d) * 27 + t * BR1 + k];
+    return sm.Bt[(ax * BR_LEVELS + d) * 36 + t * BR1 + k];
 }
 
-// value of a corner owned by the brick's leaf through owner cell oc[], from the
-// shared window; 'interior' means oc = qc - 1 so the tabulated basis values apply
-__device__ __forceinline__ float brick_corner(const BrickShared& sm, const EvalArgs& a, int r, const int Lc[3],
-                                              const int oc[3], const int qc[3], const int kk[3], bool interior) {
-    const int D = a.D;
-    const float inv = 1.0f / (float)(1 << D);
+// value of corner kk owned by the brick's leaf, from the shared window, in the
+// order of virtual_corner_value.  sft[ax] is 1 on the axes where the owner cell
+// is the corner's own cell (lower faces), 0 where it is the cell below.  Terms
+// that virtual_corner_value skips (levels whose 3x3x3 block lies inside the
+// leaf, cells inside the leaf, absent nodes) read 0 here, and adding a zero
+// product leaves the sum unchanged, so the value is the same.
+__device__ __forceinline__ float brick_corner(const BrickShared& sm, int D, int r, const int oc[3], const int kk[3],
+                                              const int sft[3]) {
     float val = 0.f;
     for (int d = D; d > r; --d) {
         const int off = sm.woff[d];
         if (off < 0) continue;
-        const int sh = D - d, span = 1 << (d - r);
-        const int V[3] = {oc[0] >> sh, oc[1] >> sh, oc[2] >> sh};
-        bool inner = true;
-        for (int ax = 0; ax < 3; ++ax) {
-            const int lo = Lc[ax] * span;
-            if (V[ax] - 1 < lo || V[ax] + 1 >= lo + span) inner = false;
-        }
-        if (inner) continue;
+        const int sh = D - d;
         float bv[3][3];
-        if (interior) {
-            for (int ax = 0; ax < 3; ++ax)
-                for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, d, t, kk[ax]);
-        } else {
-            const int fb = (1 << d) - 1, lim = 1 << d;
-            for (int ax = 0; ax < 3; ++ax)
-                for (int t = 0; t < 3; ++t) {
-                    const int cc = V[ax] + t - 1;
-                    bv[ax][t] = (cc >= 0 && cc < lim) ? cpoly_value<3>(a.basis[fb + cc], (float)qc[ax] * inv) : 0.f;
-                }
-        }
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, d, t + sft[ax], kk[ax]);
         const int e1 = sm.wext[d][1], e2 = sm.wext[d][2];
-        const int b0 = V[0] - 1 - sm.wlo[d][0], b1 = V[1] - 1 - sm.wlo[d][1], b2 = V[2] - 1 - sm.wlo[d][2];
-        const int s2 = d - r;
+        const float* xw = sm.Xw + off + (((oc[0] >> sh) - 1 - sm.wlo[d][0]) * e1 + ((oc[1] >> sh) - 1 - sm.wlo[d][1])) * e2 +
+                          ((oc[2] >> sh) - 1 - sm.wlo[d][2]);
+#pragma unroll
         for (int j = 0; j < 27; ++j) {
             const int jx = j / 9, jy = (j / 3) % 3, jz = j % 3;
-            if (((V[0] + jx - 1) >> s2) == Lc[0] && ((V[1] + jy - 1) >> s2) == Lc[1] && ((V[2] + jz - 1) >> s2) == Lc[2])
-                continue;                                     // inside the subdivided leaf: no coefficient
-            const float xn = sm.Xw[off + ((b0 + jx) * e1 + (b1 + jy)) * e2 + (b2 + jz)];
-            val = fmaf(xn * bv[0][jx] * bv[1][jy], bv[2][jz], val);
+            val = fmaf(xw[(jx * e1 + jy) * e2 + jz] * bv[0][jx] * bv[1][jy], bv[2][jz], val);
         }
     }
     // the leaf itself and its real ancestors (walk_up with absent neighbours as 0)
     for (int l = r; l >= 0; --l) {
         const float* xs = sm.xL + 27 * l;
-        for (int j = 0; j < 27; ++j)
-            val = fmaf(xs[j] * bt_at(sm, 0, l, j / 9, kk[0]) * bt_at(sm, 1, l, (j / 3) % 3, kk[1]),
-                       bt_at(sm, 2, l, j % 3, kk[2]), val);
+        float bv[3][3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, l, t, kk[ax]);
+#pragma unroll
+        for (int j = 0; j < 27; ++j) val = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
     }
     return val;
 }
@@ -801,6 +804,7 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
         const int g0[3] = {Lc[0] * S + bb[0] * BR, Lc[1] * S + bb[1] * BR, Lc[2] * S + bb[2] * BR};
+        const bool fposs = brick_foreign_possible(v, R, bb);
         // the large-root index of this root (for the tables)
         int big = 0;
         {
@@ -828,12 +832,13 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
                     sm.woff[d] = -1;
                 }
             }
+            sm.nforeign = 0;
         }
         for (int e = threadIdx.x; e < 27 * (r + 1); e += blockDim.x)
             sm.xL[e] = bix.xl[(i64)big * BR_LEVELS * 27 + e];
-        for (int e = threadIdx.x; e < 3 * 27 * (D + 1); e += blockDim.x) {
-            const int ax = e / (27 * (D + 1)), q = e % (27 * (D + 1));
-            sm.Bt[ax * BR_LEVELS * 27 + q] = brick_row(bix, D, big, nb, ax, bb[ax])[ROW_BT * (D + 1) + q];
+        for (int e = threadIdx.x; e < 3 * 36 * (D + 1); e += blockDim.x) {
+            const int ax = e / (36 * (D + 1)), q = e % (36 * (D + 1));
+            sm.Bt[ax * BR_LEVELS * 36 + q] = brick_row(bix, D, big, nb, ax, bb[ax])[ROW_BT * (D + 1) + q];
         }
         __syncthreads();
         for (int d = r + 1; d <= D; ++d) {
@@ -852,17 +857,25 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
             const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
             const int uu = bb[0] * BR + kk[0], ww = bb[1] * BR + kk[1], zz = bb[2] * BR + kk[2];
             const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
-            float val;
-            if (uu && ww && zz) {
-                const int oc[3] = {qc[0] - 1, qc[1] - 1, qc[2] - 1};
-                val = brick_corner(sm, a, r, Lc, oc, qc, kk, true);
-            } else {
-                int oc[3] = {0, 0, 0};
-                const int own = lower_face_owner(v, R, Lc, qc, oc);
-                val = (own == L) ? brick_corner(sm, a, r, Lc, oc, qc, kk, false)
-                                 : foreign_corner_value(v, own, r, oc, qc);
+            const int sft[3] = {uu == 0, ww == 0, zz == 0};
+            const int oc[3] = {qc[0] - 1 + sft[0], qc[1] - 1 + sft[1], qc[2] - 1 + sft[2]};
+            if (fposs && (sft[0] | sft[1] | sft[2])) {
+                int o2[3];
+                if (lower_face_owner(v, R, Lc, qc, o2) != L) {
+                    sm.foreign[atomicAdd(&sm.nforeign, 1)] = (short)e;
+                    continue;
+                }
             }
-            out[e] = val - v.iso;
+            out[e] = brick_corner(sm, D, r, oc, kk, sft) - v.iso;
+        }
+        __syncthreads();
+        for (int f = threadIdx.x; f < sm.nforeign; f += blockDim.x) {
+            const int e = sm.foreign[f];
+            const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
+            const int qc[3] = {Lc[0] * S + bb[0] * BR + kk[0], Lc[1] * S + bb[1] * BR + kk[1], Lc[2] * S + bb[2] * BR + kk[2]};
+            int oc[3] = {0, 0, 0};
+            const int own = lower_face_owner(v, R, Lc, qc, oc);
+            out[e] = foreign_corner_value(v, own, r, oc, qc) - v.iso;
         }
     }
 }
