@@ -111,40 +111,80 @@ __global__ void k_div_thread(NodeArrays nd, DivArgs a, i64 lo, i64 hi, float* __
     }
 }
 
-// nodes with many terms: one block per node, FP64 block reduction
-constexpr int DIV_BLOCK = 256;
-__global__ void k_div_block(NodeArrays nd, DivArgs a, i64 lo, float* __restrict__ out) {
-    __shared__ int pre[28];
-    __shared__ int sidx[27];
-    __shared__ double red[DIV_BLOCK / 32];
-    const i64 i = lo + blockIdx.x;
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int j = 0; j < 27; ++j) {
-            const int nb = nd.neigh[(i64)j * a.M + i];
-            pre[j] = run;
-            sidx[j] = (nb == -1) ? 0 : nd.didx[nb];
-            run += (nb == -1) ? 0 : nd.dnum[nb];
+// nodes with many terms (depths < D-1): the node's terms, in neighbour order,
+// are cut into chunks of DIV_CHUNK; one warp sums a chunk in FP64 and the
+// chunk sums are added per node in chunk order (deterministic)
+constexpr int DIV_CHUNK = 2048;
+constexpr int DIV_WARPS = 8;
+
+__device__ __forceinline__ i64 node_terms(const NodeArrays& nd, i64 M, i64 i) {
+    i64 T = 0;
+    for (int j = 0; j < 27; ++j) {
+        const int nb = nd.neigh[(i64)j * M + i];
+        if (nb != -1) T += nd.dnum[nb];
+    }
+    return T;
+}
+
+__global__ void k_div_count(NodeArrays nd, i64 n, int* __restrict__ nchunks) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        nchunks[i] = (int)((node_terms(nd, nd.M, i) + DIV_CHUNK - 1) / DIV_CHUNK);
+}
+
+__global__ void k_div_items(const int* __restrict__ nchunks, const int* __restrict__ first, i64 n,
+                            int* __restrict__ item_node) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        for (int c = 0; c < nchunks[i]; ++c) item_node[first[i] + c] = (int)i;
+}
+
+__global__ void __launch_bounds__(DIV_WARPS * 32) k_div_chunks(NodeArrays nd, DivArgs a, const int* __restrict__ item_node,
+                                                               const int* __restrict__ first, i64 nitems,
+                                                               double* __restrict__ partial) {
+    __shared__ int pre[DIV_WARPS][28];
+    __shared__ int sidx[DIV_WARPS][27];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    for (i64 it = warp; it < nitems; it += nwarps) {
+        const i64 i = item_node[it];
+        const int chunk = (int)(it - first[i]);
+        // prefix of the neighbours' finest-descendant counts, in neighbour order
+        int cnt = 0, sx = 0;
+        if (lane < 27) {
+            const int nb = nd.neigh[(i64)lane * a.M + i];
+            if (nb != -1) { cnt = nd.dnum[nb]; sx = nd.didx[nb]; }
         }
-        pre[27] = run;
+        int inc = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        __syncwarp();
+        if (lane < 27) { pre[w][lane] = inc - cnt; sidx[w][lane] = sx; }
+        if (lane == 26) pre[w][27] = inc;
+        __syncwarp();
+        const float *r0, *r1, *r2;
+        int t0[3];
+        node_rows(a, nd.key[i], nd.depth[i], r0, r1, r2, t0);
+        const int total = pre[w][27];
+        const int lo = chunk * DIV_CHUNK, hi = min(total, lo + DIV_CHUNK);
+        double val = 0.0;
+        int j = 0;
+        for (int t = lo + lane; t < hi; t += 32) {
+            while (pre[w][j + 1] <= t) ++j;
+            val += (double)div_term(a, r0, r1, r2, t0, (i64)sidx[w][j] + (t - pre[w][j]));
+        }
+        for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+        if (lane == 0) partial[it] = val;
+        __syncwarp();
     }
-    __syncthreads();
-    const float *r0, *r1, *r2;
-    int t0[3];
-    node_rows(a, nd.key[i], nd.depth[i], r0, r1, r2, t0);
-    const int total = pre[27];
-    double val = 0.0;
-    int j = 0;
-    for (int t = threadIdx.x; t < total; t += DIV_BLOCK) {
-        while (pre[j + 1] <= t) ++j;
-        val += (double)div_term(a, r0, r1, r2, t0, (i64)sidx[j] + (t - pre[j]));
-    }
-    for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = val;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0;
-        for (int w = 0; w < DIV_BLOCK / 32; ++w) s += red[w];
+}
+
+__global__ void k_div_final(const int* __restrict__ nchunks, const int* __restrict__ first,
+                            const double* __restrict__ partial, i64 n, float* __restrict__ out) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks[i]; ++c) s += partial[first[i] + c];
         out[i] = (float)s;
     }
 }
@@ -188,9 +228,29 @@ void stage_divergence(Ctx& c) {
     k_div_thread<<<grid_for(M - c.base[split], 128, 1ll << 30), 128, 0, s>>>(c.nodes, a, c.base[split], M,
                                                                              c.divergence);
     CK_LAUNCH();
-    if (c.base[split] > 0) {
-        k_div_block<<<(unsigned)c.base[split], DIV_BLOCK, 0, s>>>(c.nodes, a, 0, c.divergence);
+    const i64 nc = c.base[split];   // nodes at depths < D-1
+    if (nc > 0) {
+        int* nch = dalloc<int>(nc, s);
+        int* first = dalloc<int>(nc + 1, s);
+        k_div_count<<<grid_for(nc, 256), 256, 0, s>>>(c.nodes, nc, nch);
         CK_LAUNCH();
+        exclusive_scan<int, int>(nch, first, nc, first + nc, s);
+        const i64 nitems = read_scalar(first + nc, s);
+        int* item_node = dalloc<int>(std::max<i64>(nitems, 1), s);
+        double* partial = dalloc<double>(std::max<i64>(nitems, 1), s);
+        k_div_items<<<grid_for(nc, 256), 256, 0, s>>>(nch, first, nc, item_node);
+        CK_LAUNCH();
+        if (nitems > 0) {
+            k_div_chunks<<<grid_for(nitems * 32, DIV_WARPS * 32, (i64)c.sms * 8), DIV_WARPS * 32, 0, s>>>(
+                c.nodes, a, item_node, first, nitems, partial);
+            CK_LAUNCH();
+        }
+        k_div_final<<<grid_for(nc, 256), 256, 0, s>>>(nch, first, partial, nc, c.divergence);
+        CK_LAUNCH();
+        dfree(nch, s);
+        dfree(first, s);
+        dfree(item_node, s);
+        dfree(partial, s);
     }
     c.kend(kt);
     dfree(fc, s);
