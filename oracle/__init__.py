@@ -27,6 +27,7 @@ _DTYPES = {
     "mesh_v": np.float32, "mesh_f": np.int32, "has_tri": np.int32, "has_int": np.int32,
     "batch_tri": np.int64, "center": np.float32, "scale": np.float32, "iso": np.float32,
     "subdivide_roots": np.int64,
+    "vcells": np.int64,
 }
 
 
@@ -52,6 +53,7 @@ def lib():
                      "orc_point_values", "orc_marching_cubes"):
             getattr(L, name).argtypes = [vp]
         L.orc_build_basis.argtypes = [vp, c_int]
+        L.orc_set_root_stride.argtypes = [vp, c_int]
         L.orc_solve.argtypes = [vp, c_int, dbl, c_int]
         L.orc_reconstruct.argtypes = [vp, c_int, dbl, c_int]
         L.orc_get.restype = vp
@@ -103,6 +105,10 @@ class Oracle:
 
     def marching_cubes(self):
         lib().orc_marching_cubes(self._h)
+
+    def set_root_stride(self, stride: int):
+        """Timing samples only: subdivide every stride-th root (0: none)."""
+        lib().orc_set_root_stride(self._h, stride)
 
     def reconstruct(self, mode: int = 0, tol: float = 1e-5, max_iter: int = 10000):
         lib().orc_reconstruct(self._h, mode, tol, max_iter)

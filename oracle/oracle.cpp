@@ -337,6 +337,10 @@ struct Ctx {
     Mesh mesh;
     std::vector<int> has_tri, has_int;      // per node at depth < D
     i64 subdivide_roots = 0;
+    // timing samples only: subdivide every root_stride-th root (0: none), and
+    // the virtual cells of all roots / of the subdivided ones
+    int root_stride = 1;
+    i64 vcells[2] = {0, 0};
     std::vector<i64> batch_tri;             // triangles per batch (0 = finest real nodes)
     std::vector<float> corner_value_D;      // per depth-D vertex (debug)
 };
@@ -843,13 +847,14 @@ static void marching_cubes(Ctx& c) {
     struct Vtx { float pos[3]; int owner, kind, depth; };
     std::vector<Vtx> V;
     {
-        std::vector<std::vector<Vtx>> local(omp_threads(c));
-        std::vector<Vtx> pre;
-        // sequential in node order keeps the copy_if ordering
-        for (i64 i = 0; i < M; ++i) {
+        // owner tests in parallel; collected in node order (the copy_if ordering)
+        std::vector<unsigned char> own_mask(M, 0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+        for (i64 i = 1; i < M; ++i) {
             int d = c.depth[i];
             float hw = 1.0f / (1 << (d + 1)), W = 1.0f / (1 << d), W2 = W * W;
             const float* nc = &cen[3 * i];
+            unsigned m = 0;
             for (int j = 0; j < 8; ++j) {
                 float vp[3] = {nc[0] + (2 * (j & 1) - 1) * hw, nc[1] + (2 * ((j & 2) >> 1) - 1) * hw,
                                nc[2] + (2 * ((j & 4) >> 2) - 1) * hw};
@@ -859,15 +864,29 @@ static void marching_cubes(Ctx& c) {
                     if (nb == -1) continue;
                     if (sqdist(vp, &cen[3 * nb]) < W2 && ownK > c.key[nb]) { ownK = c.key[nb]; own = nb; }
                 }
-                if (own == i && i > 0) {
-                    Vtx v; memcpy(v.pos, vp, sizeof vp); v.owner = (int)i; v.kind = j; v.depth = d;
-                    V.push_back(v);
-                }
+                if (own == i) m |= 1u << j;
+            }
+            own_mask[i] = (unsigned char)m;
+        }
+        for (i64 i = 1; i < M; ++i) {
+            if (!own_mask[i]) continue;
+            int d = c.depth[i];
+            float hw = 1.0f / (1 << (d + 1));
+            const float* nc = &cen[3 * i];
+            for (int j = 0; j < 8; ++j) {
+                if (!((own_mask[i] >> j) & 1)) continue;
+                Vtx v;
+                v.pos[0] = nc[0] + (2 * (j & 1) - 1) * hw;
+                v.pos[1] = nc[1] + (2 * ((j & 2) >> 1) - 1) * hw;
+                v.pos[2] = nc[2] + (2 * ((j & 4) >> 2) - 1) * hw;
+                v.owner = (int)i; v.kind = j; v.depth = d;
+                V.push_back(v);
             }
         }
     }
     const i64 NV = (i64)V.size();
-    // back-links (maintainVertexNodePointerNonAtomic main.cu:1640-1682)
+    // back-links (maintainVertexNodePointerNonAtomic main.cu:1640-1682); every slot has one owner
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
     for (i64 v = 0; v < NV; ++v) {
         int o = V[v].owner, d = c.depth[o];
         float W = 1.0f / (1 << d), W2 = W * W;
@@ -894,22 +913,32 @@ static void marching_cubes(Ctx& c) {
             ec[k] = nc[k] + m * hw;
         }
     };
-    for (i64 i = c.base[D]; i < M; ++i) {
-        float hw = 1.0f / (1 << (D + 1)), W = 1.0f / (1 << D), W2 = W * W;
-        for (int j = 0; j < 12; ++j) {
-            float ec[3];
-            edge_center(&cen[3 * i], hw, j, ec);
-            i64 ownK = 0x7fffffff; int own = -1;
-            for (int k = 0; k < 27; ++k) {
-                int nb = c.neighs[27 * i + k];
-                if (nb == -1) continue;
-                if (sqdist(ec, &cen[3 * nb]) < W2 && ownK > c.key[nb]) { ownK = c.key[nb]; own = nb; }
+    {
+        std::vector<unsigned short> emask(M - c.base[D], 0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+        for (i64 i = c.base[D]; i < M; ++i) {
+            float hw = 1.0f / (1 << (D + 1)), W = 1.0f / (1 << D), W2 = W * W;
+            unsigned m = 0;
+            for (int j = 0; j < 12; ++j) {
+                float ec[3];
+                edge_center(&cen[3 * i], hw, j, ec);
+                i64 ownK = 0x7fffffff; int own = -1;
+                for (int k = 0; k < 27; ++k) {
+                    int nb = c.neighs[27 * i + k];
+                    if (nb == -1) continue;
+                    if (sqdist(ec, &cen[3 * nb]) < W2 && ownK > c.key[nb]) { ownK = c.key[nb]; own = nb; }
+                }
+                if (own == i) m |= 1u << j;
             }
-            if (own == i) E.push_back({j, (int)i});
+            emask[i - c.base[D]] = (unsigned short)m;
         }
+        for (i64 i = c.base[D]; i < M; ++i)
+            for (int j = 0; j < 12; ++j)
+                if ((emask[i - c.base[D]] >> j) & 1) E.push_back({j, (int)i});
     }
     // (maintainEdgeNodePointer main.cu:2021-2082)
-    for (size_t e = 0; e < E.size(); ++e) {
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+    for (i64 e = 0; e < (i64)E.size(); ++e) {
         int o = E[e].owner;
         float hw = 1.0f / (1 << (D + 1)), W = 1.0f / (1 << D), W2 = W * W;
         float ec[3];
@@ -929,26 +958,39 @@ static void marching_cubes(Ctx& c) {
     // --- faces of every depth (initFaceArray main.cu:2827-2899) ---
     struct Fac { int kind, owner, hasParent; };
     std::vector<Fac> Fa;
-    for (i64 i = 0; i < M; ++i) {
-        int d = c.depth[i];
-        float hw = 1.0f / (1 << (d + 1)), W = 1.0f / (1 << d), W2 = W * W;
-        int son = (int)((c.key[i] >> (3 * (D - d))) & 7);
-        for (int j = 0; j < 6; ++j) {
-            float fc[3] = {cen[3 * i], cen[3 * i + 1], cen[3 * i + 2]};
-            fc[j >> 1] += (2 * (j & 1) - 1) * hw;
-            i64 ownK = 0x7fffffff; int own = -1;
-            for (int k = 0; k < 27; ++k) {
-                int nb = c.neighs[27 * i + k];
-                if (nb == -1) continue;
-                if (sqdist(fc, &cen[3 * nb]) < W2 && ownK > c.key[nb]) { ownK = c.key[nb]; own = nb; }
+    {
+        std::vector<unsigned char> fmask(M, 0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+        for (i64 i = 0; i < M; ++i) {
+            int d = c.depth[i];
+            float hw = 1.0f / (1 << (d + 1)), W = 1.0f / (1 << d), W2 = W * W;
+            unsigned m = 0;
+            for (int j = 0; j < 6; ++j) {
+                float fc[3] = {cen[3 * i], cen[3 * i + 1], cen[3 * i + 2]};
+                fc[j >> 1] += (2 * (j & 1) - 1) * hw;
+                i64 ownK = 0x7fffffff; int own = -1;
+                for (int k = 0; k < 27; ++k) {
+                    int nb = c.neighs[27 * i + k];
+                    if (nb == -1) continue;
+                    if (sqdist(fc, &cen[3 * nb]) < W2 && ownK > c.key[nb]) { ownK = c.key[nb]; own = nb; }
+                }
+                if (own == i) m |= 1u << j;
             }
-            if (own == i) {
+            fmask[i] = (unsigned char)m;
+        }
+        for (i64 i = 0; i < M; ++i) {
+            if (!fmask[i]) continue;
+            int d = c.depth[i];
+            int son = (int)((c.key[i] >> (3 * (D - d))) & 7);
+            for (int j = 0; j < 6; ++j) {
+                if (!((fmask[i] >> j) & 1)) continue;
                 int hp = (c.parent[i] == -1) ? -1 : (parentFaceKind[son][j] != -1 ? 1 : -1);
                 Fa.push_back({j, (int)i, hp});
             }
         }
     }
-    for (size_t f = 0; f < Fa.size(); ++f) {  // maintainFaceNodePointer main.cu:2908-2955
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+    for (i64 f = 0; f < (i64)Fa.size(); ++f) {  // maintainFaceNodePointer main.cu:2908-2955
         int o = Fa[f].owner, d = c.depth[o];
         float hw = 1.0f / (1 << (d + 1)), W = 1.0f / (1 << d), W2 = W * W;
         float fc[3] = {cen[3 * (i64)o], cen[3 * (i64)o + 1], cen[3 * (i64)o + 2]};
@@ -1051,6 +1093,15 @@ static void marching_cubes(Ctx& c) {
     for (i64 i = 0; i < c.base[D]; ++i)
         if (c.children[8 * i] == -1 && (c.has_tri[i] || c.has_int[i])) roots.push_back((int)i);
     c.subdivide_roots = (i64)roots.size();
+    c.vcells[0] = c.vcells[1] = 0;
+    for (int r : roots) c.vcells[0] += (i64)1 << (3 * (D - c.depth[r]));
+    if (c.root_stride != 1) {
+        std::vector<int> kept;
+        if (c.root_stride > 1)
+            for (size_t k = 0; k < roots.size(); k += (size_t)c.root_stride) kept.push_back(roots[k]);
+        roots.swap(kept);
+    }
+    for (int r : roots) c.vcells[1] += (i64)1 << (3 * (D - c.depth[r]));
     if (roots.empty()) return;
 
     // working copy of the children pointers (the rebuild rewires them)
@@ -1069,8 +1120,11 @@ static void marching_cubes(Ctx& c) {
         };
         // vertices owned by rebuilt finest nodes (initSubdivideVertexOwner main.cu:1501-1566)
         std::vector<Vtx> SV;
+        std::vector<unsigned char> vmask(nv_nodes - first_D, 0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
         for (i64 i = first_D; i < nv_nodes; ++i) {
             const float* ncen = &nv.vcenter[3 * i];
+            unsigned m = 0;
             for (int j = 0; j < 8; ++j) {
                 float vp[3] = {ncen[0] + (2 * (j & 1) - 1) * hwD, ncen[1] + (2 * ((j & 2) >> 1) - 1) * hwD,
                                ncen[2] + (2 * ((j & 4) >> 2) - 1) * hwD};
@@ -1083,14 +1137,27 @@ static void marching_cubes(Ctx& c) {
                         if (ownK > kk) { ownK = kk; own = nb; }
                     }
                 }
-                if (own == MM + i) {
-                    Vtx v; memcpy(v.pos, vp, sizeof vp); v.owner = own; v.kind = j; v.depth = D;
-                    SV.push_back(v);
-                }
+                if (own == MM + i) m |= 1u << j;
+            }
+            vmask[i - first_D] = (unsigned char)m;
+        }
+        for (i64 i = first_D; i < nv_nodes; ++i) {
+            const unsigned m = vmask[i - first_D];
+            if (!m) continue;
+            const float* ncen = &nv.vcenter[3 * i];
+            for (int j = 0; j < 8; ++j) {
+                if (!((m >> j) & 1)) continue;
+                Vtx v;
+                v.pos[0] = ncen[0] + (2 * (j & 1) - 1) * hwD;
+                v.pos[1] = ncen[1] + (2 * ((j & 2) >> 1) - 1) * hwD;
+                v.pos[2] = ncen[2] + (2 * ((j & 4) >> 2) - 1) * hwD;
+                v.owner = (int)(MM + i); v.kind = j; v.depth = D;
+                SV.push_back(v);
             }
         }
         // (maintainSubdivideVertexNodePointer main.cu:1684-1793)
-        for (size_t v = 0; v < SV.size(); ++v) {
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+        for (i64 v = 0; v < (i64)SV.size(); ++v) {
             int o = SV[v].owner;
             for (int k = 0; k < 27; ++k) {
                 int nb = nv.vneighs[27 * (i64)(o - MM) + k];
@@ -1106,7 +1173,10 @@ static void marching_cubes(Ctx& c) {
         }
         // edges (initSubdivideEdgeArray main.cu:1868-1943, maintainSubdivideEdgeNodePointer :2085-2153)
         std::vector<Edg> SE;
+        std::vector<unsigned short> emask(nv_nodes - first_D, 0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
         for (i64 i = first_D; i < nv_nodes; ++i) {
+            unsigned m = 0;
             for (int j = 0; j < 12; ++j) {
                 float ec[3];
                 edge_center(&nv.vcenter[3 * i], hwD, j, ec);
@@ -1119,10 +1189,15 @@ static void marching_cubes(Ctx& c) {
                         if (ownK > kk) { ownK = kk; own = nb; }
                     }
                 }
-                if (own == MM + i) SE.push_back({j, own});
+                if (own == MM + i) m |= 1u << j;
             }
+            emask[i - first_D] = (unsigned short)m;
         }
-        for (size_t e = 0; e < SE.size(); ++e) {
+        for (i64 i = first_D; i < nv_nodes; ++i)
+            for (int j = 0; j < 12; ++j)
+                if ((emask[i - first_D] >> j) & 1) SE.push_back({j, (int)(MM + i)});
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 1024)
+        for (i64 e = 0; e < (i64)SE.size(); ++e) {
             int o = SE[e].owner;
             float ec[3];
             edge_center(&nv.vcenter[3 * (i64)(o - MM)], hwD, SE[e].kind, ec);
@@ -1194,6 +1269,7 @@ static void marching_cubes(Ctx& c) {
 
     auto rebuild_neighbours = [&](NodeView& nv, i64 lo, i64 hi, int d) {  // computeRebuildNeighbor
         const i64 MM = nv.M;
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(static)
         for (i64 i = lo; i < hi; ++i) {
             int son = (int)((nv.vkey[i] >> (3 * (D - d))) & 7);
             int par = nv.vparent[i];
@@ -1228,6 +1304,7 @@ static void marching_cubes(Ctx& c) {
         std::vector<i64> addr(D + 2, 0), num(D + 2, 0);
         for (int j = rd; j <= D; ++j) num[j] = qpow8(j - rd);
         for (int j = rd + 1; j <= D; ++j) addr[j] = addr[j - 1] + num[j - 1];
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(static)
         for (i64 i = 0; i < sz; ++i) {  // singleRebuildArray main.cu:3114-3155
             int rel = 0; i64 up = i * 7 + 1, b = 8;
             while (b <= up) { ++rel; b <<= 3; }
@@ -1325,6 +1402,8 @@ int orc_divergence(void* h) { divergence(*(Ctx*)h); return 0; }
 int orc_solve(void* h, int mode, double tol, int max_iter) { solve(*(Ctx*)h, mode, tol, max_iter); return 0; }
 int orc_point_values(void* h) { point_values(*(Ctx*)h); return 0; }
 int orc_marching_cubes(void* h) { marching_cubes(*(Ctx*)h); return 0; }
+// timing samples: subdivide every stride-th root only (0: none); the default 1 is the full path
+int orc_set_root_stride(void* h, int stride) { ((Ctx*)h)->root_stride = stride; return 0; }
 
 // one call for the whole path, reference CG schedule
 int orc_reconstruct(void* h, int mode, double tol, int max_iter) {
@@ -1378,6 +1457,7 @@ const void* orc_get(void* h, const char* name, int64_t* count) {
     if (n == "scale") { *count = 1; return &c->scale; }
     if (n == "iso") { *count = 1; return &c->iso; }
     if (n == "subdivide_roots") { *count = 1; return &c->subdivide_roots; }
+    if (n == "vcells") { *count = 2; return c->vcells; }
     *count = -1;
     return nullptr;
 }
