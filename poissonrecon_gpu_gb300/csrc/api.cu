@@ -33,6 +33,8 @@ void Ctx::free_all() {
     dfree(point_node, s); dfree(basis, s); dfree(ddot_div, s); dfree(full_tables, s);
     dfree(vfield, s); dfree(divergence, s); dfree(x, s); dfree(point_value, s);
     dfree(d_cg_iters, s); dfree(d_cg_rr, s);
+    dfree(d_has_tri, s); dfree(d_has_int, s);
+    n_coarse = 0;
 }
 
 int Ctx::kbegin(const char* name, double bytes) {
@@ -386,8 +388,8 @@ int prgpu_get_array(void* h, const char* name, void* dst, int64_t max_bytes, int
         if (n == "iso") return copy_out(c, &c->iso, 4, dst, max_bytes, nbytes, true);
     }
     if (c->stage >= 6) {
-        if (n == "has_tri") return copy_out(c, c->has_tri.data(), (int64_t)c->has_tri.size() * 4, dst, max_bytes, nbytes, true);
-        if (n == "has_int") return copy_out(c, c->has_int.data(), (int64_t)c->has_int.size() * 4, dst, max_bytes, nbytes, true);
+        if (n == "has_tri") return copy_out(c, c->d_has_tri, c->n_coarse * 4, dst, max_bytes, nbytes);
+        if (n == "has_int") return copy_out(c, c->d_has_int, c->n_coarse * 4, dst, max_bytes, nbytes);
         if (n == "batch_tri")
             return copy_out(c, c->batch_tri.data(), (int64_t)c->batch_tri.size() * 8, dst, max_bytes, nbytes, true);
         if (n == "subdivide_roots") return copy_out(c, &c->subdivide_roots, 8, dst, max_bytes, nbytes, true);

@@ -117,7 +117,9 @@ struct Ctx {
     // mesh (host, input coordinates)
     PinnedBuf<float> mesh_v;
     PinnedBuf<int32_t> mesh_f;
-    std::vector<int> has_tri, has_int;
+    int* d_has_tri = nullptr;           // per node at depth < D (device)
+    int* d_has_int = nullptr;
+    i64 n_coarse = 0;
     i64 subdivide_roots = 0;
     std::vector<i64> batch_tri;
     std::vector<i64> roots_per_depth;   // subdivided leaves by depth

@@ -70,7 +70,56 @@ struct EvalArgs {
     int D;
     const CPoly* basis;
     const float* x;
+    const float* x27;      // nodes [0, nx27): x of the 27 neighbours (0: none), 28 floats per node; or null
+    i64 nx27;
+    const float* lb;       // basis values at finest-lattice points (see lattice_basis), or null
+    i64 lb_off[17];        // start of each depth in lb
 };
+
+// B_{d,n}(u / 2^D) for a finest-lattice coordinate u: the value cpoly_value
+// computes, read from the table when u lies in the support [(n-1)w, (n+2)w]
+// (w = 2^(D-d), 3w+1 points per function), evaluated otherwise
+__device__ __forceinline__ float lattice_basis(const EvalArgs& a, int d, int n, int u) {
+    const int w = 1 << (a.D - d);
+    const int k = u - (n - 1) * w;
+    if (a.lb && k >= 0 && k <= 3 * w) return a.lb[a.lb_off[d] + (i64)n * (3 * w + 1) + k];
+    return cpoly_value<3>(a.basis[(1 << d) - 1 + n], (float)u * (1.0f / (float)(1 << a.D)));
+}
+
+__global__ void k_lattice_basis(const CPoly* __restrict__ basis, int D, i64 total, float* __restrict__ lb) {
+    const float inv = 1.0f / (float)(1 << D);
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+        // depth d holds 2^d functions of 3w+1 points: offset sum_{l<d} 2^l (3 2^(D-l) + 1)
+        int d = 0;
+        i64 off = 0;
+        for (;;) {
+            const i64 len = (1ll << d) * (3ll * (1ll << (D - d)) + 1);
+            if (e < off + len) break;
+            off += len;
+            ++d;
+        }
+        const int w = 1 << (D - d);
+        const i64 r = e - off;
+        const int n = (int)(r / (3 * w + 1)), k = (int)(r % (3 * w + 1));
+        lb[e] = cpoly_value<3>(basis[(1 << d) - 1 + n], (float)((n - 1) * w + k) * inv);
+    }
+}
+
+// x of the 27 neighbours of every node below the finest depth, contiguous per
+// node (the evaluation walks read one 112-byte row per ancestor)
+constexpr int X27_STRIDE = 28;
+__global__ void k_build_x27(NodeArrays nd, const float* __restrict__ x, i64 n, float* __restrict__ x27) {
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < n * X27_STRIDE; e += (i64)gridDim.x * blockDim.x) {
+        const i64 i = e / X27_STRIDE;
+        const int j = (int)(e % X27_STRIDE);
+        float v = 0.f;
+        if (j < 27) {
+            const int nb = nd.neigh[(i64)j * nd.M + i];
+            if (nb != -1) v = x[nb];
+        }
+        x27[e] = v;
+    }
+}
 
 // sum over the 27 neighbours of real node 'node' (at depth d, coordinates xyz)
 // of x_n * B_n(q), in neighbour order with the reference's FMA
@@ -86,6 +135,19 @@ __device__ __forceinline__ float level_sum(const EvalArgs& a, i64 node, int d, c
             int c = xyz[ax] + t - 1;
             bv[ax][t] = (c >= 0 && c < lim) ? cpoly_value<3>(a.basis[fb + c], q[ax]) : 0.f;
         }
+    if (node < a.nx27) {
+        // absent neighbours read 0: adding a zero product leaves the sum unchanged
+        const float4* row = reinterpret_cast<const float4*>(a.x27 + node * X27_STRIDE);
+        float xs[28];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const float4 t = row[k];
+            xs[4 * k] = t.x; xs[4 * k + 1] = t.y; xs[4 * k + 2] = t.z; xs[4 * k + 3] = t.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 27; ++j) val = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
+        return val;
+    }
     const i64 M = a.nd.M;
 #pragma unroll
     for (int j = 0; j < 27; ++j) {
@@ -93,6 +155,59 @@ __device__ __forceinline__ float level_sum(const EvalArgs& a, i64 node, int d, c
         if (nb == -1) continue;
         const float vx = bv[0][j / 9], vy = bv[1][(j / 3) % 3], vz = bv[2][j % 3];
         val = fmaf(a.x[nb] * vx * vy, vz, val);
+    }
+    return val;
+}
+
+// the x27 rows for nodes [0, n) on the stage's stream; null when n is 0
+inline float* build_x27(const Ctx& c, i64 n) {
+    if (n <= 0) return nullptr;
+    float* x27 = dalloc<float>(n * X27_STRIDE, c.stream);
+    k_build_x27<<<grid_for(n * X27_STRIDE, 256), 256, 0, c.stream>>>(c.nodes, c.x, n, x27);
+    CK_LAUNCH();
+    return x27;
+}
+
+// level_sum at a finest-lattice point u (q = u / 2^D), basis values from the table
+__device__ __forceinline__ float level_sum_u(const EvalArgs& a, i64 node, int d, const int xyz[3], const int u[3],
+                                             float val) {
+    const int lim = 1 << d;
+    float bv[3][3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int c = xyz[ax] + t - 1;
+            bv[ax][t] = (c >= 0 && c < lim) ? lattice_basis(a, d, c, u[ax]) : 0.f;
+        }
+    if (node < a.nx27) {
+        const float4* row = reinterpret_cast<const float4*>(a.x27 + node * X27_STRIDE);
+        float xs[28];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const float4 t = row[k];
+            xs[4 * k] = t.x; xs[4 * k + 1] = t.y; xs[4 * k + 2] = t.z; xs[4 * k + 3] = t.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 27; ++j) val = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
+        return val;
+    }
+    const i64 M = a.nd.M;
+#pragma unroll
+    for (int j = 0; j < 27; ++j) {
+        const int nb = a.nd.neigh[(i64)j * M + node];
+        if (nb == -1) continue;
+        val = fmaf(a.x[nb] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
+    }
+    return val;
+}
+__device__ __forceinline__ float walk_up_u(const EvalArgs& a, i64 node, const int u[3], float val) {
+    while (node != -1) {
+        const int d = a.nd.depth[node];
+        int xyz[3];
+        key_coords(a.nd.key[node], d, a.D, xyz);
+        val = level_sum_u(a, node, d, xyz, u, val);
+        node = a.nd.parent[node];
     }
     return val;
 }
@@ -127,13 +242,15 @@ void stage_points(Ctx& c) {
     c.point_value = dalloc<float>(c.N, s);
     double* sum = dalloc<double>(1, s);
     CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
-    EvalArgs a{c.nodes, c.D, c.basis, c.x};
+    float* x27 = build_x27(c, c.base[c.D]);
+    EvalArgs a{c.nodes, c.D, c.basis, c.x, x27, x27 ? c.base[c.D] : 0, nullptr, {0}};
     const int kt = c.kbegin("point_values", (double)c.N * (12 + 4 + 4) + (double)c.nodes.M * (4 + 4 + 8 + 108));
     k_point_values<<<grid_for(c.N, 128, 1ll << 30), 128, 0, s>>>(a, c.pts, c.point_node, c.N, c.point_value, sum);
     CK_LAUNCH();
     c.kend(kt);
     double h = read_scalar(sum, s);
     dfree(sum, s);
+    dfree(x27, s);
     c.iso = (float)h / (float)c.N;
 }
 
@@ -173,11 +290,12 @@ __device__ float owner_corner_value(const EvalArgs& a, i64 o, int kind, float is
     const int d = a.nd.depth[o];
     int xyz[3];
     key_coords(a.nd.key[o], d, a.D, xyz);
-    float q[3];
-    corner_pos(xyz, d, kind, q);
+    // the corner as a finest-lattice point: (xyz + bit) / 2^d = u / 2^D exactly
+    const int sh = a.D - d;
+    const int u[3] = {(xyz[0] + (kind & 1)) << sh, (xyz[1] + ((kind >> 1) & 1)) << sh, (xyz[2] + ((kind >> 2) & 1)) << sh};
     float val = 0.f;
     if (o > 0) {
-        val = walk_up(a, o, q, val);
+        val = walk_up_u(a, o, u, val);
         const int exceed = c_vid[kind];
         i64 node = o;
         for (int dd = d + 1; dd <= a.D; ++dd) {
@@ -186,7 +304,7 @@ __device__ float owner_corner_value(const EvalArgs& a, i64 o, int kind, float is
             node = c0 + exceed;
             int cx[3];
             key_coords(a.nd.key[node], dd, a.D, cx);
-            val = level_sum(a, node, dd, cx, q, val);
+            val = level_sum_u(a, node, dd, cx, u, val);
         }
     }
     return val - iso;
@@ -264,10 +382,28 @@ __global__ void k_mark_faces(NodeArrays nd, int D, i64 lo, i64 hi, const unsigne
     }
 }
 
+// corners of the leaves above the finest depth: mark each owner's corner once
+__global__ void k_coarse_need(NodeArrays nd, i64 lo, i64 hi, unsigned char* __restrict__ need) {
+    for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
+        if (nd.child0[i] != -1) continue;
+        for (int kind = 0; kind < 8; ++kind) {
+            int ok;
+            const int own = corner_owner(nd, i, kind, ok);
+            need[8 * (i64)own + ok] = 1;
+        }
+    }
+}
+__global__ void k_coarse_corner_values(EvalArgs a, i64 n, float iso, const unsigned char* __restrict__ need,
+                                       float* __restrict__ cval) {
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < 8 * n; e += (i64)gridDim.x * blockDim.x)
+        if (need[e]) cval[e] = owner_corner_value(a, e >> 3, (int)(e & 7), iso);
+}
+
 // leaves above the finest depth: sign change at their corners or a marked face
 // (ProcessLeafNodesAtOtherDepth main.cu:2957-2986, ifSubdivide :2988-2992)
-__global__ void k_coarse_leaves(EvalArgs a, i64 lo, i64 hi, float iso, const int* __restrict__ fflag,
-                                int* __restrict__ has_tri, int* __restrict__ has_int, int* __restrict__ is_root) {
+__global__ void k_coarse_leaves(EvalArgs a, i64 lo, i64 hi, const float* __restrict__ cval,
+                                const int* __restrict__ fflag, int* __restrict__ has_tri, int* __restrict__ has_int,
+                                int* __restrict__ is_root) {
     const NodeArrays& nd = a.nd;
     for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
         if (nd.child0[i] != -1) { is_root[i] = 0; continue; }
@@ -275,7 +411,7 @@ __global__ void k_coarse_leaves(EvalArgs a, i64 lo, i64 hi, float iso, const int
         for (int kind = 0; kind < 8; ++kind) {
             int ok;
             const int own = corner_owner(nd, i, kind, ok);
-            v[c_vid[kind]] = owner_corner_value(a, own, ok, iso);
+            v[c_vid[kind]] = cval[8 * (i64)own + ok];
         }
         const int sign = v[0] < 0 ? -1 : 1;
         int ht = 0;
@@ -346,15 +482,13 @@ __device__ float virtual_corner_value(const VArgs& v, int L, int r, const int oc
     const EvalArgs& a = v.e;
     const NodeArrays& nd = a.nd;
     const int D = a.D;
-    const float inv = 1.0f / (float)(1 << D);
-    const float q[3] = {(float)qc[0] * inv, (float)qc[1] * inv, (float)qc[2] * inv};
     int Lc[3];
     key_coords(nd.key[L], r, D, Lc);
     float val = 0.f;
     for (int d = D; d > r; --d) {
         const int sh = D - d;
         const int V[3] = {oc[0] >> sh, oc[1] >> sh, oc[2] >> sh};
-        const int fb = (1 << d) - 1, lim = 1 << d;
+        const int lim = 1 << d;
         // a virtual cell whose 3x3x3 block lies inside the leaf has no real neighbour
         const int span = 1 << (d - r);
         bool inner = true;
@@ -367,7 +501,7 @@ __device__ float virtual_corner_value(const VArgs& v, int L, int r, const int oc
         for (int ax = 0; ax < 3; ++ax)
             for (int t = 0; t < 3; ++t) {
                 int cc = V[ax] + t - 1;
-                bv[ax][t] = (cc >= 0 && cc < lim) ? cpoly_value<3>(a.basis[fb + cc], q[ax]) : 0.f;
+                bv[ax][t] = (cc >= 0 && cc < lim) ? lattice_basis(a, d, cc, qc[ax]) : 0.f;
             }
         for (int j = 0; j < 27; ++j) {
             const int N[3] = {V[0] + j / 9 - 1, V[1] + (j / 3) % 3 - 1, V[2] + j % 3 - 1};
@@ -386,7 +520,7 @@ __device__ float virtual_corner_value(const VArgs& v, int L, int r, const int oc
         }
     }
     // the leaf itself and its real ancestors
-    val = walk_up(a, L, q, val);
+    val = walk_up_u(a, L, qc, val);
     return val;
 }
 
@@ -1109,6 +1243,12 @@ __global__ void k_vertex_ids(const u64* __restrict__ keys, const uint32_t* __res
         }
     }
 }
+// subdivision roots: node index and depth, in node order
+__global__ void k_root_list(NodeArrays nd, const int* __restrict__ is_root, const int* __restrict__ pos, i64 n,
+                            int2* __restrict__ out) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        if (is_root[i]) out[pos[i]] = make_int2((int)i, (int)nd.depth[i]);
+}
 __global__ void k_key_heads(const u64* __restrict__ keys, i64 n, int* __restrict__ f) {
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
         f[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1 : 0;
@@ -1139,7 +1279,21 @@ void stage_mesh(Ctx& c) {
     const int D = c.D;
     const NodeArrays& nd = c.nodes;
     const i64 M = nd.M, lo = c.base[D], nD = c.count[D];
-    EvalArgs ea{c.nodes, D, c.basis, c.x};
+    float* x27 = build_x27(c, lo);
+    EvalArgs ea{c.nodes, D, c.basis, c.x, x27, x27 ? lo : 0, nullptr, {0}};
+    float* lb = nullptr;
+    {
+        i64 total = 0;
+        for (int d = 0; d <= D; ++d) {
+            ea.lb_off[d] = total;
+            total += (1ll << d) * (3ll * (1ll << (D - d)) + 1);
+        }
+        ea.lb_off[D + 1] = total;
+        lb = dalloc<float>(total, s);
+        k_lattice_basis<<<grid_for(total, 256), 256, 0, s>>>(c.basis, D, total, lb);
+        CK_LAUNCH();
+        ea.lb = lb;
+    }
     // ---- finest corner values, categories
     float* cval = dalloc<float>(8 * nD, s);
     float* cell_v = dalloc<float>(8 * nD, s);
@@ -1157,48 +1311,62 @@ void stage_mesh(Ctx& c) {
     // ---- face marks and subdivision roots
     int* fflag = dalloc<int>(6 * M, s);
     CK(cudaMemsetAsync(fflag, 0, (size_t)(6 * M) * sizeof(int), s));
+    kt = c.kbegin("mark_faces", (double)nD * (1 + 108) + (double)M * 24);
     k_mark_faces<<<grid_for(nD, 128, 1ll << 30), 128, 0, s>>>(nd, D, lo, M, cat, fflag);
     CK_LAUNCH();
+    c.kend(kt);
     const i64 nCoarse = lo;   // nodes at depth < D
-    int* has_tri = dalloc<int>(nCoarse, s);
-    int* has_int = dalloc<int>(nCoarse, s);
+    dfree(c.d_has_tri, s);
+    dfree(c.d_has_int, s);
+    c.n_coarse = nCoarse;
+    int* has_tri = c.d_has_tri = dalloc<int>(nCoarse, s);
+    int* has_int = c.d_has_int = dalloc<int>(nCoarse, s);
     int* is_root = dalloc<int>(nCoarse, s);
     CK(cudaMemsetAsync(has_tri, 0, nCoarse * sizeof(int), s));
     CK(cudaMemsetAsync(has_int, 0, nCoarse * sizeof(int), s));
     CK(cudaMemsetAsync(is_root, 0, nCoarse * sizeof(int), s));
     if (nCoarse > 1) {
-        const int kc = c.kbegin("coarse_leaves", (double)nCoarse * (4 + 108 + 8 + 3 * 4) + (double)M * 4);
-        k_coarse_leaves<<<grid_for(nCoarse - 1, 128, 1ll << 30), 128, 0, s>>>(ea, 1, nCoarse, c.iso, fflag, has_tri,
+        const int kc = c.kbegin("coarse_leaves", (double)nCoarse * (4 + 108 + 8 + 3 * 4 + 8 * 4) + (double)M * 4);
+        unsigned char* need = dalloc<unsigned char>(8 * nCoarse, s);
+        float* ccv = dalloc<float>(8 * nCoarse, s);
+        CK(cudaMemsetAsync(need, 0, 8 * nCoarse, s));
+        k_coarse_need<<<grid_for(nCoarse - 1, 256), 256, 0, s>>>(nd, 1, nCoarse, need);
+        CK_LAUNCH();
+        k_coarse_corner_values<<<grid_for(8 * nCoarse, 128, 1ll << 30), 128, 0, s>>>(ea, nCoarse, c.iso, need, ccv);
+        CK_LAUNCH();
+        k_coarse_leaves<<<grid_for(nCoarse - 1, 128, 1ll << 30), 128, 0, s>>>(ea, 1, nCoarse, ccv, fflag, has_tri,
                                                                              has_int, is_root);
         CK_LAUNCH();
         c.kend(kc);
+        dfree(need, s);
+        dfree(ccv, s);
     }
     dfree(fflag, s);
-    c.has_tri.assign(nCoarse, 0);
-    c.has_int.assign(nCoarse, 0);
-    std::vector<int> hroot(nCoarse, 0);
-    CK(cudaMemcpyAsync(c.has_tri.data(), has_tri, nCoarse * sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(c.has_int.data(), has_int, nCoarse * sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(hroot.data(), is_root, nCoarse * sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    dfree(has_tri, s); dfree(has_int, s); dfree(is_root, s);
-    // roots in node order; batches: one per root above depth 3, one per depth from 3
+    // subdivision roots in node order, compacted on the device
+    std::vector<int2> hroots;
+    {
+        int* rpos = dalloc<int>(nCoarse + 1, s);
+        exclusive_scan<int, int>(is_root, rpos, nCoarse, rpos + nCoarse, s);
+        const i64 nr = read_scalar(rpos + nCoarse, s);
+        int2* dr = dalloc<int2>(std::max<i64>(nr, 1), s);
+        k_root_list<<<grid_for(nCoarse, 256), 256, 0, s>>>(nd, is_root, rpos, nCoarse, dr);
+        CK_LAUNCH();
+        hroots.resize(nr);
+        if (nr > 0) CK(cudaMemcpyAsync(hroots.data(), dr, nr * sizeof(int2), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        dfree(rpos, s);
+        dfree(dr, s);
+    }
+    dfree(is_root, s);
+    // batches: one per root above depth 3, one per depth from 3
     std::vector<VRoot> roots;
     std::vector<int> bflag_host;   // filled lazily below
-    std::vector<int> depth_of(nCoarse, 0);
-    {
-        std::vector<int8_t> hd(nCoarse);
-        CK(cudaMemcpyAsync(hd.data(), nd.depth, nCoarse * sizeof(int8_t), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        for (i64 i = 0; i < nCoarse; ++i) depth_of[i] = hd[i];
-    }
     int nb = 0;
     std::vector<int> depth_batch(D + 1, 0);
-    for (i64 i = 0; i < nCoarse; ++i) {
-        if (!hroot[i]) continue;
+    for (const int2& hr : hroots) {
         VRoot R;
-        R.node = (int)i;
-        R.depth = depth_of[i];
+        R.node = hr.x;
+        R.depth = hr.y;
         R.pad = 0;
         if (R.depth < 3) R.batch = ++nb;
         else {
@@ -1416,6 +1584,7 @@ void stage_mesh(Ctx& c) {
         em.keys = dalloc<u64>(nem, s);
         em.slot = dalloc<uint32_t>(nem, s);
         em.pos = dalloc<float>(3 * nem, s);
+        const int kem = c.kbegin("emit", (double)nem * (8 + 4 + 12));
         if (nact_real > 0) {
             k_emit_real<<<grid_for(nact_real, 128, 1ll << 30), 128, 0, s>>>(nd, em, lo, act_real, nact_real, cat,
                                                                             tri_real, cell_v);
@@ -1428,6 +1597,7 @@ void stage_mesh(Ctx& c) {
                                                                                tri_virt);
             CK_LAUNCH();
         }
+        c.kend(kem);
         u64* ktmp = dalloc<u64>(nem, s);
         uint32_t* stmp = dalloc<uint32_t>(nem, s);
         const int ks = c.kbegin("edge_sort", (double)nem * 12 * 2);
@@ -1435,6 +1605,7 @@ void stage_mesh(Ctx& c) {
         c.kend(ks);
         dfree(ktmp, s);
         dfree(stmp, s);
+        const int kvi = c.kbegin("vertex_ids", (double)nem * (8 * 2 + 4 + 4 + 12));
         int* hf = dalloc<int>(nem, s);
         int* hp = dalloc<int>(nem + 1, s);
         k_key_heads<<<grid_for(nem, 256), 256, 0, s>>>(em.keys, nem, hf);
@@ -1447,6 +1618,7 @@ void stage_mesh(Ctx& c) {
                                                         make_float3(c.center[0], c.center[1], c.center[2]),
                                                         tri_vid, vpos);
         CK_LAUNCH();
+        c.kend(kvi);
         c.mesh_v.resize(3 * nvert);
         c.mesh_f.resize(nem);
         CK(cudaMemcpyAsync(c.mesh_v.data(), vpos, 3 * nvert * sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -1462,6 +1634,8 @@ void stage_mesh(Ctx& c) {
     dfree(d_small, s); dfree(d_small_cells, s); dfree(d_small_lat, s);
     dfree(lat_small, s); dfree(lat_brick, s); dfree(live, s);
     dfree(cell_v, s);
+    dfree(x27, s);
+    dfree(lb, s);
     dfree(cat, s);
     dfree(ntri, s);
 }

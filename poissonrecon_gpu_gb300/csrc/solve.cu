@@ -62,7 +62,8 @@ struct CgArgs {
     const float* b;
     float* x;
     float* r;
-    float* p;
+    float* p;               // search direction, two buffers used alternately
+    float* p2;
     float* q;
     PartState* state;
     int* err;
@@ -126,7 +127,7 @@ __global__ void k_group_table(NodeArrays nd, i64 ngroups, int* __restrict__ gn) 
 
 constexpr int CG_TILE_GROUPS = CG_BLOCK / 8;   // sibling groups per tile, one thread per row
 
-__global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
+__global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
                                                      const int* __restrict__ block_depth) {
     __shared__ float sp[CG_TILE_GROUPS * 64];
     __shared__ float sst[27];
@@ -170,23 +171,16 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __
     float r1 = (float)bb;
     float r0 = 0.f;
     int k = 1;
+    // p = r + beta p is formed where p is read: from the previous direction in
+    // 'pold' (never written during the pass) into 'pnew' (each row by its own thread)
+    const float* pold = a.p2;
+    float* pnew = a.p;
     while (ok) {
         const bool go = (a.mode == PRGPU_SOLVE_REFERENCE) ? (r1 > a.tol2) : ((double)r1 > a.rel2 * bb);
         if (!go || k > a.max_iter) break;
-        // p = r + beta p
-        if (k > 1) {
-            const float beta = r1 / r0;
-            for (i64 t = start; t < dp.n; t += stride) {
-                const i64 i = dp.lo + t;
-                a.p[i] = fmaf(beta, a.p[i], a.r[i]);
-            }
-        } else {
-            for (i64 t = start; t < dp.n; t += stride) {
-                const i64 i = dp.lo + t;
-                a.p[i] = a.r[i];
-            }
-        }
-        if (!part_barrier(ps, dp.nblocks, a.err, &sh_ok)) break;
+        const bool first = (k == 1);
+        const float beta = first ? 0.f : r1 / r0;
+        auto pdir = [&](i64 i) -> float { return first ? a.r[i] : fmaf(beta, pold[i], a.r[i]); };
         // q = A p, partial p.q
         loc = 0;
         if (d == 0) {
@@ -196,10 +190,12 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __
 #pragma unroll
                 for (int j = 0; j < 27; ++j) {
                     const int nb = a.neigh[(i64)j * a.M + i];
-                    if (nb != -1 && sst[j] != 0.f) o = fmaf(sst[j], a.p[nb], o);
+                    if (nb != -1 && sst[j] != 0.f) o = fmaf(sst[j], pdir(nb), o);
                 }
+                const float pi = pdir(i);
+                pnew[i] = pi;
                 a.q[i] = o;
-                loc += (double)(a.p[i] * o);
+                loc += (double)(pi * o);
             }
         } else {
             const i64 gfirst = (dp.lo - 1) >> 3, ng = dp.n >> 3;
@@ -216,7 +212,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __
                     if (g < ng) {
                         const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
                         const int cn = a.gn[(i64)jp * a.ngroups + gfirst + g];
-                        if (cn != -1) pv = a.p[cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1))];
+                        if (cn != -1) pv = pdir(cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)));
                     }
                     sp[e] = pv;
                 }
@@ -228,8 +224,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __
 #pragma unroll
                     for (int j = 0; j < 27; ++j)
                         o = fmaf(sst[j], blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
+                    const float pi = blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
+                    pnew[dp.lo + 8 * g + ch] = pi;
                     a.q[dp.lo + 8 * g + ch] = o;
-                    loc += (double)(blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)] * o);
+                    loc += (double)(pi * o);
                 }
             }
         }
@@ -240,7 +238,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __
         loc = 0;
         for (i64 t = start; t < dp.n; t += stride) {
             const i64 i = dp.lo + t;
-            a.x[i] = fmaf(al, a.p[i], a.x[i]);
+            a.x[i] = fmaf(al, pnew[i], a.x[i]);
             const float ri = fmaf(nal, a.q[i], a.r[i]);
             a.r[i] = ri;
             loc += (double)(ri * ri);
@@ -248,6 +246,8 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_all(CgArgs a, const CgDepth* __
         r0 = r1;
         r1 = (float)preduce(loc, ok);
         ++k;
+        pold = pnew;
+        pnew = (pnew == a.p) ? a.p2 : a.p;
     }
     if (rank == 0 && threadIdx.x == 0) {
         ps->iters = k - 1;
@@ -265,6 +265,7 @@ void stage_solve(Ctx& c) {
     float* r = dalloc<float>(M, s);
     float* p = dalloc<float>(M, s);
     float* q = dalloc<float>(M, s);
+    float* p2 = dalloc<float>(M, s);
     // sibling-group table for the matrix-vector products
     const i64 ngroups = (M - 1) / 8;
     int* gn = dalloc<int>(std::max<i64>(ngroups * 27, 1), s);
@@ -340,6 +341,7 @@ void stage_solve(Ctx& c) {
     a.x = c.x;
     a.r = r;
     a.p = p;
+    a.p2 = p2;
     a.q = q;
     a.state = st;
     a.err = err;
@@ -357,13 +359,14 @@ void stage_solve(Ctx& c) {
     c.cg_rr.assign(D + 1, 0.f);
     for (int d = 0; d <= D; ++d) { c.cg_iters[d] = hs[d].iters; c.cg_rr[d] = hs[d].rr; }
     if (kt >= 0) {
-        // compulsory per row and iteration: the group table (27 indices per 8 rows), p
-        // gathered once, p/q/x/r streams (read p,r,q,x; write p,q,x,r: 7 words)
+        // compulsory per row and iteration: the group table (27 indices per 8 rows), the
+        // previous direction and r read once, p and q written, then p/q/x/r read and x/r
+        // written (8 words)
         double bytes = 0;
-        for (int d = 0; d <= D; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 7 * 4);
+        for (int d = 0; d <= D; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 8 * 4);
         c.kpending[kt].bytes = bytes;
     }
-    dfree(r, s); dfree(p, s); dfree(q, s); dfree(gn, s);
+    dfree(r, s); dfree(p, s); dfree(p2, s); dfree(q, s); dfree(gn, s);
     dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(err, s);
     if (herr) {
         set_last_error("solver barrier timed out");
