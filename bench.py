@@ -281,7 +281,8 @@ def main():
         "stages_ms": stats.get("ms"),
         "cg_iters": stats.get("cg_iters"),
         "kernels": stats.get("kernels"),
-        "subdivision": {k: stats.get(k) for k in ("roots_per_depth", "virtual_cells", "bricks", "live_bricks")},
+        "subdivision": {k: stats.get(k) for k in ("roots_per_depth", "virtual_cells", "bricks", "live_bricks",
+                                                  "foreign_corners")},
         "nodes": stats.get("nodes"),
         "mesh": {"vertices": nv, "triangles": nt},
     }

@@ -124,7 +124,8 @@ struct Ctx {
     std::vector<i64> batch_tri;
     std::vector<i64> roots_per_depth;   // subdivided leaves by depth
     i64 virtual_cells = 0;
-    i64 total_bricks = 0, live_bricks = 0;   // large subdivided leaves: bricks, and those not culled
+    i64 total_bricks = 0, live_bricks = 0;   // subdivided leaves: bricks, and those not culled
+    i64 foreign_corners = 0;                 // brick corners owned by another leaf of the batch
 
     StageTimes t;
     bool profile = false;

@@ -526,42 +526,11 @@ __device__ float virtual_corner_value(const VArgs& v, int L, int r, const int oc
 
 __device__ __forceinline__ u64 cell_key_D(const int c[3], int D) { return coords_key(c[0], c[1], c[2], D, D); }
 
-// one thread per lattice corner of the listed roots (the small ones)
-__global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i64* __restrict__ list_prefix,
-                                  int nlist, i64 total, float* __restrict__ lat) {
-    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nlist - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (list_prefix[mid] <= e) lo = mid; else hi = mid - 1;
-        }
-        const int ri = list[lo];
-        const VRoot R = v.roots[ri];
-        const int D = v.e.D, S = 1 << (D - R.depth), S1 = S + 1;
-        const i64 loc = e - list_prefix[lo];
-        const int u = (int)(loc / ((i64)S1 * S1)), w = (int)((loc / S1) % S1), z = (int)(loc % S1);
-        int Lc[3];
-        key_coords(v.e.nd.key[R.node], R.depth, D, Lc);
-        const int qc[3] = {Lc[0] * S + u, Lc[1] * S + w, Lc[2] * S + z};
-        // owner: min key among batch cells sharing the corner
-        u64 best = ~0ull;
-        int own_root = -1, oc[3] = {0, 0, 0};
-        for (int eo = 0; eo < 8; ++eo) {
-            const int cell[3] = {qc[0] - (eo & 1), qc[1] - ((eo >> 1) & 1), qc[2] - ((eo >> 2) & 1)};
-            const int m = batch_member(v, R, Lc, cell);
-            if (m < 0) continue;
-            const u64 kk = cell_key_D(cell, D);
-            if (kk < best) { best = kk; own_root = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
-        }
-        lat[e] = virtual_corner_value(v, own_root, R.depth, oc, qc) - v.iso;
-    }
-}
-
-// ---- large subdivided leaves (lattice edge >= 16): bricks of 8^3 cells.
+// ---- subdivided leaves in bricks: the leaf's lattice of finest cells is cut
+// into bricks of B^3 cells, B = min(lattice edge, 8).
 //
-// Most corners of a large subdivided leaf lie far from the surface.  The leaf
-// is cut into bricks of 8^3 cells (9^3 corners) and each brick is bounded
-// before any of its corners is evaluated:
+// Most corners of a subdivided leaf lie far from the surface.  Each brick is
+// bounded before any of its corners is evaluated:
 //   * every term of a corner value is x_n * B_x * B_y * B_z with the
 //     single-precision basis values the evaluation uses, so the range of a term
 //     over the corners that include it is an interval product; terms that only
@@ -574,8 +543,8 @@ __global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i
 // The surviving ("live") bricks are evaluated exactly, in the order of
 // virtual_corner_value, so culling changes no value.  Corners on the leaf's
 // lower faces may be owned by a cell of another leaf of the same depth batch:
-// those go through virtual_corner_value, and a brick with such a corner is
-// never culled.
+// those go through virtual_corner_value (k_foreign_corners), and a brick with
+// such a corner is never culled.
 //
 // Everything a brick needs along one axis depends only on the leaf, the axis
 // and the brick's index along it (a "brick row"), so it is tabulated once per
@@ -587,50 +556,49 @@ __global__ void k_virtual_corners(VArgs v, const int* __restrict__ list, const i
 //   RA[l][t]      range over k of BT[l][t][k], l <= r
 //   RW[d][n]      range (with 0) of the depth-d function of window cell n over
 //                 the corners whose owner cell is within one cell of it
-constexpr int BR = 8;              // brick edge (cells); corners per axis BR+1
+constexpr int BR = 8;              // largest brick edge (cells); corners per axis up to BR+1
 constexpr int BR1 = BR + 1;
 constexpr int BR_CORNERS = BR1 * BR1 * BR1;
-constexpr int BR_CELLS = BR * BR * BR;
 constexpr int BR_BLOCK = 128;
 constexpr int BR_LEVELS = 16;      // depths 0..15
 constexpr int BR_WEXT = BR + 3;    // window edge at the finest depth
 // window cells over all virtual depths of a brick whose first corner is a
-// multiple of 8: 11^3 + 7^3 + 5^3 + 12 * 4^3 = 2567
+// multiple of its edge B <= 8: at most 11^3 + 7^3 + 5^3 + 12 * 4^3 = 2567
 constexpr int BR_XW = 2600;
-// brick-row table: BT (27 per depth), RA (6 per depth), RW (22 per depth)
+// brick-row table: BT (36 per depth), RA (6 per depth), RW (22 per depth)
 constexpr int ROW_BT = 0, ROW_RA = 36, ROW_RW = 42, ROW_PER_DEPTH = 64;
 
-struct BrickIndex {                // bricks of the large roots, numbered root by root
-    const int* big;                // root indices of the large roots
-    const i64* prefix;             // first brick of each large root
-    const i64* row_prefix;         // first brick row of each large root (3 * bricks per edge rows each)
-    int nbig;
+__device__ __forceinline__ int brick_edge(int D, int r) { return min(1 << (D - r), BR); }
+
+struct BrickIndex {                // bricks of all subdivided leaves, numbered root by root
+    const i64* prefix;             // first brick of each root
+    const i64* row_prefix;         // first brick row of each root (3 * bricks per edge rows each)
+    int nroots;
     const float* rows;             // brick-row tables, 64 (D+1) floats each
-    const float* xl;               // per large root: x of the 27 neighbours of each ancestor, 16 x 27
+    const float* xl;               // per root: x of the 27 neighbours of each ancestor, 16 x 27
 };
 struct VBrick {
     int root;                      // index into roots
-    int big;                       // index into the large roots
     int b[3];                      // brick coordinates in the leaf
 };
 __device__ __forceinline__ VBrick brick_of(const VArgs& v, const BrickIndex& bx, i64 g) {
-    int lo = 0, hi = bx.nbig - 1;
+    int lo = 0, hi = bx.nroots - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (bx.prefix[mid] <= g) lo = mid; else hi = mid - 1;
     }
     VBrick b;
-    b.big = lo;
-    b.root = bx.big[lo];
-    const int nb = (1 << (v.e.D - v.roots[b.root].depth)) / BR;
+    b.root = lo;
+    const int r = v.roots[lo].depth;
+    const int nb = (1 << (v.e.D - r)) / brick_edge(v.e.D, r);
     const i64 l = g - bx.prefix[lo];
     b.b[0] = (int)(l / ((i64)nb * nb));
     b.b[1] = (int)((l / nb) % nb);
     b.b[2] = (int)(l % nb);
     return b;
 }
-__device__ __forceinline__ const float* brick_row(const BrickIndex& bx, int D, int big, int nb, int ax, int b) {
-    return bx.rows + (bx.row_prefix[big] + (i64)ax * nb + b) * (i64)(ROW_PER_DEPTH * (D + 1));
+__device__ __forceinline__ const float* brick_row(const BrickIndex& bx, int D, int root, int nb, int ax, int b) {
+    return bx.rows + (bx.row_prefix[root] + (i64)ax * nb + b) * (i64)(ROW_PER_DEPTH * (D + 1));
 }
 
 __device__ __forceinline__ float x_or_zero(const EvalArgs& a, int node) { return node < 0 ? 0.f : a.x[node]; }
@@ -661,26 +629,37 @@ __device__ __forceinline__ void term_interval(float x, const float* lo, const fl
     thi = b;
 }
 
-// can a lower-face corner of brick b[] be owned by a cell of another leaf of
-// the batch?  Only if a lower neighbour across a face the brick touches is a
-// root of the same batch (batch_member's rule)
-__device__ __forceinline__ bool brick_foreign_possible(const VArgs& v, const VRoot& R, const int b[3]) {
+// can a corner of brick b[] (nb bricks per edge) be owned by a cell of another
+// leaf of the batch?  The candidate cells of a corner lie in the leaf or in a
+// neighbour at offset (dx,dy,dz): -1 on an axis only for corners on the leaf's
+// lower face there, +1 only for corners on its upper face.  A cell outside the
+// leaf can have the least key only if one offset is -1 (Morton order is
+// monotone per axis).  So: only if such a neighbour is a root of the same batch
+// (batch_member's rule)
+__device__ __forceinline__ bool brick_foreign_possible(const VArgs& v, const VRoot& R, const int b[3], int nb) {
     if (R.depth < 3 || (b[0] && b[1] && b[2])) return false;
     const NodeArrays& nd = v.e.nd;
-    for (int m = 1; m < 8; ++m) {
-        const int dx = (m & 1) ? -1 : 0, dy = (m & 2) ? -1 : 0, dz = (m & 4) ? -1 : 0;
-        if ((dx && b[0]) || (dy && b[1]) || (dz && b[2])) continue;
-        const int nb = nd.neigh[(i64)(9 * (dx + 1) + 3 * (dy + 1) + (dz + 1)) * nd.M + R.node];
-        if (nb != -1 && v.batch_root_flag[nb] == R.batch) return true;
+    for (int j = 0; j < 27; ++j) {
+        const int off[3] = {j / 9 - 1, (j / 3) % 3 - 1, j % 3 - 1};
+        bool ok = false, allowed = true;
+        for (int ax = 0; ax < 3; ++ax) {
+            if (off[ax] == -1) { ok = true; if (b[ax] != 0) allowed = false; }
+            if (off[ax] == 1 && b[ax] != nb - 1) allowed = false;
+        }
+        if (!ok || !allowed) continue;
+        const int n = nd.neigh[(i64)j * nd.M + R.node];
+        if (n != -1 && v.batch_root_flag[n] == R.batch) return true;
     }
     return false;
 }
 
-// window of depth d around a brick along one axis: origin and extent of the
-// cells the brick's owner cells can reach; 'cross' when that reaches outside the leaf
-__device__ __forceinline__ void window_axis(int g0, int Lc_ax, int r, int d, int D, int& wlo, int& ext, bool& cross) {
+// window of depth d around a brick (edge B) along one axis: origin and extent
+// of the cells the brick's owner cells can reach; 'cross' when that reaches
+// outside the leaf
+__device__ __forceinline__ void window_axis(int g0, int B, int Lc_ax, int r, int d, int D, int& wlo, int& ext,
+                                            bool& cross) {
     const int sh = D - d, span = 1 << (d - r);
-    const int Vlo = (g0 - 1) >> sh, Vhi = (g0 + BR - 1) >> sh;
+    const int Vlo = (g0 - 1) >> sh, Vhi = (g0 + B - 1) >> sh;
     const int llo = Lc_ax * span;
     cross = (Vlo - 1 < llo || Vhi + 1 >= llo + span);
     wlo = Vlo - 1;
@@ -691,48 +670,49 @@ __device__ __forceinline__ void window_axis(int g0, int Lc_ax, int r, int d, int
 __global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrows, float* __restrict__ rows) {
     const EvalArgs& a = v.e;
     const int D = a.D;
-    const float inv = 1.0f / (float)(1 << D);
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < nrows * (D + 1); e += (i64)gridDim.x * blockDim.x) {
         const i64 row = e / (D + 1);
         const int d = (int)(e % (D + 1));
         const int4 rd = rowdesc[row];             // root, axis, brick index
         const VRoot R = v.roots[rd.x];
-        const int ax = rd.y, r = R.depth, S = 1 << (D - r);
+        const int ax = rd.y, r = R.depth, S = 1 << (D - r), B = brick_edge(D, r);
         int Lc[3];
         key_coords(a.nd.key[R.node], r, D, Lc);
-        const int g0 = Lc[ax] * S + rd.z * BR;
-        const int c0 = rd.z * BR;
+        const int g0 = Lc[ax] * S + rd.z * B;
+        const int c0 = rd.z * B;
         float* out = rows + row * (i64)(ROW_PER_DEPTH * (D + 1));
         float bt[4][BR1];
         for (int t = 0; t < 4; ++t)
             for (int k = 0; k <= BR; ++k) {
-                const int cidx = (d <= r) ? (Lc[ax] >> (r - d)) + t - 1 : ((g0 + k - 1) >> (D - d)) + t - 1;
                 float val = 0.f;
-                if (cidx >= 0 && cidx < (1 << d)) val = cpoly_value<3>(a.basis[(1 << d) - 1 + cidx], (float)(g0 + k) * inv);
+                if (k <= B) {
+                    const int cidx = (d <= r) ? (Lc[ax] >> (r - d)) + t - 1 : ((g0 + k - 1) >> (D - d)) + t - 1;
+                    if (cidx >= 0 && cidx < (1 << d)) val = lattice_basis(a, d, cidx, g0 + k);
+                }
                 bt[t][k] = val;
                 out[ROW_BT * (D + 1) + (d * 4 + t) * BR1 + k] = val;
             }
         if (d <= r) {
             for (int t = 0; t < 3; ++t) {
                 float mn = bt[t][0], mx = bt[t][0];
-                for (int k = 1; k <= BR; ++k) { mn = fminf(mn, bt[t][k]); mx = fmaxf(mx, bt[t][k]); }
+                for (int k = 1; k <= B; ++k) { mn = fminf(mn, bt[t][k]); mx = fmaxf(mx, bt[t][k]); }
                 out[ROW_RA * (D + 1) + (d * 3 + t) * 2] = mn;
                 out[ROW_RA * (D + 1) + (d * 3 + t) * 2 + 1] = mx;
             }
         } else {
             int wlo, ext;
             bool cross;
-            window_axis(g0, Lc[ax], r, d, D, wlo, ext, cross);
+            window_axis(g0, B, Lc[ax], r, d, D, wlo, ext, cross);
             const int sh = D - d, lim = 1 << d;
             for (int n = 0; n < BR_WEXT; ++n) {
                 const int N = wlo + n;
                 float mn = 0.f, mx = 0.f;             // 0: corners without this term
                 if (n < ext && N >= 0 && N < lim) {
-                    for (int k = 0; k <= BR; ++k) {
+                    for (int k = 0; k <= B; ++k) {
                         const int Va = (g0 + k - 1) >> sh;
                         const int Vb = (k == 0 && c0 == 0) ? (g0 >> sh) : Va;   // lower-face owner cell
                         if (N < Va - 1 || N > Vb + 1) continue;
-                        const float b = cpoly_value<3>(a.basis[lim - 1 + N], (float)(g0 + k) * inv);
+                        const float b = lattice_basis(a, d, N, g0 + k);
                         mn = fminf(mn, b);
                         mx = fmaxf(mx, b);
                     }
@@ -744,13 +724,13 @@ __global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrow
     }
 }
 
-// x of the 27 neighbours of each ancestor of a large root (0: no neighbour)
-__global__ void k_brick_xl(VArgs v, const int* __restrict__ big, int nbig, float* __restrict__ xl) {
+// x of the 27 neighbours of each ancestor of every root (0: no neighbour)
+__global__ void k_brick_xl(VArgs v, int nroots, float* __restrict__ xl) {
     const NodeArrays& nd = v.e.nd;
-    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < (i64)nbig * BR_LEVELS * 27;
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < (i64)nroots * BR_LEVELS * 27;
          e += (i64)gridDim.x * blockDim.x) {
-        const int bi = (int)(e / (BR_LEVELS * 27)), l = (int)((e / 27) % BR_LEVELS), j = (int)(e % 27);
-        const VRoot R = v.roots[big[bi]];
+        const int ri = (int)(e / (BR_LEVELS * 27)), l = (int)((e / 27) % BR_LEVELS), j = (int)(e % 27);
+        const VRoot R = v.roots[ri];
         float x = 0.f;
         if (l <= R.depth) {
             int node = R.node;
@@ -789,17 +769,17 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
     for (i64 bi = warp; bi < nbricks; bi += nwarps) {
         const VBrick B = brick_of(v, bix, bi);
         const VRoot R = v.roots[B.root];
-        if (brick_foreign_possible(v, R, B.b)) {   // never culled
+        if (brick_foreign_possible(v, R, B.b, (1 << (D - R.depth)) / brick_edge(D, R.depth))) {   // never culled
             if (lane == 0) culled[bi] = 0;
             continue;
         }
-        const int r = R.depth, S = 1 << (D - r), L = R.node, nb = S / BR;
+        const int r = R.depth, S = 1 << (D - r), L = R.node, E = brick_edge(D, r), nb = S / E;
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
-        const int g0[3] = {Lc[0] * S + B.b[0] * BR, Lc[1] * S + B.b[1] * BR, Lc[2] * S + B.b[2] * BR};
+        const int g0[3] = {Lc[0] * S + B.b[0] * E, Lc[1] * S + B.b[1] * E, Lc[2] * S + B.b[2] * E};
         const float* row[3];
-        for (int ax = 0; ax < 3; ++ax) row[ax] = brick_row(bix, D, B.big, nb, ax, B.b[ax]);
-        const float* xl = bix.xl + (i64)B.big * BR_LEVELS * 27;
+        for (int ax = 0; ax < 3; ++ax) row[ax] = brick_row(bix, D, B.root, nb, ax, B.b[ax]);
+        const float* xl = bix.xl + (i64)B.root * BR_LEVELS * 27;
         float lo = 0.f, hi = 0.f, amax = 0.f;
         int cnt = 0;
         // the leaf and its ancestors
@@ -825,7 +805,7 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             bool cross = false;
             for (int ax = 0; ax < 3; ++ax) {
                 bool c;
-                window_axis(g0[ax], Lc[ax], r, d, D, wlo[ax], ext[ax], c);
+                window_axis(g0[ax], E, Lc[ax], r, d, D, wlo[ax], ext[ax], c);
                 cross |= c;
             }
             if (!cross) continue;
@@ -872,8 +852,6 @@ struct BrickShared {
     int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
     int wext[BR_LEVELS][3];
     int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
-    int nforeign;
-    short foreign[3 * BR1 * BR1];             // lower-face corners owned by another leaf
 };
 __device__ __forceinline__ float bt_at(const BrickShared& sm, int ax, int d, int t, int k) {
     return sm.Bt[(ax * BR_LEVELS + d) * 36 + t * BR1 + k];
@@ -920,35 +898,31 @@ __device__ __forceinline__ float brick_corner(const BrickShared& sm, int D, int 
     return val;
 }
 
-__device__ __noinline__ float foreign_corner_value(const VArgs& v, int own, int r, const int oc[3], const int qc[3]) {
-    return virtual_corner_value(v, own, r, oc, qc);
-}
+// live brick: root, brick coordinates; first corner value and first cell
+struct LiveBrick {
+    int root;
+    int b[3];
+    i64 lat;
+    i64 cell;
+};
 
-// one block per live brick: exact corner values into the brick's 9^3 slot
-__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const int4* __restrict__ live,
-                                                         i64 nlive, float* __restrict__ blat) {
+// one block per live brick: exact corner values into the brick's (B+1)^3 slot;
+// corners owned by another leaf are listed for k_foreign_corners
+__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const LiveBrick* __restrict__ live,
+                                                         i64 nlive, float* __restrict__ blat,
+                                                         unsigned long long* __restrict__ nforeign,
+                                                         int2* __restrict__ foreign, i64 foreign_cap) {
     __shared__ BrickShared sm;
     const EvalArgs& a = v.e;
     const int D = a.D;
     for (i64 li = blockIdx.x; li < nlive; li += gridDim.x) {
-        const int4 ld = live[li];                  // root, brick coordinates
-        const VRoot R = v.roots[ld.x];
-        const int r = R.depth, S = 1 << (D - r), L = R.node, nb = S / BR;
-        const int bb[3] = {ld.y, ld.z, ld.w};
+        const LiveBrick lb = live[li];
+        const VRoot R = v.roots[lb.root];
+        const int r = R.depth, S = 1 << (D - r), L = R.node, E = brick_edge(D, r), nb = S / E, E1 = E + 1;
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
-        const int g0[3] = {Lc[0] * S + bb[0] * BR, Lc[1] * S + bb[1] * BR, Lc[2] * S + bb[2] * BR};
-        const bool fposs = brick_foreign_possible(v, R, bb);
-        // the large-root index of this root (for the tables)
-        int big = 0;
-        {
-            int lo = 0, hi = bix.nbig - 1;
-            while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                if (bix.big[mid] < ld.x) lo = mid + 1; else hi = mid;
-            }
-            big = lo;
-        }
+        const int g0[3] = {Lc[0] * S + lb.b[0] * E, Lc[1] * S + lb.b[1] * E, Lc[2] * S + lb.b[2] * E};
+        const bool fposs = brick_foreign_possible(v, R, lb.b, nb);
         __syncthreads();
         if (threadIdx.x == 0) {
             int off = 0;
@@ -956,7 +930,7 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
                 bool cross = false;
                 for (int ax = 0; ax < 3; ++ax) {
                     bool c;
-                    window_axis(g0[ax], Lc[ax], r, d, D, sm.wlo[d][ax], sm.wext[d][ax], c);
+                    window_axis(g0[ax], E, Lc[ax], r, d, D, sm.wlo[d][ax], sm.wext[d][ax], c);
                     cross |= c;
                 }
                 if (cross) {
@@ -966,13 +940,12 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
                     sm.woff[d] = -1;
                 }
             }
-            sm.nforeign = 0;
         }
         for (int e = threadIdx.x; e < 27 * (r + 1); e += blockDim.x)
-            sm.xL[e] = bix.xl[(i64)big * BR_LEVELS * 27 + e];
+            sm.xL[e] = bix.xl[(i64)lb.root * BR_LEVELS * 27 + e];
         for (int e = threadIdx.x; e < 3 * 36 * (D + 1); e += blockDim.x) {
             const int ax = e / (36 * (D + 1)), q = e % (36 * (D + 1));
-            sm.Bt[ax * BR_LEVELS * 36 + q] = brick_row(bix, D, big, nb, ax, bb[ax])[ROW_BT * (D + 1) + q];
+            sm.Bt[ax * BR_LEVELS * 36 + q] = brick_row(bix, D, lb.root, nb, ax, lb.b[ax])[ROW_BT * (D + 1) + q];
         }
         __syncthreads();
         for (int d = r + 1; d <= D; ++d) {
@@ -986,41 +959,71 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
             }
         }
         __syncthreads();
-        float* out = blat + li * BR_CORNERS;
-        for (int e = threadIdx.x; e < BR_CORNERS; e += blockDim.x) {
-            const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
-            const int uu = bb[0] * BR + kk[0], ww = bb[1] * BR + kk[1], zz = bb[2] * BR + kk[2];
-            const int qc[3] = {Lc[0] * S + uu, Lc[1] * S + ww, Lc[2] * S + zz};
+        float* out = blat + lb.lat;
+        const int ncorner = E1 * E1 * E1;
+        for (int e = threadIdx.x; e < ncorner; e += blockDim.x) {
+            const int kk[3] = {e / (E1 * E1), (e / E1) % E1, e % E1};
+            const int uu = lb.b[0] * E + kk[0], ww = lb.b[1] * E + kk[1], zz = lb.b[2] * E + kk[2];
             const int sft[3] = {uu == 0, ww == 0, zz == 0};
+            const int qc[3] = {g0[0] + kk[0], g0[1] + kk[1], g0[2] + kk[2]};
             const int oc[3] = {qc[0] - 1 + sft[0], qc[1] - 1 + sft[1], qc[2] - 1 + sft[2]};
             if (fposs && (sft[0] | sft[1] | sft[2])) {
                 int o2[3];
                 if (lower_face_owner(v, R, Lc, qc, o2) != L) {
-                    sm.foreign[atomicAdd(&sm.nforeign, 1)] = (short)e;
+                    const unsigned long long f = atomicAdd(nforeign, 1ull);
+                    if ((i64)f < foreign_cap) foreign[f] = make_int2((int)li, e);
                     continue;
                 }
             }
             out[e] = brick_corner(sm, D, r, oc, kk, sft) - v.iso;
         }
-        __syncthreads();
-        for (int f = threadIdx.x; f < sm.nforeign; f += blockDim.x) {
-            const int e = sm.foreign[f];
-            const int kk[3] = {e / (BR1 * BR1), (e / BR1) % BR1, e % BR1};
-            const int qc[3] = {Lc[0] * S + bb[0] * BR + kk[0], Lc[1] * S + bb[1] * BR + kk[1], Lc[2] * S + bb[2] * BR + kk[2]};
-            int oc[3] = {0, 0, 0};
-            const int own = lower_face_owner(v, R, Lc, qc, oc);
-            out[e] = foreign_corner_value(v, own, r, oc, qc) - v.iso;
-        }
     }
 }
 
-// live bricks in brick order: root and brick coordinates
+// corners on a leaf's lower faces owned by another leaf of the batch
+__global__ void k_foreign_corners(VArgs v, const LiveBrick* __restrict__ live, const int2* __restrict__ foreign,
+                                  i64 n, float* __restrict__ blat) {
+    const int D = v.e.D;
+    for (i64 f = (i64)blockIdx.x * blockDim.x + threadIdx.x; f < n; f += (i64)gridDim.x * blockDim.x) {
+        const int2 fe = foreign[f];
+        const LiveBrick lb = live[fe.x];
+        const VRoot R = v.roots[lb.root];
+        const int r = R.depth, S = 1 << (D - r), E = brick_edge(D, r), E1 = E + 1;
+        int Lc[3];
+        key_coords(v.e.nd.key[R.node], r, D, Lc);
+        const int e = fe.y;
+        const int qc[3] = {Lc[0] * S + lb.b[0] * E + e / (E1 * E1), Lc[1] * S + lb.b[1] * E + (e / E1) % E1,
+                           Lc[2] * S + lb.b[2] * E + e % E1};
+        int oc[3] = {0, 0, 0};
+        const int own = lower_face_owner(v, R, Lc, qc, oc);
+        blat[lb.lat + e] = virtual_corner_value(v, own, r, oc, qc) - v.iso;
+    }
+}
+
+// live bricks in brick order
 __global__ void k_live_bricks(VArgs v, BrickIndex bix, const unsigned char* __restrict__ culled,
-                              const int* __restrict__ pos, i64 nbricks, int4* __restrict__ live) {
+                              const int* __restrict__ pos, i64 nbricks, LiveBrick* __restrict__ live,
+                              i64* __restrict__ lat_size, i64* __restrict__ cell_size) {
     for (i64 bi = (i64)blockIdx.x * blockDim.x + threadIdx.x; bi < nbricks; bi += (i64)gridDim.x * blockDim.x) {
         if (culled[bi]) continue;
         const VBrick B = brick_of(v, bix, bi);
-        live[pos[bi]] = make_int4(B.root, B.b[0], B.b[1], B.b[2]);
+        const int E = brick_edge(v.e.D, v.roots[B.root].depth);
+        const int p = pos[bi];
+        LiveBrick lb;
+        lb.root = B.root;
+        lb.b[0] = B.b[0]; lb.b[1] = B.b[1]; lb.b[2] = B.b[2];
+        lb.lat = 0;
+        lb.cell = 0;
+        live[p] = lb;
+        lat_size[p] = (i64)(E + 1) * (E + 1) * (E + 1);
+        cell_size[p] = (i64)E * E * E;
+    }
+}
+__global__ void k_live_offsets(LiveBrick* __restrict__ live, const i64* __restrict__ lat_pos,
+                               const i64* __restrict__ cell_pos, i64 n) {
+    for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        live[k].lat = lat_pos[k];
+        live[k].cell = cell_pos[k];
     }
 }
 __global__ void k_live_flags(const unsigned char* __restrict__ culled, i64 n, int* __restrict__ f) {
@@ -1028,50 +1031,31 @@ __global__ void k_live_flags(const unsigned char* __restrict__ culled, i64 n, in
         f[k] = culled[k] ? 0 : 1;
 }
 
-// ---- virtual cells: the small leaves' lattices, then the live bricks
+// ---- virtual cells: the cells of the live bricks
 struct VirtCells {
-    const int* small;              // root indices of the small leaves
-    const i64* small_cells;        // first cell of each small leaf
-    const i64* small_lat;          // first corner of each small leaf
-    int nsmall;
-    i64 cells_small;               // cells of all small leaves
-    const float* lat_small;        // corner values (minus iso) of the small leaves
-    const int4* live;              // live bricks: root, brick coordinates
-    const float* lat_brick;        // 9^3 corner values (minus iso) per live brick
+    const LiveBrick* live;
+    i64 nlive;
+    const float* lat;              // corner values (minus iso) of the live bricks
 };
 
 // root, cell coordinates in the root's lattice and the 8 corner values of virtual cell e
 __device__ __forceinline__ int virt_cell(const VirtCells& vc, const VArgs& v, i64 e, int cu[3], float cv[8]) {
-    const int D = v.e.D;
-    if (e < vc.cells_small) {
-        int lo = 0, hi = vc.nsmall - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (vc.small_cells[mid] <= e) lo = mid; else hi = mid - 1;
-        }
-        const int root = vc.small[lo];
-        const int S = 1 << (D - v.roots[root].depth), S1 = S + 1;
-        const i64 loc = e - vc.small_cells[lo];
-        cu[0] = (int)(loc / ((i64)S * S));
-        cu[1] = (int)((loc / S) % S);
-        cu[2] = (int)(loc % S);
-        const float* L = vc.lat_small + vc.small_lat[lo];
-        for (int kind = 0; kind < 8; ++kind)
-            cv[kind] = L[((i64)(cu[0] + (kind & 1)) * S1 + (cu[1] + ((kind >> 1) & 1))) * S1 + (cu[2] + ((kind >> 2) & 1))];
-        return root;
+    i64 lo = 0, hi = vc.nlive - 1;
+    while (lo < hi) {
+        const i64 mid = (lo + hi + 1) >> 1;
+        if (vc.live[mid].cell <= e) lo = mid; else hi = mid - 1;
     }
-    const i64 be = e - vc.cells_small;
-    const i64 li = be / BR_CELLS;
-    const int loc = (int)(be % BR_CELLS);
-    const int l3[3] = {loc / (BR * BR), (loc / BR) % BR, loc % BR};
-    const int4 ld = vc.live[li];
-    cu[0] = ld.y * BR + l3[0];
-    cu[1] = ld.z * BR + l3[1];
-    cu[2] = ld.w * BR + l3[2];
-    const float* L = vc.lat_brick + li * BR_CORNERS;
+    const LiveBrick lb = vc.live[lo];
+    const int E = brick_edge(v.e.D, v.roots[lb.root].depth), E1 = E + 1;
+    const int loc = (int)(e - lb.cell);
+    const int l3[3] = {loc / (E * E), (loc / E) % E, loc % E};
+    cu[0] = lb.b[0] * E + l3[0];
+    cu[1] = lb.b[1] * E + l3[1];
+    cu[2] = lb.b[2] * E + l3[2];
+    const float* L = vc.lat + lb.lat;
     for (int kind = 0; kind < 8; ++kind)
-        cv[kind] = L[((l3[0] + (kind & 1)) * BR1 + (l3[1] + ((kind >> 1) & 1))) * BR1 + (l3[2] + ((kind >> 2) & 1))];
-    return ld.x;
+        cv[kind] = L[((l3[0] + (kind & 1)) * E1 + (l3[1] + ((kind >> 1) & 1))) * E1 + (l3[2] + ((kind >> 2) & 1))];
+    return lb.root;
 }
 
 __global__ void k_virtual_cells(VArgs v, VirtCells vc, i64 total, unsigned char* __restrict__ cat,
@@ -1400,20 +1384,19 @@ void stage_mesh(Ctx& c) {
     const i64 ntri_real = read_scalar(tri_real + nact_real, s);
     dfree(flags, s);
     dfree(fpos, s);
-    // ---- virtual cells: small leaves (lattice edge <= 8) one thread per corner,
-    // large leaves in bricks of 8^3 cells, bounded and culled before evaluation
+    // ---- virtual cells: every subdivided leaf cut into bricks, bounded and culled
+    // before evaluation
     i64 ntri_virt = 0, nact_virt = 0, total_cells = 0;
     c.total_bricks = 0;
     c.live_bricks = 0;
+    c.foreign_corners = 0;
     VRoot* droots = nullptr;
     i64 *act_virt = nullptr, *tri_virt = nullptr;
     unsigned char* vcat = nullptr;
     int* vntri = nullptr;
     int* bflag = nullptr;
-    int* d_small = nullptr;
-    i64 *d_small_cells = nullptr, *d_small_lat = nullptr;
-    float *lat_small = nullptr, *lat_brick = nullptr;
-    int4* live = nullptr;
+    float* lat_brick = nullptr;
+    LiveBrick* live = nullptr;
     VArgs va;
     va.e = ea;
     va.iso = c.iso;
@@ -1428,112 +1411,107 @@ void stage_mesh(Ctx& c) {
         CK(cudaMemcpyAsync(bflag, bflag_host.data(), M * sizeof(int), cudaMemcpyHostToDevice, s));
         va.roots = droots;
         va.batch_root_flag = bflag;
-        std::vector<int> small_list, big_list;
-        std::vector<i64> small_lat, small_cells, brick_prefix, row_prefix;
+        const int nr = (int)roots.size();
+        std::vector<i64> brick_prefix(nr), row_prefix(nr);
         std::vector<int4> rowdesc;
-        i64 lat_total = 0, cells_small = 0, nbricks = 0;
-        for (size_t k = 0; k < roots.size(); ++k) {
-            const int S = 1 << (D - roots[k].depth);
-            if (S <= BR) {
-                small_list.push_back((int)k);
-                small_lat.push_back(lat_total);
-                small_cells.push_back(cells_small);
-                lat_total += (i64)(S + 1) * (S + 1) * (S + 1);
-                cells_small += (i64)S * S * S;
-            } else {
-                const int nb = S / BR;
-                big_list.push_back((int)k);
-                brick_prefix.push_back(nbricks);
-                row_prefix.push_back((i64)rowdesc.size());
-                nbricks += (i64)nb * nb * nb;
-                for (int ax = 0; ax < 3; ++ax)
-                    for (int b = 0; b < nb; ++b) rowdesc.push_back(make_int4((int)k, ax, b, 0));
+        i64 nbricks = 0;
+        for (int k = 0; k < nr; ++k) {
+            const int S = 1 << (D - roots[k].depth), E = std::min(S, BR), nbk = S / E;
+            brick_prefix[k] = nbricks;
+            row_prefix[k] = (i64)rowdesc.size();
+            nbricks += (i64)nbk * nbk * nbk;
+            for (int ax = 0; ax < 3; ++ax)
+                for (int b = 0; b < nbk; ++b) rowdesc.push_back(make_int4(k, ax, b, 0));
+        }
+        const i64 nrows = (i64)rowdesc.size();
+        i64* dbpre = dalloc<i64>(nr, s);
+        i64* drpre = dalloc<i64>(nr, s);
+        int4* drd = dalloc<int4>(nrows, s);
+        float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
+        float* xl = dalloc<float>((i64)nr * BR_LEVELS * 27, s);
+        CK(cudaMemcpyAsync(dbpre, brick_prefix.data(), nr * sizeof(i64), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(drpre, row_prefix.data(), nr * sizeof(i64), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(drd, rowdesc.data(), nrows * sizeof(int4), cudaMemcpyHostToDevice, s));
+        BrickIndex bix{dbpre, drpre, nr, rows, xl};
+        const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
+        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drd, nrows, rows);
+        CK_LAUNCH();
+        k_brick_xl<<<grid_for((i64)nr * BR_LEVELS * 27, 256), 256, 0, s>>>(va, nr, xl);
+        CK_LAUNCH();
+        c.kend(kr);
+        unsigned char* culled = dalloc<unsigned char>(nbricks, s);
+        // compulsory: each brick's three rows and its culled flag
+        const int kb = c.kbegin("brick_bound", (double)nbricks * (3.0 * 33 * (D + 1) * 4 + 1));
+        k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks, culled);
+        CK_LAUNCH();
+        c.kend(kb);
+        int* bf = dalloc<int>(nbricks, s);
+        int* bp = dalloc<int>(nbricks + 1, s);
+        k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
+        CK_LAUNCH();
+        exclusive_scan<int, int>(bf, bp, nbricks, bp + nbricks, s);
+        const i64 nlive = read_scalar(bp + nbricks, s);
+        c.total_bricks = nbricks;
+        c.live_bricks = nlive;
+        if (nlive > 0) {
+            live = dalloc<LiveBrick>(nlive, s);
+            i64* lsz = dalloc<i64>(nlive, s);
+            i64* csz = dalloc<i64>(nlive, s);
+            i64* lpos = dalloc<i64>(nlive + 1, s);
+            i64* cpos = dalloc<i64>(nlive + 1, s);
+            k_live_bricks<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, culled, bp, nbricks, live, lsz, csz);
+            CK_LAUNCH();
+            exclusive_scan<i64, i64>(lsz, lpos, nlive, lpos + nlive, s);
+            exclusive_scan<i64, i64>(csz, cpos, nlive, cpos + nlive, s);
+            k_live_offsets<<<grid_for(nlive, 256), 256, 0, s>>>(live, lpos, cpos, nlive);
+            CK_LAUNCH();
+            const i64 lat_total = read_scalar(lpos + nlive, s);
+            total_cells = read_scalar(cpos + nlive, s);
+            lat_brick = dalloc<float>(lat_total, s);
+            // corners owned by another leaf: at most the lower-face corners of the live bricks
+            const i64 fcap = std::min<i64>(lat_total, nlive * (BR_CORNERS - BR * BR * BR));
+            int2* foreign = dalloc<int2>(std::max<i64>(fcap, 1), s);
+            unsigned long long* nfor = dalloc<unsigned long long>(1, s);
+            CK(cudaMemsetAsync(nfor, 0, sizeof(unsigned long long), s));
+            const int ke = c.kbegin("brick_eval", (double)lat_total * 4);
+            k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_brick,
+                                                                                  nfor, foreign, fcap);
+            CK_LAUNCH();
+            c.kend(ke);
+            const i64 nf = (i64)read_scalar(nfor, s);
+            if (nf > fcap) {
+                set_last_error("foreign corner list overflow (%lld > %lld)", (long long)nf, (long long)fcap);
+                throw Error{PRGPU_ERR_LIMIT, {0}};
             }
-        }
-        vc.nsmall = (int)small_list.size();
-        vc.cells_small = cells_small;
-        if (!small_list.empty()) {
-            d_small = dalloc<int>((i64)small_list.size(), s);
-            d_small_cells = dalloc<i64>((i64)small_list.size(), s);
-            d_small_lat = dalloc<i64>((i64)small_list.size(), s);
-            lat_small = dalloc<float>(lat_total, s);
-            CK(cudaMemcpyAsync(d_small, small_list.data(), small_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(d_small_cells, small_cells.data(), small_cells.size() * sizeof(i64),
-                               cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(d_small_lat, small_lat.data(), small_lat.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
-            const int kvs = c.kbegin("virtual_small", (double)lat_total * 4);
-            k_virtual_corners<<<grid_for(lat_total, 128, 1ll << 30), 128, 0, s>>>(
-                va, d_small, d_small_lat, (int)small_list.size(), lat_total, lat_small);
-            CK_LAUNCH();
-            c.kend(kvs);
-        }
-        vc.small = d_small;
-        vc.small_cells = d_small_cells;
-        vc.small_lat = d_small_lat;
-        vc.lat_small = lat_small;
-        i64 nlive = 0;
-        if (nbricks > 0) {
-            const i64 nrows = (i64)rowdesc.size();
-            int* dbig = dalloc<int>((i64)big_list.size(), s);
-            i64* dbpre = dalloc<i64>((i64)brick_prefix.size(), s);
-            i64* drpre = dalloc<i64>((i64)row_prefix.size(), s);
-            int4* drd = dalloc<int4>(nrows, s);
-            float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
-            float* xl = dalloc<float>((i64)big_list.size() * BR_LEVELS * 27, s);
-            CK(cudaMemcpyAsync(dbig, big_list.data(), big_list.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(dbpre, brick_prefix.data(), brick_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(drpre, row_prefix.data(), row_prefix.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
-            CK(cudaMemcpyAsync(drd, rowdesc.data(), nrows * sizeof(int4), cudaMemcpyHostToDevice, s));
-            BrickIndex bix{dbig, dbpre, drpre, (int)big_list.size(), rows, xl};
-            const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
-            k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drd, nrows, rows);
-            CK_LAUNCH();
-            k_brick_xl<<<grid_for((i64)big_list.size() * BR_LEVELS * 27, 256), 256, 0, s>>>(
-                va, dbig, (int)big_list.size(), xl);
-            CK_LAUNCH();
-            c.kend(kr);
-            unsigned char* culled = dalloc<unsigned char>(nbricks, s);
-            // compulsory: each brick's three rows and its culled flag
-            const int kb = c.kbegin("brick_bound", (double)nbricks * (3.0 * 33 * (D + 1) * 4 + 1));
-            k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks,
-                                                                                                culled);
-            CK_LAUNCH();
-            c.kend(kb);
-            int* bf = dalloc<int>(nbricks, s);
-            int* bp = dalloc<int>(nbricks + 1, s);
-            k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
-            CK_LAUNCH();
-            exclusive_scan<int, int>(bf, bp, nbricks, bp + nbricks, s);
-            nlive = read_scalar(bp + nbricks, s);
-            c.total_bricks = nbricks;
-            c.live_bricks = nlive;
-            if (nlive > 0) {
-                live = dalloc<int4>(nlive, s);
-                k_live_bricks<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, culled, bp, nbricks, live);
+            c.foreign_corners = nf;
+            if (nf > 0) {
+                const int kf = c.kbegin("foreign_corners", (double)nf * 4);
+                k_foreign_corners<<<grid_for(nf, 128, 1ll << 30), 128, 0, s>>>(va, live, foreign, nf, lat_brick);
                 CK_LAUNCH();
-                lat_brick = dalloc<float>(nlive * BR_CORNERS, s);
-                const int ke = c.kbegin("brick_eval", (double)nlive * BR_CORNERS * 4);
-                k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_brick);
-                CK_LAUNCH();
-                c.kend(ke);
+                c.kend(kf);
             }
-            dfree(bf, s);
-            dfree(bp, s);
-            dfree(culled, s);
-            dfree(dbig, s);
-            dfree(dbpre, s);
-            dfree(drpre, s);
-            dfree(drd, s);
-            dfree(rows, s);
-            dfree(xl, s);
+            dfree(foreign, s);
+            dfree(nfor, s);
+            dfree(lsz, s);
+            dfree(csz, s);
+            dfree(lpos, s);
+            dfree(cpos, s);
         }
+        dfree(bf, s);
+        dfree(bp, s);
+        dfree(culled, s);
+        dfree(dbpre, s);
+        dfree(drpre, s);
+        dfree(drd, s);
+        dfree(rows, s);
+        dfree(xl, s);
         vc.live = live;
-        vc.lat_brick = lat_brick;
-        total_cells = cells_small + nlive * BR_CELLS;
+        vc.nlive = nlive;
+        vc.lat = lat_brick;
         if (total_cells > 0) {
             vcat = dalloc<unsigned char>(total_cells, s);
             vntri = dalloc<int>(total_cells, s);
-            const int kc2 = c.kbegin("virtual_cells", (double)(lat_total + nlive * BR_CORNERS) * 4 + (double)total_cells * 5);
+            const int kc2 = c.kbegin("virtual_cells", (double)total_cells * (8 * 4 + 5));
             k_virtual_cells<<<grid_for(total_cells, 256, 1ll << 30), 256, 0, s>>>(va, vc, total_cells, vcat, vntri);
             CK_LAUNCH();
             c.kend(kc2);
@@ -1631,8 +1609,7 @@ void stage_mesh(Ctx& c) {
     dfree(tri_real, s);
     dfree(droots, s); dfree(act_virt, s); dfree(tri_virt, s);
     dfree(vcat, s); dfree(vntri, s); dfree(bflag, s);
-    dfree(d_small, s); dfree(d_small_cells, s); dfree(d_small_lat, s);
-    dfree(lat_small, s); dfree(lat_brick, s); dfree(live, s);
+    dfree(lat_brick, s); dfree(live, s);
     dfree(cell_v, s);
     dfree(x27, s);
     dfree(lb, s);

@@ -198,15 +198,21 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                 loc += (double)(pi * o);
             }
         } else {
+            // one warp per tile of 4 groups (32 rows); warps run their tiles independently
             const i64 gfirst = (dp.lo - 1) >> 3, ng = dp.n >> 3;
-            const int ch = threadIdx.x & 7, gl = threadIdx.x >> 3;
+            const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+            const int ch = lane & 7, gl = lane >> 3;
             const int sx = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
-            for (i64 tile = rank; tile * CG_TILE_GROUPS < ng; tile += dp.nblocks) {
-                __syncthreads();
+            float* wsp = sp + wib * (4 * 64);
+            const i64 wstride = (i64)dp.nblocks * (CG_BLOCK / 32);
+            for (i64 tile = (i64)rank * (CG_BLOCK / 32) + wib; tile * 4 < ng; tile += wstride) {
+                __syncwarp();
                 // the 4x4x4 block of each group: cell (bx,by,bz) is child ((bx+1)&1, ...) of the
                 // parent's neighbour ((bx+1)>>1, ...) in 0..2 per axis
-                for (int e = threadIdx.x; e < CG_TILE_GROUPS * 64; e += CG_BLOCK) {
-                    const i64 g = tile * CG_TILE_GROUPS + (e >> 6);
+#pragma unroll
+                for (int m = 0; m < 8; ++m) {
+                    const int e = lane + 32 * m;
+                    const i64 g = tile * 4 + (e >> 6);
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
                     float pv = 0.f;
                     if (g < ng) {
@@ -214,12 +220,12 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                         const int cn = a.gn[(i64)jp * a.ngroups + gfirst + g];
                         if (cn != -1) pv = pdir(cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)));
                     }
-                    sp[e] = pv;
+                    wsp[e] = pv;
                 }
-                __syncthreads();
-                const i64 g = tile * CG_TILE_GROUPS + gl;
+                __syncwarp();
+                const i64 g = tile * 4 + gl;
                 if (g < ng) {
-                    const float* blk = sp + gl * 64;
+                    const float* blk = wsp + gl * 64;
                     float o = 0.f;
 #pragma unroll
                     for (int j = 0; j < 27; ++j)
