@@ -542,9 +542,13 @@ __device__ __forceinline__ u64 cell_key_D(const int c[3], int D) { return coords
 //     corners are never read.
 // The surviving ("live") bricks are evaluated exactly, in the order of
 // virtual_corner_value, so culling changes no value.  Corners on the leaf's
-// lower faces may be owned by a cell of another leaf of the same depth batch:
-// those go through virtual_corner_value (k_foreign_corners), and a brick with
-// such a corner is never culled.
+// lower faces may be owned by a cell of another leaf of the same depth batch
+// ("foreign" corners): their virtual depths read the same window (a real node
+// is the same node in either leaf's frame, and every cell inside either leaf
+// reads 0), their real ancestors are the owner's.  Such a corner is a corner
+// of the owner leaf's brick that contains its owner cell, where the owner's own
+// bound covers it; so a brick with foreign corners is culled only when its own
+// bound and those of the owner bricks prove the same sign.
 //
 // Everything a brick needs along one axis depends only on the leaf, the axis
 // and the brick's index along it (a "brick row"), so it is tabulated once per
@@ -561,12 +565,13 @@ constexpr int BR1 = BR + 1;
 constexpr int BR_CORNERS = BR1 * BR1 * BR1;
 constexpr int BR_BLOCK = 128;
 constexpr int BR_LEVELS = 16;      // depths 0..15
-constexpr int BR_WEXT = BR + 3;    // window edge at the finest depth
+constexpr int BR_WEXT = BR + 4;    // window edge at the finest depth, with the extra upper cell
 // window cells over all virtual depths of a brick whose first corner is a
-// multiple of its edge B <= 8: at most 11^3 + 7^3 + 5^3 + 12 * 4^3 = 2567
-constexpr int BR_XW = 2600;
-// brick-row table: BT (36 per depth), RA (6 per depth), RW (22 per depth)
-constexpr int ROW_BT = 0, ROW_RA = 36, ROW_RW = 42, ROW_PER_DEPTH = 64;
+// multiple of its edge B <= 8, with the extra upper cell per axis (bricks
+// with foreign corners): at most 12^3 + 8^3 + 6^3 + 12 * 5^3 = 3956
+constexpr int BR_XW = 3968;
+// brick-row table: BT (36 per depth), RA (6 per depth), RW (24 per depth)
+constexpr int ROW_BT = 0, ROW_RA = 36, ROW_RW = 42, ROW_PER_DEPTH = 66;
 
 __device__ __forceinline__ int brick_edge(int D, int r) { return min(1 << (D - r), BR); }
 
@@ -654,16 +659,17 @@ __device__ __forceinline__ bool brick_foreign_possible(const VArgs& v, const VRo
 }
 
 // window of depth d around a brick (edge B) along one axis: origin and extent
-// of the cells the brick's owner cells can reach; 'cross' when that reaches
-// outside the leaf
-__device__ __forceinline__ void window_axis(int g0, int B, int Lc_ax, int r, int d, int D, int& wlo, int& ext,
-                                            bool& cross) {
+// of the cells the brick's owner cells can reach (one more upper cell when
+// 'extra': owner cells of foreign corners on the leaf's upper faces); 'cross'
+// when that reaches outside the leaf
+__device__ __forceinline__ void window_axis(int g0, int B, int Lc_ax, int r, int d, int D, int extra, int& wlo,
+                                            int& ext, bool& cross) {
     const int sh = D - d, span = 1 << (d - r);
     const int Vlo = (g0 - 1) >> sh, Vhi = (g0 + B - 1) >> sh;
     const int llo = Lc_ax * span;
     cross = (Vlo - 1 < llo || Vhi + 1 >= llo + span);
     wlo = Vlo - 1;
-    ext = Vhi - Vlo + 3;
+    ext = Vhi - Vlo + 3 + extra;
 }
 
 // one thread per (brick row, depth)
@@ -702,7 +708,7 @@ __global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrow
         } else {
             int wlo, ext;
             bool cross;
-            window_axis(g0, B, Lc[ax], r, d, D, wlo, ext, cross);
+            window_axis(g0, B, Lc[ax], r, d, D, 0, wlo, ext, cross);
             const int sh = D - d, lim = 1 << d;
             for (int n = 0; n < BR_WEXT; ++n) {
                 const int N = wlo + n;
@@ -756,10 +762,11 @@ __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, 
     return own;
 }
 
-// one warp per brick: the bound, and the culled flag
+// one warp per brick: the bound over the corners the brick's leaf owns;
+// sign[bi] = 1 (all above iso), -1 (all below) or 0 (not proven)
 constexpr int BB_BLOCK = 256;
 __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bix, i64 nbricks,
-                                                          unsigned char* __restrict__ culled) {
+                                                          signed char* __restrict__ sign) {
     const EvalArgs& a = v.e;
     const int D = a.D;
     const int lane = threadIdx.x & 31;
@@ -769,10 +776,6 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
     for (i64 bi = warp; bi < nbricks; bi += nwarps) {
         const VBrick B = brick_of(v, bix, bi);
         const VRoot R = v.roots[B.root];
-        if (brick_foreign_possible(v, R, B.b, (1 << (D - R.depth)) / brick_edge(D, R.depth))) {   // never culled
-            if (lane == 0) culled[bi] = 0;
-            continue;
-        }
         const int r = R.depth, S = 1 << (D - r), L = R.node, E = brick_edge(D, r), nb = S / E;
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
@@ -805,7 +808,7 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             bool cross = false;
             for (int ax = 0; ax < 3; ++ax) {
                 bool c;
-                window_axis(g0[ax], E, Lc[ax], r, d, D, wlo[ax], ext[ax], c);
+                window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wlo[ax], ext[ax], c);
                 cross |= c;
             }
             if (!cross) continue;
@@ -840,9 +843,58 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             const double margin = (2.0 * cnt + 8.0) * u * A + 4.0 * u * (fabs((double)lo) + fabs((double)hi) + 2.0 * fabs(iso)) +
                                   1e-30;
             const bool above = (double)lo - margin > iso, below = (double)hi + margin < iso;
-            culled[bi] = (above || below) ? 1 : 0;
+            sign[bi] = above ? 1 : (below ? -1 : 0);
         }
     }
+}
+
+// culled: the brick's own bound is proven and, where some of its corners may be
+// owned by another leaf L' of the batch, every brick of L' that can hold such
+// an owner cell is proven with the same sign
+__global__ void k_brick_cull(VArgs v, BrickIndex bix, const int* __restrict__ root_of, const signed char* __restrict__ sign,
+                             i64 nbricks, unsigned char* __restrict__ culled) {
+    const int D = v.e.D;
+    const NodeArrays& nd = v.e.nd;
+    for (i64 bi = (i64)blockIdx.x * blockDim.x + threadIdx.x; bi < nbricks; bi += (i64)gridDim.x * blockDim.x) {
+        const int sg = sign[bi];
+        if (sg == 0) { culled[bi] = 0; continue; }
+        const VBrick B = brick_of(v, bix, bi);
+        const VRoot R = v.roots[B.root];
+        const int E = brick_edge(D, R.depth), nb = (1 << (D - R.depth)) / E;
+        bool ok = true;
+        if (R.depth >= 3 && !(B.b[0] && B.b[1] && B.b[2])) {
+            for (int j = 0; j < 27 && ok; ++j) {
+                const int off[3] = {j / 9 - 1, (j / 3) % 3 - 1, j % 3 - 1};
+                bool lower = false, allowed = true;
+                for (int ax = 0; ax < 3; ++ax) {
+                    if (off[ax] == -1) { lower = true; if (B.b[ax] != 0) allowed = false; }
+                    if (off[ax] == 1 && B.b[ax] != nb - 1) allowed = false;
+                }
+                if (!lower || !allowed) continue;
+                const int n = nd.neigh[(i64)j * nd.M + R.node];
+                if (n == -1 || v.batch_root_flag[n] != R.batch) continue;
+                const int k2 = root_of[n];
+                // bricks of the neighbour holding owner cells within one cell of this brick
+                int lo3[3], hi3[3];
+                for (int ax = 0; ax < 3; ++ax) {
+                    if (off[ax] == -1) { lo3[ax] = hi3[ax] = nb - 1; }
+                    else if (off[ax] == 1) { lo3[ax] = hi3[ax] = 0; }
+                    else { lo3[ax] = max(B.b[ax] - 1, 0); hi3[ax] = min(B.b[ax] + 1, nb - 1); }
+                }
+                for (int x = lo3[0]; x <= hi3[0] && ok; ++x)
+                    for (int y = lo3[1]; y <= hi3[1] && ok; ++y)
+                        for (int z = lo3[2]; z <= hi3[2] && ok; ++z)
+                            if (sign[bix.prefix[k2] + ((i64)x * nb + y) * nb + z] != sg) ok = false;
+            }
+        }
+        culled[bi] = ok ? 1 : 0;
+    }
+}
+
+// root index of each subdivided leaf's node (-1 elsewhere)
+__global__ void k_root_of(const VRoot* __restrict__ roots, int nroots, int* __restrict__ root_of) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nroots; k += gridDim.x * blockDim.x)
+        root_of[roots[k].node] = k;
 }
 
 struct BrickShared {
@@ -857,34 +909,44 @@ __device__ __forceinline__ float bt_at(const BrickShared& sm, int ax, int d, int
     return sm.Bt[(ax * BR_LEVELS + d) * 36 + t * BR1 + k];
 }
 
-// value of corner kk owned by the brick's leaf, from the shared window, in the
-// order of virtual_corner_value.  sft[ax] is 1 on the axes where the owner cell
-// is the corner's own cell (lower faces), 0 where it is the cell below.  Terms
-// that virtual_corner_value skips (levels whose 3x3x3 block lies inside the
-// leaf, cells inside the leaf, absent nodes) read 0 here, and adding a zero
-// product leaves the sum unchanged, so the value is the same.
-__device__ __forceinline__ float brick_corner(const BrickShared& sm, int D, int r, const int oc[3], const int kk[3],
-                                              const int sft[3]) {
+// virtual-depth part of the value of corner qc (brick-local kk) whose owner
+// cell is oc -- in the brick's leaf or, for a foreign corner, in the leaf of
+// the batch that owns it -- from the shared window, in the order of
+// virtual_corner_value.  At depth d the owner cell is oc >> sh, the tabulated
+// one (qc - 1) >> sh, so the basis row is taken t + ((oc >> sh) - ((qc-1) >> sh))
+// (0 or 1).  Terms that virtual_corner_value skips (levels whose 3x3x3 block
+// lies inside the owner's leaf, cells inside either leaf, absent nodes) read 0
+// here, and adding a zero product leaves the sum unchanged, so the value is the
+// same.
+__device__ __forceinline__ float brick_virtual(const BrickShared& sm, int D, int r, const int oc[3], const int qc[3],
+                                               const int kk[3]) {
     float val = 0.f;
     for (int d = D; d > r; --d) {
         const int off = sm.woff[d];
         if (off < 0) continue;
         const int sh = D - d;
+        const int V[3] = {oc[0] >> sh, oc[1] >> sh, oc[2] >> sh};
         float bv[3][3];
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax)
+        for (int ax = 0; ax < 3; ++ax) {
+            const int toff = V[ax] - ((qc[ax] - 1) >> sh);
 #pragma unroll
-            for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, d, t + sft[ax], kk[ax]);
+            for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, d, t + toff, kk[ax]);
+        }
         const int e1 = sm.wext[d][1], e2 = sm.wext[d][2];
-        const float* xw = sm.Xw + off + (((oc[0] >> sh) - 1 - sm.wlo[d][0]) * e1 + ((oc[1] >> sh) - 1 - sm.wlo[d][1])) * e2 +
-                          ((oc[2] >> sh) - 1 - sm.wlo[d][2]);
+        const float* xw = sm.Xw + off + ((V[0] - 1 - sm.wlo[d][0]) * e1 + (V[1] - 1 - sm.wlo[d][1])) * e2 +
+                          (V[2] - 1 - sm.wlo[d][2]);
 #pragma unroll
         for (int j = 0; j < 27; ++j) {
             const int jx = j / 9, jy = (j / 3) % 3, jz = j % 3;
             val = fmaf(xw[(jx * e1 + jy) * e2 + jz] * bv[0][jx] * bv[1][jy], bv[2][jz], val);
         }
     }
-    // the leaf itself and its real ancestors (walk_up with absent neighbours as 0)
+    return val;
+}
+
+// the brick's leaf itself and its real ancestors (walk_up with absent neighbours as 0)
+__device__ __forceinline__ float brick_leaf_levels(const BrickShared& sm, int r, const int kk[3], float val) {
     for (int l = r; l >= 0; --l) {
         const float* xs = sm.xL + 27 * l;
         float bv[3][3];
@@ -906,12 +968,10 @@ struct LiveBrick {
     i64 cell;
 };
 
-// one block per live brick: exact corner values into the brick's (B+1)^3 slot;
-// corners owned by another leaf are listed for k_foreign_corners
+// one block per live brick: exact corner values into the brick's (B+1)^3 slot
 __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const LiveBrick* __restrict__ live,
                                                          i64 nlive, float* __restrict__ blat,
-                                                         unsigned long long* __restrict__ nforeign,
-                                                         int2* __restrict__ foreign, i64 foreign_cap) {
+                                                         unsigned long long* __restrict__ nforeign) {
     __shared__ BrickShared sm;
     const EvalArgs& a = v.e;
     const int D = a.D;
@@ -930,7 +990,7 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
                 bool cross = false;
                 for (int ax = 0; ax < 3; ++ax) {
                     bool c;
-                    window_axis(g0[ax], E, Lc[ax], r, d, D, sm.wlo[d][ax], sm.wext[d][ax], c);
+                    window_axis(g0[ax], E, Lc[ax], r, d, D, fposs ? 1 : 0, sm.wlo[d][ax], sm.wext[d][ax], c);
                     cross |= c;
                 }
                 if (cross) {
@@ -964,39 +1024,20 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
         for (int e = threadIdx.x; e < ncorner; e += blockDim.x) {
             const int kk[3] = {e / (E1 * E1), (e / E1) % E1, e % E1};
             const int uu = lb.b[0] * E + kk[0], ww = lb.b[1] * E + kk[1], zz = lb.b[2] * E + kk[2];
-            const int sft[3] = {uu == 0, ww == 0, zz == 0};
             const int qc[3] = {g0[0] + kk[0], g0[1] + kk[1], g0[2] + kk[2]};
-            const int oc[3] = {qc[0] - 1 + sft[0], qc[1] - 1 + sft[1], qc[2] - 1 + sft[2]};
-            if (fposs && (sft[0] | sft[1] | sft[2])) {
-                int o2[3];
-                if (lower_face_owner(v, R, Lc, qc, o2) != L) {
-                    const unsigned long long f = atomicAdd(nforeign, 1ull);
-                    if ((i64)f < foreign_cap) foreign[f] = make_int2((int)li, e);
-                    continue;
-                }
+            // owner cell: the cell below the corner on every axis, except on the leaf's lower faces
+            int oc[3] = {qc[0] - 1 + (uu == 0), qc[1] - 1 + (ww == 0), qc[2] - 1 + (zz == 0)};
+            int own = L;
+            if (fposs && (uu == 0 || ww == 0 || zz == 0)) own = lower_face_owner(v, R, Lc, qc, oc);
+            float val = brick_virtual(sm, D, r, oc, qc, kk);
+            if (own == L) {
+                val = brick_leaf_levels(sm, r, kk, val);
+            } else {
+                atomicAdd(nforeign, 1ull);
+                val = walk_up_u(a, own, qc, val);
             }
-            out[e] = brick_corner(sm, D, r, oc, kk, sft) - v.iso;
+            out[e] = val - v.iso;
         }
-    }
-}
-
-// corners on a leaf's lower faces owned by another leaf of the batch
-__global__ void k_foreign_corners(VArgs v, const LiveBrick* __restrict__ live, const int2* __restrict__ foreign,
-                                  i64 n, float* __restrict__ blat) {
-    const int D = v.e.D;
-    for (i64 f = (i64)blockIdx.x * blockDim.x + threadIdx.x; f < n; f += (i64)gridDim.x * blockDim.x) {
-        const int2 fe = foreign[f];
-        const LiveBrick lb = live[fe.x];
-        const VRoot R = v.roots[lb.root];
-        const int r = R.depth, S = 1 << (D - r), E = brick_edge(D, r), E1 = E + 1;
-        int Lc[3];
-        key_coords(v.e.nd.key[R.node], r, D, Lc);
-        const int e = fe.y;
-        const int qc[3] = {Lc[0] * S + lb.b[0] * E + e / (E1 * E1), Lc[1] * S + lb.b[1] * E + (e / E1) % E1,
-                           Lc[2] * S + lb.b[2] * E + e % E1};
-        int oc[3] = {0, 0, 0};
-        const int own = lower_face_owner(v, R, Lc, qc, oc);
-        blat[lb.lat + e] = virtual_corner_value(v, own, r, oc, qc) - v.iso;
     }
 }
 
@@ -1440,11 +1481,20 @@ void stage_mesh(Ctx& c) {
         CK_LAUNCH();
         c.kend(kr);
         unsigned char* culled = dalloc<unsigned char>(nbricks, s);
+        signed char* bsign = dalloc<signed char>(nbricks, s);
+        int* root_of = dalloc<int>(nCoarse, s);
+        CK(cudaMemsetAsync(root_of, 0xff, nCoarse * sizeof(int), s));
+        k_root_of<<<grid_for(nr, 256), 256, 0, s>>>(droots, nr, root_of);
+        CK_LAUNCH();
         // compulsory: each brick's three rows and its culled flag
         const int kb = c.kbegin("brick_bound", (double)nbricks * (3.0 * 33 * (D + 1) * 4 + 1));
-        k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks, culled);
+        k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks, bsign);
+        CK_LAUNCH();
+        k_brick_cull<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, root_of, bsign, nbricks, culled);
         CK_LAUNCH();
         c.kend(kb);
+        dfree(bsign, s);
+        dfree(root_of, s);
         int* bf = dalloc<int>(nbricks, s);
         int* bp = dalloc<int>(nbricks + 1, s);
         k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
@@ -1468,29 +1518,14 @@ void stage_mesh(Ctx& c) {
             const i64 lat_total = read_scalar(lpos + nlive, s);
             total_cells = read_scalar(cpos + nlive, s);
             lat_brick = dalloc<float>(lat_total, s);
-            // corners owned by another leaf: at most the lower-face corners of the live bricks
-            const i64 fcap = std::min<i64>(lat_total, nlive * (BR_CORNERS - BR * BR * BR));
-            int2* foreign = dalloc<int2>(std::max<i64>(fcap, 1), s);
             unsigned long long* nfor = dalloc<unsigned long long>(1, s);
             CK(cudaMemsetAsync(nfor, 0, sizeof(unsigned long long), s));
             const int ke = c.kbegin("brick_eval", (double)lat_total * 4);
             k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_brick,
-                                                                                  nfor, foreign, fcap);
+                                                                                  nfor);
             CK_LAUNCH();
             c.kend(ke);
-            const i64 nf = (i64)read_scalar(nfor, s);
-            if (nf > fcap) {
-                set_last_error("foreign corner list overflow (%lld > %lld)", (long long)nf, (long long)fcap);
-                throw Error{PRGPU_ERR_LIMIT, {0}};
-            }
-            c.foreign_corners = nf;
-            if (nf > 0) {
-                const int kf = c.kbegin("foreign_corners", (double)nf * 4);
-                k_foreign_corners<<<grid_for(nf, 128, 1ll << 30), 128, 0, s>>>(va, live, foreign, nf, lat_brick);
-                CK_LAUNCH();
-                c.kend(kf);
-            }
-            dfree(foreign, s);
+            c.foreign_corners = (i64)read_scalar(nfor, s);
             dfree(nfor, s);
             dfree(lsz, s);
             dfree(csz, s);
