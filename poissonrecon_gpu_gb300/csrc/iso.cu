@@ -1486,8 +1486,10 @@ void stage_mesh(Ctx& c) {
         CK(cudaMemsetAsync(root_of, 0xff, nCoarse * sizeof(int), s));
         k_root_of<<<grid_for(nr, 256), 256, 0, s>>>(droots, nr, root_of);
         CK_LAUNCH();
-        // compulsory: each brick's three rows and its culled flag
-        const int kb = c.kbegin("brick_bound", (double)nbricks * (3.0 * 33 * (D + 1) * 4 + 1));
+        // compulsory: the range part of every brick row and the leaves' neighbour x once, the
+        // sign written and read, the culled flag written
+        const int kb = c.kbegin("brick_bound", (double)nrows * (6 + 2 * BR_WEXT) * (D + 1) * 4 +
+                                                   (double)nr * BR_LEVELS * 27 * 4 + (double)nbricks * 3);
         k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks, bsign);
         CK_LAUNCH();
         k_brick_cull<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, root_of, bsign, nbricks, culled);
