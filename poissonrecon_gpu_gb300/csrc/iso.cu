@@ -73,8 +73,12 @@ struct EvalArgs {
     const float* x27;      // nodes [0, nx27): x of the 27 neighbours (0: none), 28 floats per node; or null
     i64 nx27;
     const float* lb;       // basis values at finest-lattice points (see lattice_basis), or null
-    i64 lb_off[17];        // start of each depth in lb
 };
+
+// start of depth d in the lattice basis table: sum_{l<d} 2^l (3 2^(D-l) + 1) = 3 d 2^D + 2^d - 1
+__device__ __host__ __forceinline__ i64 lattice_basis_offset(int D, int d) {
+    return 3ll * d * (1ll << D) + (1ll << d) - 1;
+}
 
 // B_{d,n}(u / 2^D) for a finest-lattice coordinate u: the value cpoly_value
 // computes, read from the table when u lies in the support [(n-1)w, (n+2)w]
@@ -82,7 +86,7 @@ struct EvalArgs {
 __device__ __forceinline__ float lattice_basis(const EvalArgs& a, int d, int n, int u) {
     const int w = 1 << (a.D - d);
     const int k = u - (n - 1) * w;
-    if (a.lb && k >= 0 && k <= 3 * w) return a.lb[a.lb_off[d] + (i64)n * (3 * w + 1) + k];
+    if (a.lb && k >= 0 && k <= 3 * w) return a.lb[lattice_basis_offset(a.D, d) + (i64)n * (3 * w + 1) + k];
     return cpoly_value<3>(a.basis[(1 << d) - 1 + n], (float)u * (1.0f / (float)(1 << a.D)));
 }
 
@@ -243,7 +247,7 @@ void stage_points(Ctx& c) {
     double* sum = dalloc<double>(1, s);
     CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
     float* x27 = build_x27(c, c.base[c.D]);
-    EvalArgs a{c.nodes, c.D, c.basis, c.x, x27, x27 ? c.base[c.D] : 0, nullptr, {0}};
+    EvalArgs a{c.nodes, c.D, c.basis, c.x, x27, x27 ? c.base[c.D] : 0, nullptr};
     const int kt = c.kbegin("point_values", (double)c.N * (12 + 4 + 4) + (double)c.nodes.M * (4 + 4 + 8 + 108));
     k_point_values<<<grid_for(c.N, 128, 1ll << 30), 128, 0, s>>>(a, c.pts, c.point_node, c.N, c.point_value, sum);
     CK_LAUNCH();
@@ -550,16 +554,16 @@ __device__ __forceinline__ u64 cell_key_D(const int c[3], int D) { return coords
 // bound covers it; so a brick with foreign corners is culled only when its own
 // bound and those of the owner bricks prove the same sign.
 //
-// Everything a brick needs along one axis depends only on the leaf, the axis
-// and the brick's index along it (a "brick row"), so it is tabulated once per
-// row by k_brick_rows:
+// The basis values a brick's corners use along one axis depend only on the
+// leaf, the axis and the brick's index along it (a "brick row"):
 //   BT[d][t][k]   basis value at corner k of the function of cell V_k + t - 1
-//                 (depth d > r, V_k the owner cell of corner k, t = 0..3; t = 3
-//                 serves corners on the leaf's lower faces, whose owner cell is
-//                 V_k + 1) or of ancestor cell + t - 1 (depth d <= r)
+//                 (depth d > r, V_k = (corner - 1) >> (D - d), t = 0..3; t = 3
+//                 serves owner cells V_k + 1) or of ancestor cell + t - 1
+//                 (depth d <= r); built per live brick by k_brick_eval
 //   RA[l][t]      range over k of BT[l][t][k], l <= r
 //   RW[d][n]      range (with 0) of the depth-d function of window cell n over
 //                 the corners whose owner cell is within one cell of it
+// RA and RW are tabulated once per row by k_brick_rows for the bounds.
 constexpr int BR = 8;              // largest brick edge (cells); corners per axis up to BR+1
 constexpr int BR1 = BR + 1;
 constexpr int BR_CORNERS = BR1 * BR1 * BR1;
@@ -570,8 +574,8 @@ constexpr int BR_WEXT = BR + 4;    // window edge at the finest depth, with the 
 // multiple of its edge B <= 8, with the extra upper cell per axis (bricks
 // with foreign corners): at most 12^3 + 8^3 + 6^3 + 12 * 5^3 = 3956
 constexpr int BR_XW = 3968;
-// brick-row table: BT (36 per depth), RA (6 per depth), RW (24 per depth)
-constexpr int ROW_BT = 0, ROW_RA = 36, ROW_RW = 42, ROW_PER_DEPTH = 66;
+// brick-row table: RA (6 per depth), RW (24 per depth)
+constexpr int ROW_RA = 0, ROW_RW = 6, ROW_PER_DEPTH = 30;
 
 __device__ __forceinline__ int brick_edge(int D, int r) { return min(1 << (D - r), BR); }
 
@@ -579,7 +583,7 @@ struct BrickIndex {                // bricks of all subdivided leaves, numbered 
     const i64* prefix;             // first brick of each root
     const i64* row_prefix;         // first brick row of each root (3 * bricks per edge rows each)
     int nroots;
-    const float* rows;             // brick-row tables, 64 (D+1) floats each
+    const float* rows;             // brick-row tables, 30 (D+1) floats each
     const float* xl;               // per root: x of the 27 neighbours of each ancestor, 16 x 27
 };
 struct VBrick {
@@ -672,6 +676,56 @@ __device__ __forceinline__ void window_axis(int g0, int B, int Lc_ax, int r, int
     ext = Vhi - Vlo + 3 + extra;
 }
 
+// BT[d][t][k] of the brick row starting at corner g0 (see above).  Every entry a
+// corner reads lies in its function's support [(n-1)w, (n+2)w] (the corner is
+// in the closure of the owner cell n - t + 1; for t = 3 at the support's left
+// end), so entries outside it -- never read -- are left 0.
+__device__ __forceinline__ float brick_bt(const EvalArgs& a, int r, int Lc_ax, int g0, int d, int t, int k) {
+    const int n = (d <= r) ? (Lc_ax >> (r - d)) + t - 1 : ((g0 + k - 1) >> (a.D - d)) + t - 1;
+    if (n < 0 || n >= (1 << d)) return 0.f;
+    const int w = 1 << (a.D - d);
+    const int kk = g0 + k - (n - 1) * w;
+    if (kk < 0 || kk > 3 * w) return 0.f;
+    return a.lb[lattice_basis_offset(a.D, d) + (i64)n * (3 * w + 1) + kk];
+}
+
+// the part of a window box [wlo, wlo+ext) outside the leaf's box [llo, llo+span)
+// (per axis, at one depth) as at most 6 disjoint boxes
+struct Box3 {
+    int lo[3];
+    int n[3];
+};
+__device__ __forceinline__ int outside_boxes(const int wlo[3], const int ext[3], const int llo[3], int span,
+                                             Box3 out[6]) {
+    int lo[3] = {wlo[0], wlo[1], wlo[2]}, hi[3] = {wlo[0] + ext[0], wlo[1] + ext[1], wlo[2] + ext[2]};
+    int nb = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        const int a = max(lo[ax], llo[ax]), b = min(hi[ax], llo[ax] + span);
+        if (a >= b) {   // no overlap along this axis: the rest is outside
+            Box3 bx;
+            for (int q = 0; q < 3; ++q) { bx.lo[q] = lo[q]; bx.n[q] = hi[q] - lo[q]; }
+            out[nb++] = bx;
+            return nb;
+        }
+        if (lo[ax] < a) {
+            Box3 bx;
+            for (int q = 0; q < 3; ++q) { bx.lo[q] = lo[q]; bx.n[q] = hi[q] - lo[q]; }
+            bx.n[ax] = a - lo[ax];
+            out[nb++] = bx;
+        }
+        if (b < hi[ax]) {
+            Box3 bx;
+            for (int q = 0; q < 3; ++q) { bx.lo[q] = lo[q]; bx.n[q] = hi[q] - lo[q]; }
+            bx.lo[ax] = b;
+            bx.n[ax] = hi[ax] - b;
+            out[nb++] = bx;
+        }
+        lo[ax] = a;
+        hi[ax] = b;
+    }
+    return nb;   // what is left lies inside the leaf
+}
+
 // one thread per (brick row, depth)
 __global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrows, float* __restrict__ rows) {
     const EvalArgs& a = v.e;
@@ -687,21 +741,14 @@ __global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrow
         const int g0 = Lc[ax] * S + rd.z * B;
         const int c0 = rd.z * B;
         float* out = rows + row * (i64)(ROW_PER_DEPTH * (D + 1));
-        float bt[4][BR1];
-        for (int t = 0; t < 4; ++t)
-            for (int k = 0; k <= BR; ++k) {
-                float val = 0.f;
-                if (k <= B) {
-                    const int cidx = (d <= r) ? (Lc[ax] >> (r - d)) + t - 1 : ((g0 + k - 1) >> (D - d)) + t - 1;
-                    if (cidx >= 0 && cidx < (1 << d)) val = lattice_basis(a, d, cidx, g0 + k);
-                }
-                bt[t][k] = val;
-                out[ROW_BT * (D + 1) + (d * 4 + t) * BR1 + k] = val;
-            }
         if (d <= r) {
             for (int t = 0; t < 3; ++t) {
-                float mn = bt[t][0], mx = bt[t][0];
-                for (int k = 1; k <= B; ++k) { mn = fminf(mn, bt[t][k]); mx = fmaxf(mx, bt[t][k]); }
+                float mn = brick_bt(a, r, Lc[ax], g0, d, t, 0), mx = mn;
+                for (int k = 1; k <= B; ++k) {
+                    const float b = brick_bt(a, r, Lc[ax], g0, d, t, k);
+                    mn = fminf(mn, b);
+                    mx = fmaxf(mx, b);
+                }
                 out[ROW_RA * (D + 1) + (d * 3 + t) * 2] = mn;
                 out[ROW_RA * (D + 1) + (d * 3 + t) * 2 + 1] = mx;
             }
@@ -812,22 +859,31 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
                 cross |= c;
             }
             if (!cross) continue;
-            const int ncell = ext[0] * ext[1] * ext[2];
-            for (int t = lane; t < ncell; t += 32) {
-                const int n[3] = {t / (ext[1] * ext[2]), (t / ext[2]) % ext[1], t % ext[2]};
-                const int N[3] = {wlo[0] + n[0], wlo[1] + n[1], wlo[2] + n[2]};
-                const i64 node = shell_node(v, L, r, Lc, d, N);
-                if (node < 0) continue;
-                float blo[3], bhi[3];
-                for (int ax = 0; ax < 3; ++ax) {
-                    blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n[ax]) * 2];
-                    bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n[ax]) * 2 + 1];
+            // only window cells outside the leaf can hold a real node
+            const int span = 1 << (d - r);
+            const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
+            Box3 bxs[6];
+            const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
+            for (int q = 0; q < nbx; ++q) {
+                const Box3& bx = bxs[q];
+                const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+                for (int t = lane; t < ncell; t += 32) {
+                    const int i0 = t / n12, rem = t - i0 * n12, i1 = rem / bx.n[2], i2 = rem - i1 * bx.n[2];
+                    const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
+                    const i64 node = shell_node(v, L, r, Lc, d, N);
+                    if (node < 0) continue;
+                    float blo[3], bhi[3];
+                    for (int ax = 0; ax < 3; ++ax) {
+                        const int n = N[ax] - wlo[ax];
+                        blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2];
+                        bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2 + 1];
+                    }
+                    float tl, th;
+                    term_interval(a.x[node], blo, bhi, tl, th);
+                    lo += tl; hi += th;
+                    amax += fmaxf(fabsf(tl), fabsf(th));
+                    ++cnt;
                 }
-                float tl, th;
-                term_interval(a.x[node], blo, bhi, tl, th);
-                lo += tl; hi += th;
-                amax += fmaxf(fabsf(tl), fabsf(th));
-                ++cnt;
             }
         }
         for (int o = 16; o; o >>= 1) {
@@ -1005,17 +1061,37 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
             sm.xL[e] = bix.xl[(i64)lb.root * BR_LEVELS * 27 + e];
         for (int e = threadIdx.x; e < 3 * 36 * (D + 1); e += blockDim.x) {
             const int ax = e / (36 * (D + 1)), q = e % (36 * (D + 1));
-            sm.Bt[ax * BR_LEVELS * 36 + q] = brick_row(bix, D, lb.root, nb, ax, lb.b[ax])[ROW_BT * (D + 1) + q];
+            const int d = q / 36, t = (q % 36) / BR1, k = q % BR1;
+            sm.Bt[ax * BR_LEVELS * 36 + q] = (k <= E) ? brick_bt(a, r, Lc[ax], g0[ax], d, t, k) : 0.f;
         }
         __syncthreads();
+        {
+            int total = 0;
+            for (int d = r + 1; d <= D; ++d)
+                if (sm.woff[d] >= 0) total = sm.woff[d] + sm.wext[d][0] * sm.wext[d][1] * sm.wext[d][2];
+            for (int t = threadIdx.x; t < total; t += blockDim.x) sm.Xw[t] = 0.f;
+        }
+        __syncthreads();
+        // only window cells outside the leaf can hold a real node
         for (int d = r + 1; d <= D; ++d) {
             const int off = sm.woff[d];
             if (off < 0) continue;
-            const int e0 = sm.wext[d][0], e1 = sm.wext[d][1], e2 = sm.wext[d][2];
-            for (int t = threadIdx.x; t < e0 * e1 * e2; t += blockDim.x) {
-                const int N[3] = {sm.wlo[d][0] + t / (e1 * e2), sm.wlo[d][1] + (t / e2) % e1, sm.wlo[d][2] + t % e2};
-                const i64 node = shell_node(v, L, r, Lc, d, N);
-                sm.Xw[off + t] = node < 0 ? 0.f : a.x[node];
+            const int span = 1 << (d - r);
+            const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
+            const int wlo[3] = {sm.wlo[d][0], sm.wlo[d][1], sm.wlo[d][2]};
+            const int ext[3] = {sm.wext[d][0], sm.wext[d][1], sm.wext[d][2]};
+            Box3 bxs[6];
+            const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
+            for (int q = 0; q < nbx; ++q) {
+                const Box3& bx = bxs[q];
+                const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+                for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+                    const int i0 = t / n12, rem = t - i0 * n12, i1 = rem / bx.n[2], i2 = rem - i1 * bx.n[2];
+                    const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
+                    const i64 node = shell_node(v, L, r, Lc, d, N);
+                    if (node >= 0)
+                        sm.Xw[off + ((N[0] - wlo[0]) * ext[1] + (N[1] - wlo[1])) * ext[2] + (N[2] - wlo[2])] = a.x[node];
+                }
             }
         }
         __syncthreads();
@@ -1305,15 +1381,10 @@ void stage_mesh(Ctx& c) {
     const NodeArrays& nd = c.nodes;
     const i64 M = nd.M, lo = c.base[D], nD = c.count[D];
     float* x27 = build_x27(c, lo);
-    EvalArgs ea{c.nodes, D, c.basis, c.x, x27, x27 ? lo : 0, nullptr, {0}};
+    EvalArgs ea{c.nodes, D, c.basis, c.x, x27, x27 ? lo : 0, nullptr};
     float* lb = nullptr;
     {
-        i64 total = 0;
-        for (int d = 0; d <= D; ++d) {
-            ea.lb_off[d] = total;
-            total += (1ll << d) * (3ll * (1ll << (D - d)) + 1);
-        }
-        ea.lb_off[D + 1] = total;
+        const i64 total = lattice_basis_offset(D, D + 1);
         lb = dalloc<float>(total, s);
         k_lattice_basis<<<grid_for(total, 256), 256, 0, s>>>(c.basis, D, total, lb);
         CK_LAUNCH();
