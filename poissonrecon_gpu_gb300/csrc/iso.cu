@@ -1025,8 +1025,9 @@ struct LiveBrick {
 };
 
 // one block per live brick: exact corner values into the brick's (B+1)^3 slot
-__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const LiveBrick* __restrict__ live,
-                                                         i64 nlive, float* __restrict__ blat,
+__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const int* __restrict__ root_of,
+                                                         const LiveBrick* __restrict__ live, i64 nlive,
+                                                         float* __restrict__ blat,
                                                          unsigned long long* __restrict__ nforeign) {
     __shared__ BrickShared sm;
     const EvalArgs& a = v.e;
@@ -1109,8 +1110,23 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
             if (own == L) {
                 val = brick_leaf_levels(sm, r, kk, val);
             } else {
+                // the owner leaf (same depth r) and its ancestors: walk_up_u(own), with the
+                // owner's neighbour x from its row of the leaves' table
                 atomicAdd(nforeign, 1ull);
-                val = walk_up_u(a, own, qc, val);
+                const float* xo = bix.xl + (i64)root_of[own] * BR_LEVELS * 27;
+                int oc3[3];
+                key_coords(a.nd.key[own], r, D, oc3);
+                for (int l = r; l >= 0; --l) {
+                    float bv[3][3];
+                    for (int ax = 0; ax < 3; ++ax)
+                        for (int t = 0; t < 3; ++t) {
+                            const int n = (oc3[ax] >> (r - l)) + t - 1;
+                            bv[ax][t] = (n >= 0 && n < (1 << l)) ? lattice_basis(a, l, n, qc[ax]) : 0.f;
+                        }
+                    const float* xs = xo + 27 * l;
+                    for (int j = 0; j < 27; ++j)
+                        val = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
+                }
             }
             out[e] = val - v.iso;
         }
@@ -1567,7 +1583,6 @@ void stage_mesh(Ctx& c) {
         CK_LAUNCH();
         c.kend(kb);
         dfree(bsign, s);
-        dfree(root_of, s);
         int* bf = dalloc<int>(nbricks, s);
         int* bp = dalloc<int>(nbricks + 1, s);
         k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
@@ -1594,8 +1609,8 @@ void stage_mesh(Ctx& c) {
             unsigned long long* nfor = dalloc<unsigned long long>(1, s);
             CK(cudaMemsetAsync(nfor, 0, sizeof(unsigned long long), s));
             const int ke = c.kbegin("brick_eval", (double)lat_total * 4);
-            k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, live, nlive, lat_brick,
-                                                                                  nfor);
+            k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, root_of, live, nlive,
+                                                                                  lat_brick, nfor);
             CK_LAUNCH();
             c.kend(ke);
             c.foreign_corners = (i64)read_scalar(nfor, s);
@@ -1608,6 +1623,7 @@ void stage_mesh(Ctx& c) {
         dfree(bf, s);
         dfree(bp, s);
         dfree(culled, s);
+        dfree(root_of, s);
         dfree(dbpre, s);
         dfree(drpre, s);
         dfree(drd, s);
