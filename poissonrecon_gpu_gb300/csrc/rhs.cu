@@ -112,8 +112,11 @@ __global__ void k_div_thread(NodeArrays nd, DivArgs a, i64 lo, i64 hi, float* __
 }
 
 // nodes with many terms (depths < D-1): the node's terms, in neighbour order,
-// are cut into chunks of DIV_CHUNK; one warp sums a chunk in FP64 and the
-// chunk sums are added per node in chunk order (deterministic)
+// are cut into chunks of DIV_CHUNK; one warp sums a chunk and the chunk sums are
+// added per node in FP64 in chunk order (deterministic).  Within a chunk each
+// lane keeps a compensated float pair (hi + lo, Neumaier's summation), whose
+// error is at most 2u|sum| + O(n u^2) sum|term| -- FP64 accuracy for these
+// lengths without FP64 arithmetic per term.
 constexpr int DIV_CHUNK = 2048;
 constexpr int DIV_WARPS = 8;
 
@@ -168,12 +171,21 @@ __global__ void __launch_bounds__(DIV_WARPS * 32) k_div_chunks(NodeArrays nd, Di
         node_rows(a, nd.key[i], nd.depth[i], r0, r1, r2, t0);
         const int total = pre[w][27];
         const int lo = chunk * DIV_CHUNK, hi = min(total, lo + DIV_CHUNK);
-        double val = 0.0;
+        float sh = 0.f, sl = 0.f;
         int j = 0;
-        for (int t = lo + lane; t < hi; t += 32) {
-            while (pre[w][j + 1] <= t) ++j;
-            val += (double)div_term(a, r0, r1, r2, t0, (i64)sidx[w][j] + (t - pre[w][j]));
+        while (pre[w][j + 1] <= lo) ++j;
+        // neighbour by neighbour: each is a contiguous range of finest slots
+        for (; j < 27 && pre[w][j] < hi; ++j) {
+            const int a0 = max(lo, pre[w][j]), a1 = min(hi, pre[w][j + 1]);
+            const i64 base = (i64)sidx[w][j] - pre[w][j];
+            for (int t = a0 + lane; t < a1; t += 32) {
+                const float term = div_term(a, r0, r1, r2, t0, base + t);
+                const float s = sh + term;
+                sl += (fabsf(sh) >= fabsf(term)) ? (sh - s) + term : (term - s) + sh;
+                sh = s;
+            }
         }
+        double val = (double)sh + (double)sl;
         for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
         if (lane == 0) partial[it] = val;
         __syncwarp();

@@ -126,10 +126,11 @@ __global__ void k_group_table(NodeArrays nd, i64 ngroups, int* __restrict__ gn) 
 }
 
 constexpr int CG_TILE_GROUPS = CG_BLOCK / 8;   // sibling groups per tile, one thread per row
+constexpr int CG_WARP_TILES = 2;               // tiles of 4 groups a warp stages at once
 
 __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
                                                      const int* __restrict__ block_depth) {
-    __shared__ float sp[CG_TILE_GROUPS * 64];
+    __shared__ float sp[CG_TILE_GROUPS * 64 * CG_WARP_TILES];
     __shared__ float sst[27];
     __shared__ double sh[CG_BLOCK / 32];
     __shared__ int sh_ok;
@@ -198,42 +199,51 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                 loc += (double)(pi * o);
             }
         } else {
-            // one warp per tile of 4 groups (32 rows); warps run their tiles independently
+            // one warp per CG_WARP_TILES tiles of 4 groups (32 rows each); warps run independently.
+            // All group-table entries of the tiles are loaded before any gather, so each warp
+            // has 2 * CG_WARP_TILES * 8 independent loads in flight per round trip.
             const i64 gfirst = (dp.lo - 1) >> 3, ng = dp.n >> 3;
             const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
             const int ch = lane & 7, gl = lane >> 3;
             const int sx = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
-            float* wsp = sp + wib * (4 * 64);
-            const i64 wstride = (i64)dp.nblocks * (CG_BLOCK / 32);
-            for (i64 tile = (i64)rank * (CG_BLOCK / 32) + wib; tile * 4 < ng; tile += wstride) {
+            float* wsp = sp + wib * (CG_WARP_TILES * 4 * 64);
+            const i64 wstride = (i64)dp.nblocks * (CG_BLOCK / 32) * CG_WARP_TILES;
+            for (i64 tile = ((i64)rank * (CG_BLOCK / 32) + wib) * CG_WARP_TILES; tile * 4 < ng; tile += wstride) {
                 __syncwarp();
                 // the 4x4x4 block of each group: cell (bx,by,bz) is child ((bx+1)&1, ...) of the
                 // parent's neighbour ((bx+1)>>1, ...) in 0..2 per axis
+                int cn[CG_WARP_TILES * 8];
 #pragma unroll
-                for (int m = 0; m < 8; ++m) {
+                for (int m = 0; m < CG_WARP_TILES * 8; ++m) {
                     const int e = lane + 32 * m;
                     const i64 g = tile * 4 + (e >> 6);
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
-                    float pv = 0.f;
-                    if (g < ng) {
-                        const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
-                        const int cn = a.gn[(i64)jp * a.ngroups + gfirst + g];
-                        if (cn != -1) pv = pdir(cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)));
-                    }
-                    wsp[e] = pv;
+                    const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
+                    cn[m] = (g < ng) ? a.gn[(i64)jp * a.ngroups + gfirst + g] : -1;
+                }
+#pragma unroll
+                for (int m = 0; m < CG_WARP_TILES * 8; ++m) {
+                    const int e = lane + 32 * m;
+                    const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
+                    wsp[e] = (cn[m] != -1)
+                                 ? pdir(cn[m] + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)))
+                                 : 0.f;
                 }
                 __syncwarp();
-                const i64 g = tile * 4 + gl;
-                if (g < ng) {
-                    const float* blk = wsp + gl * 64;
-                    float o = 0.f;
 #pragma unroll
-                    for (int j = 0; j < 27; ++j)
-                        o = fmaf(sst[j], blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
-                    const float pi = blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
-                    pnew[dp.lo + 8 * g + ch] = pi;
-                    a.q[dp.lo + 8 * g + ch] = o;
-                    loc += (double)(pi * o);
+                for (int tt = 0; tt < CG_WARP_TILES; ++tt) {
+                    const i64 g = (tile + tt) * 4 + gl;
+                    if (g < ng) {
+                        const float* blk = wsp + tt * 256 + gl * 64;
+                        float o = 0.f;
+#pragma unroll
+                        for (int j = 0; j < 27; ++j)
+                            o = fmaf(sst[j], blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
+                        const float pi = blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
+                        pnew[dp.lo + 8 * g + ch] = pi;
+                        a.q[dp.lo + 8 * g + ch] = o;
+                        loc += (double)(pi * o);
+                    }
                 }
             }
         }
@@ -242,12 +252,32 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
         const float al = (float)((double)r1 / pq);
         const float nal = -al;
         loc = 0;
-        for (i64 t = start; t < dp.n; t += stride) {
-            const i64 i = dp.lo + t;
-            a.x[i] = fmaf(al, pnew[i], a.x[i]);
-            const float ri = fmaf(nal, a.q[i], a.r[i]);
-            a.r[i] = ri;
-            loc += (double)(ri * ri);
+        {
+            // four rows per thread per step, loads first (independent requests in flight)
+            i64 t = start;
+            for (; t + 3 * stride < dp.n; t += 4 * stride) {
+                float pv[4], qv[4], xv[4], rv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const i64 i = dp.lo + t + u * stride;
+                    pv[u] = pnew[i]; qv[u] = a.q[i]; xv[u] = a.x[i]; rv[u] = a.r[i];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const i64 i = dp.lo + t + u * stride;
+                    a.x[i] = fmaf(al, pv[u], xv[u]);
+                    const float ri = fmaf(nal, qv[u], rv[u]);
+                    a.r[i] = ri;
+                    loc += (double)(ri * ri);
+                }
+            }
+            for (; t < dp.n; t += stride) {
+                const i64 i = dp.lo + t;
+                a.x[i] = fmaf(al, pnew[i], a.x[i]);
+                const float ri = fmaf(nal, a.q[i], a.r[i]);
+                a.r[i] = ri;
+                loc += (double)(ri * ri);
+            }
         }
         r0 = r1;
         r1 = (float)preduce(loc, ok);
