@@ -314,14 +314,89 @@ __device__ float owner_corner_value(const EvalArgs& a, i64 o, int kind, float is
     return val - iso;
 }
 
-// finest-depth corners: each corner evaluated by its owner
-__global__ void k_finest_corner_values(EvalArgs a, i64 lo, i64 hi, float iso, float* __restrict__ cval) {
+// finest-depth corners: each corner evaluated by its owner.  A node owns a
+// corner when no other existing node of the 8 around it has a smaller key; the
+// owned corners of a node share one walk to the root (the same levels and
+// neighbour x, each corner with its own basis values and FMA chain, in the
+// order of owner_corner_value).
+__global__ void __launch_bounds__(128, 6) k_finest_corner_values(EvalArgs a, i64 lo, i64 hi, float iso,
+                                                                 float* __restrict__ cval) {
+    const NodeArrays& nd = a.nd;
+    const int D = a.D;
+    const i64 M = nd.M;
     for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
-        for (int kind = 0; kind < 8; ++kind) {
-            int ok;
-            const int own = corner_owner(a.nd, i, kind, ok);
-            if (own == i) cval[8 * (i - lo) + kind] = owner_corner_value(a, i, kind, iso);
+        const u64 ki = nd.key[i];
+        unsigned smaller = 0;   // bit j: neighbour j exists and has a smaller key
+#pragma unroll
+        for (int j = 0; j < 27; ++j) {
+            if (j == 13) continue;
+            const int nb = nd.neigh[(i64)j * M + i];
+            if (nb != -1 && nd.key[nb] < ki) smaller |= 1u << j;
         }
+        unsigned owned = 0;
+#pragma unroll
+        for (int kind = 0; kind < 8; ++kind) {
+            const int sx = kind & 1, sy = (kind >> 1) & 1, sz = (kind >> 2) & 1;
+            bool own = true;
+#pragma unroll
+            for (int e = 1; e < 8; ++e) {
+                const int j = 9 * (sx - (e & 1) + 1) + 3 * (sy - ((e >> 1) & 1) + 1) + (sz - ((e >> 2) & 1) + 1);
+                if ((smaller >> j) & 1) own = false;
+            }
+            if (own) owned |= 1u << kind;
+        }
+        if (!owned) continue;
+        int xyz[3];
+        key_coords(ki, D, D, xyz);
+        float val[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) val[k] = 0.f;
+        i64 node = i;
+        int d = D;
+        int c[3] = {xyz[0], xyz[1], xyz[2]};
+        while (node != -1) {
+            float xs[27];
+            if (node < a.nx27) {
+                const float4* row = reinterpret_cast<const float4*>(a.x27 + node * X27_STRIDE);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const float4 t = row[k];
+                    xs[4 * k] = t.x; xs[4 * k + 1] = t.y; xs[4 * k + 2] = t.z; xs[4 * k + 3] = t.w;
+                }
+                const float4 t = row[6];
+                xs[24] = t.x; xs[25] = t.y; xs[26] = t.z;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 27; ++j) {
+                    const int nb = nd.neigh[(i64)j * M + node];
+                    xs[j] = nb == -1 ? 0.f : a.x[nb];   // absent: a zero product leaves the sum unchanged
+                }
+            }
+            const int lim = 1 << d;
+#pragma unroll 1
+            for (int kind = 0; kind < 8; ++kind) {
+                if (!((owned >> kind) & 1)) continue;
+                const int u[3] = {xyz[0] + (kind & 1), xyz[1] + ((kind >> 1) & 1), xyz[2] + ((kind >> 2) & 1)};
+                float bv[3][3];
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+                    for (int t = 0; t < 3; ++t) {
+                        const int n = c[ax] + t - 1;
+                        bv[ax][t] = (n >= 0 && n < lim) ? lattice_basis(a, d, n, u[ax]) : 0.f;
+                    }
+                float v = val[kind];
+#pragma unroll
+                for (int j = 0; j < 27; ++j) v = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], v);
+                val[kind] = v;
+            }
+            node = nd.parent[node];
+            --d;
+            c[0] >>= 1; c[1] >>= 1; c[2] >>= 1;
+        }
+#pragma unroll
+        for (int kind = 0; kind < 8; ++kind)
+            if ((owned >> kind) & 1) cval[8 * (i - lo) + kind] = val[kind] - iso;
     }
 }
 

@@ -101,11 +101,21 @@ __global__ void k_div_thread(NodeArrays nd, DivArgs a, i64 lo, i64 hi, float* __
         int t0[3];
         node_rows(a, nd.key[i], nd.depth[i], r0, r1, r2, t0);
         double val = 0.0;
-        for (int j = 0; j < 27; ++j) {
-            const int nb = nd.neigh[(i64)j * a.M + i];
-            if (nb == -1) continue;
-            const int s0 = nd.didx[nb], sn = nd.dnum[nb];
-            for (int k = 0; k < sn; ++k) val += (double)div_term(a, r0, r1, r2, t0, (i64)s0 + k);
+        // neighbours in three batches of nine: indices, then descendant ranges, then terms,
+        // so that each batch's loads are in flight together
+#pragma unroll
+        for (int jb = 0; jb < 27; jb += 9) {
+            int nb[9], s0[9], sn[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) nb[q] = nd.neigh[(i64)(jb + q) * a.M + i];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                s0[q] = nb[q] == -1 ? 0 : nd.didx[nb[q]];
+                sn[q] = nb[q] == -1 ? 0 : nd.dnum[nb[q]];
+            }
+#pragma unroll
+            for (int q = 0; q < 9; ++q)
+                for (int k = 0; k < sn[q]; ++k) val += (double)div_term(a, r0, r1, r2, t0, (i64)s0[q] + k);
         }
         out[i] = (float)val;
     }
