@@ -1028,16 +1028,23 @@ __global__ void k_root_of(const VRoot* __restrict__ roots, int nroots, int* __re
         root_of[roots[k].node] = k;
 }
 
+// shared memory of one brick of edge at most EB: bricks of edge 8 (leaves with
+// lattice edge >= 8) and of edge 2 or 4 (the smallest leaves) are evaluated by
+// two instances.  Window bound for EB = 4 with the extra upper cell: 8^3 + 6^3.
+template <int EB>
 struct BrickShared {
+    static constexpr int K1 = EB + 1;         // corners per axis
+    static constexpr int XW = (EB == BR) ? BR_XW : 728;
     float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
-    float Bt[3 * BR_LEVELS * 36];             // [axis][depth][t][k], from the brick-row tables
-    float Xw[BR_XW];                          // window coefficients, virtual depths (0: none or inside the leaf)
+    float Bt[3 * BR_LEVELS * 4 * K1];         // [axis][depth][t][k]
+    float Xw[XW];                             // window coefficients, virtual depths (0: none or inside the leaf)
     int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
     int wext[BR_LEVELS][3];
     int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
 };
-__device__ __forceinline__ float bt_at(const BrickShared& sm, int ax, int d, int t, int k) {
-    return sm.Bt[(ax * BR_LEVELS + d) * 36 + t * BR1 + k];
+template <int EB>
+__device__ __forceinline__ float bt_at(const BrickShared<EB>& sm, int ax, int d, int t, int k) {
+    return sm.Bt[((ax * BR_LEVELS + d) * 4 + t) * BrickShared<EB>::K1 + k];
 }
 
 // virtual-depth part of the value of corner qc (brick-local kk) whose owner
@@ -1049,7 +1056,8 @@ __device__ __forceinline__ float bt_at(const BrickShared& sm, int ax, int d, int
 // lies inside the owner's leaf, cells inside either leaf, absent nodes) read 0
 // here, and adding a zero product leaves the sum unchanged, so the value is the
 // same.
-__device__ __forceinline__ float brick_virtual(const BrickShared& sm, int D, int r, const int oc[3], const int qc[3],
+template <int EB>
+__device__ __forceinline__ float brick_virtual(const BrickShared<EB>& sm, int D, int r, const int oc[3], const int qc[3],
                                                const int kk[3]) {
     float val = 0.f;
     for (int d = D; d > r; --d) {
@@ -1077,7 +1085,8 @@ __device__ __forceinline__ float brick_virtual(const BrickShared& sm, int D, int
 }
 
 // the brick's leaf itself and its real ancestors (walk_up with absent neighbours as 0)
-__device__ __forceinline__ float brick_leaf_levels(const BrickShared& sm, int r, const int kk[3], float val) {
+template <int EB>
+__device__ __forceinline__ float brick_leaf_levels(const BrickShared<EB>& sm, int r, const int kk[3], float val) {
     for (int l = r; l >= 0; --l) {
         const float* xs = sm.xL + 27 * l;
         float bv[3][3];
@@ -1100,14 +1109,17 @@ struct LiveBrick {
 };
 
 // one block per live brick: exact corner values into the brick's (B+1)^3 slot
-__global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix, const int* __restrict__ root_of,
-                                                         const LiveBrick* __restrict__ live, i64 nlive,
-                                                         float* __restrict__ blat,
-                                                         unsigned long long* __restrict__ nforeign) {
-    __shared__ BrickShared sm;
+template <int EB, int NT>
+__global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, const int* __restrict__ root_of,
+                                                   const LiveBrick* __restrict__ live, const int* __restrict__ list,
+                                                   i64 nlist, float* __restrict__ blat,
+                                                   unsigned long long* __restrict__ nforeign) {
+    __shared__ BrickShared<EB> sm;
+    constexpr int K1 = BrickShared<EB>::K1;
     const EvalArgs& a = v.e;
     const int D = a.D;
-    for (i64 li = blockIdx.x; li < nlive; li += gridDim.x) {
+    for (i64 it = blockIdx.x; it < nlist; it += gridDim.x) {
+        const i64 li = list[it];
         const LiveBrick lb = live[li];
         const VRoot R = v.roots[lb.root];
         const int r = R.depth, S = 1 << (D - r), L = R.node, E = brick_edge(D, r), nb = S / E, E1 = E + 1;
@@ -1116,37 +1128,34 @@ __global__ void __launch_bounds__(BR_BLOCK) k_brick_eval(VArgs v, BrickIndex bix
         const int g0[3] = {Lc[0] * S + lb.b[0] * E, Lc[1] * S + lb.b[1] * E, Lc[2] * S + lb.b[2] * E};
         const bool fposs = brick_foreign_possible(v, R, lb.b, nb);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            int off = 0;
-            for (int d = r + 1; d <= D; ++d) {
-                bool cross = false;
-                for (int ax = 0; ax < 3; ++ax) {
-                    bool c;
-                    window_axis(g0[ax], E, Lc[ax], r, d, D, fposs ? 1 : 0, sm.wlo[d][ax], sm.wext[d][ax], c);
-                    cross |= c;
-                }
-                if (cross) {
-                    sm.woff[d] = off;
-                    off += sm.wext[d][0] * sm.wext[d][1] * sm.wext[d][2];
-                } else {
-                    sm.woff[d] = -1;
-                }
+        // window layout (every thread sizes it; thread 0 records it), leaf tables, zeroed window
+        int total = 0;
+        for (int d = r + 1; d <= D; ++d) {
+            int wl[3], we[3];
+            bool cross = false;
+            for (int ax = 0; ax < 3; ++ax) {
+                bool c;
+                window_axis(g0[ax], E, Lc[ax], r, d, D, fposs ? 1 : 0, wl[ax], we[ax], c);
+                cross |= c;
             }
+            if (threadIdx.x == 0) {
+                for (int ax = 0; ax < 3; ++ax) { sm.wlo[d][ax] = wl[ax]; sm.wext[d][ax] = we[ax]; }
+                sm.woff[d] = cross ? total : -1;
+            }
+            if (cross) total += we[0] * we[1] * we[2];
+        }
+        if (total > BrickShared<EB>::XW) {   // cannot happen for aligned bricks: reported, brick skipped
+            if (threadIdx.x == 0) atomicAdd(nforeign + 1, 1ull);
+            continue;
         }
         for (int e = threadIdx.x; e < 27 * (r + 1); e += blockDim.x)
             sm.xL[e] = bix.xl[(i64)lb.root * BR_LEVELS * 27 + e];
-        for (int e = threadIdx.x; e < 3 * 36 * (D + 1); e += blockDim.x) {
-            const int ax = e / (36 * (D + 1)), q = e % (36 * (D + 1));
-            const int d = q / 36, t = (q % 36) / BR1, k = q % BR1;
-            sm.Bt[ax * BR_LEVELS * 36 + q] = (k <= E) ? brick_bt(a, r, Lc[ax], g0[ax], d, t, k) : 0.f;
+        for (int e = threadIdx.x; e < 3 * 4 * K1 * (D + 1); e += blockDim.x) {
+            const int ax = e / (4 * K1 * (D + 1)), q = e % (4 * K1 * (D + 1));
+            const int d = q / (4 * K1), t = (q % (4 * K1)) / K1, k = q % K1;
+            sm.Bt[ax * BR_LEVELS * 4 * K1 + q] = (k <= E) ? brick_bt(a, r, Lc[ax], g0[ax], d, t, k) : 0.f;
         }
-        __syncthreads();
-        {
-            int total = 0;
-            for (int d = r + 1; d <= D; ++d)
-                if (sm.woff[d] >= 0) total = sm.woff[d] + sm.wext[d][0] * sm.wext[d][1] * sm.wext[d][2];
-            for (int t = threadIdx.x; t < total; t += blockDim.x) sm.Xw[t] = 0.f;
-        }
+        for (int t = threadIdx.x; t < total; t += blockDim.x) sm.Xw[t] = 0.f;
         __syncthreads();
         // only window cells outside the leaf can hold a real node
         for (int d = r + 1; d <= D; ++d) {
@@ -1232,6 +1241,14 @@ __global__ void k_live_offsets(LiveBrick* __restrict__ live, const i64* __restri
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
         live[k].lat = lat_pos[k];
         live[k].cell = cell_pos[k];
+    }
+}
+// live bricks split by edge: 8 (first list) and 2 or 4 (second list)
+__global__ void k_live_split(VArgs v, const LiveBrick* __restrict__ live, i64 n, int* __restrict__ big,
+                             int* __restrict__ small, unsigned long long* __restrict__ cnt) {
+    for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        if (brick_edge(v.e.D, v.roots[live[k].root].depth) == BR) big[atomicAdd(&cnt[0], 1ull)] = (int)k;
+        else small[atomicAdd(&cnt[1], 1ull)] = (int)k;
     }
 }
 __global__ void k_live_flags(const unsigned char* __restrict__ culled, i64 n, int* __restrict__ f) {
@@ -1681,15 +1698,41 @@ void stage_mesh(Ctx& c) {
             const i64 lat_total = read_scalar(lpos + nlive, s);
             total_cells = read_scalar(cpos + nlive, s);
             lat_brick = dalloc<float>(lat_total, s);
-            unsigned long long* nfor = dalloc<unsigned long long>(1, s);
-            CK(cudaMemsetAsync(nfor, 0, sizeof(unsigned long long), s));
-            const int ke = c.kbegin("brick_eval", (double)lat_total * 4);
-            k_brick_eval<<<grid_for(nlive, 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(va, bix, root_of, live, nlive,
-                                                                                  lat_brick, nfor);
+            // bricks of edge 8 and the smaller ones go to the two instances of the evaluation
+            // big, small, foreign corners, window layout overflows
+            unsigned long long* cnt3 = dalloc<unsigned long long>(4, s);
+            int* lists = dalloc<int>(2 * nlive, s);
+            CK(cudaMemsetAsync(cnt3, 0, 4 * sizeof(unsigned long long), s));
+            k_live_split<<<grid_for(nlive, 256), 256, 0, s>>>(va, live, nlive, lists, lists + nlive, cnt3);
             CK_LAUNCH();
+            unsigned long long hc[2];
+            CK(cudaMemcpyAsync(hc, cnt3, sizeof hc, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            // compulsory: the corner values written (bricks of edge 8: 729 each)
+            const int ke = c.kbegin("brick_eval", (double)hc[0] * BR_CORNERS * 4);
+            if (hc[0] > 0) {
+                k_brick_eval<BR, BR_BLOCK><<<grid_for((i64)hc[0], 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(
+                    va, bix, root_of, live, lists, (i64)hc[0], lat_brick, cnt3 + 2);
+                CK_LAUNCH();
+            }
             c.kend(ke);
-            c.foreign_corners = (i64)read_scalar(nfor, s);
-            dfree(nfor, s);
+            const int ks = c.kbegin("brick_eval_small", (double)(lat_total - (i64)hc[0] * BR_CORNERS) * 4);
+            if (hc[1] > 0) {
+                k_brick_eval<4, 64><<<grid_for((i64)hc[1], 1, (i64)c.sms * 24), 64, 0, s>>>(
+                    va, bix, root_of, live, lists + nlive, (i64)hc[1], lat_brick, cnt3 + 2);
+                CK_LAUNCH();
+            }
+            c.kend(ks);
+            unsigned long long hf[2];
+            CK(cudaMemcpyAsync(hf, cnt3 + 2, sizeof hf, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            c.foreign_corners = (i64)hf[0];
+            dfree(cnt3, s);
+            dfree(lists, s);
+            if (hf[1]) {
+                set_last_error("brick window layout overflow in %llu bricks", hf[1]);
+                throw Error{PRGPU_ERR_LIMIT, {0}};
+            }
             dfree(lsz, s);
             dfree(csz, s);
             dfree(lpos, s);
