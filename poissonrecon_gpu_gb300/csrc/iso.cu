@@ -314,6 +314,60 @@ __device__ float owner_corner_value(const EvalArgs& a, i64 o, int kind, float is
     return val - iso;
 }
 
+// for each corner k in 'mask' of node 'node' (depth d, coordinates xyz): the
+// walk_up_u sum from the node to the root at the corner's lattice point
+// (xyz + bit) << sh, all corners sharing the walk (the same levels and
+// neighbour x, each corner with its own basis values and FMA chain)
+__device__ __forceinline__ void walk_up_corners(const EvalArgs& a, i64 node, int d, const int xyz[3], int sh,
+                                                unsigned mask, float val[8]) {
+    const NodeArrays& nd = a.nd;
+    const i64 M = nd.M;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) val[k] = 0.f;
+    int c[3] = {xyz[0], xyz[1], xyz[2]};
+    while (node != -1) {
+        float xs[27];
+        if (node < a.nx27) {
+            const float4* row = reinterpret_cast<const float4*>(a.x27 + node * X27_STRIDE);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const float4 t = row[k];
+                xs[4 * k] = t.x; xs[4 * k + 1] = t.y; xs[4 * k + 2] = t.z; xs[4 * k + 3] = t.w;
+            }
+            const float4 t = row[6];
+            xs[24] = t.x; xs[25] = t.y; xs[26] = t.z;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                const int nb = nd.neigh[(i64)j * M + node];
+                xs[j] = nb == -1 ? 0.f : a.x[nb];   // absent: a zero product leaves the sum unchanged
+            }
+        }
+        const int lim = 1 << d;
+#pragma unroll 1
+        for (int kind = 0; kind < 8; ++kind) {
+            if (!((mask >> kind) & 1)) continue;
+            const int u[3] = {(xyz[0] + (kind & 1)) << sh, (xyz[1] + ((kind >> 1) & 1)) << sh,
+                              (xyz[2] + ((kind >> 2) & 1)) << sh};
+            float bv[3][3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const int n = c[ax] + t - 1;
+                    bv[ax][t] = (n >= 0 && n < lim) ? lattice_basis(a, d, n, u[ax]) : 0.f;
+                }
+            float v = val[kind];
+#pragma unroll
+            for (int j = 0; j < 27; ++j) v = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], v);
+            val[kind] = v;
+        }
+        node = nd.parent[node];
+        --d;
+        c[0] >>= 1; c[1] >>= 1; c[2] >>= 1;
+    }
+}
+
 // finest-depth corners: each corner evaluated by its owner.  A node owns a
 // corner when no other existing node of the 8 around it has a smaller key; the
 // owned corners of a node share one walk to the root (the same levels and
@@ -349,51 +403,7 @@ __global__ void __launch_bounds__(128, 6) k_finest_corner_values(EvalArgs a, i64
         int xyz[3];
         key_coords(ki, D, D, xyz);
         float val[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) val[k] = 0.f;
-        i64 node = i;
-        int d = D;
-        int c[3] = {xyz[0], xyz[1], xyz[2]};
-        while (node != -1) {
-            float xs[27];
-            if (node < a.nx27) {
-                const float4* row = reinterpret_cast<const float4*>(a.x27 + node * X27_STRIDE);
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    const float4 t = row[k];
-                    xs[4 * k] = t.x; xs[4 * k + 1] = t.y; xs[4 * k + 2] = t.z; xs[4 * k + 3] = t.w;
-                }
-                const float4 t = row[6];
-                xs[24] = t.x; xs[25] = t.y; xs[26] = t.z;
-            } else {
-#pragma unroll
-                for (int j = 0; j < 27; ++j) {
-                    const int nb = nd.neigh[(i64)j * M + node];
-                    xs[j] = nb == -1 ? 0.f : a.x[nb];   // absent: a zero product leaves the sum unchanged
-                }
-            }
-            const int lim = 1 << d;
-#pragma unroll 1
-            for (int kind = 0; kind < 8; ++kind) {
-                if (!((owned >> kind) & 1)) continue;
-                const int u[3] = {xyz[0] + (kind & 1), xyz[1] + ((kind >> 1) & 1), xyz[2] + ((kind >> 2) & 1)};
-                float bv[3][3];
-#pragma unroll
-                for (int ax = 0; ax < 3; ++ax)
-#pragma unroll
-                    for (int t = 0; t < 3; ++t) {
-                        const int n = c[ax] + t - 1;
-                        bv[ax][t] = (n >= 0 && n < lim) ? lattice_basis(a, d, n, u[ax]) : 0.f;
-                    }
-                float v = val[kind];
-#pragma unroll
-                for (int j = 0; j < 27; ++j) v = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], v);
-                val[kind] = v;
-            }
-            node = nd.parent[node];
-            --d;
-            c[0] >>= 1; c[1] >>= 1; c[2] >>= 1;
-        }
+        walk_up_corners(a, i, D, xyz, 0, owned, val);
 #pragma unroll
         for (int kind = 0; kind < 8; ++kind)
             if ((owned >> kind) & 1) cval[8 * (i - lo) + kind] = val[kind] - iso;
@@ -472,10 +482,53 @@ __global__ void k_coarse_need(NodeArrays nd, i64 lo, i64 hi, unsigned char* __re
         }
     }
 }
-__global__ void k_coarse_corner_values(EvalArgs a, i64 n, float iso, const unsigned char* __restrict__ need,
-                                       float* __restrict__ cval) {
-    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < 8 * n; e += (i64)gridDim.x * blockDim.x)
-        if (need[e]) cval[e] = owner_corner_value(a, e >> 3, (int)(e & 7), iso);
+// the needed corners of one node share the walk up (owner_corner_value: walk
+// up, then for each corner its own descent through children[childrenVertexKind])
+__global__ void __launch_bounds__(128, 6) k_coarse_corner_values(EvalArgs a, i64 n, float iso,
+                                                                 const unsigned char* __restrict__ need,
+                                                                 float* __restrict__ cval) {
+    const NodeArrays& nd = a.nd;
+    const int D = a.D;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        unsigned mask = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) mask |= need[8 * i + k] ? (1u << k) : 0u;
+        if (!mask) continue;
+        float val[8];
+        if (i == 0) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) val[k] = 0.f;   // the root has no corner value of its own
+        } else {
+            const int d = nd.depth[i];
+            int xyz[3];
+            key_coords(nd.key[i], d, D, xyz);
+            const int sh = D - d;
+            walk_up_corners(a, i, d, xyz, sh, mask, val);
+            if (nd.child0[i] != -1) {
+#pragma unroll 1
+                for (int kind = 0; kind < 8; ++kind) {
+                    if (!((mask >> kind) & 1)) continue;
+                    const int u[3] = {(xyz[0] + (kind & 1)) << sh, (xyz[1] + ((kind >> 1) & 1)) << sh,
+                                      (xyz[2] + ((kind >> 2) & 1)) << sh};
+                    const int exceed = c_vid[kind];
+                    i64 node = i;
+                    float v = val[kind];
+                    for (int dd = d + 1; dd <= D; ++dd) {
+                        const int c0 = nd.child0[node];
+                        if (c0 == -1) break;
+                        node = c0 + exceed;
+                        int cx[3];
+                        key_coords(nd.key[node], dd, D, cx);
+                        v = level_sum_u(a, node, dd, cx, u, v);
+                    }
+                    val[kind] = v;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if ((mask >> k) & 1) cval[8 * i + k] = val[k] - iso;
+    }
 }
 
 // leaves above the finest depth: sign change at their corners or a marked face
@@ -1536,7 +1589,7 @@ void stage_mesh(Ctx& c) {
         CK(cudaMemsetAsync(need, 0, 8 * nCoarse, s));
         k_coarse_need<<<grid_for(nCoarse - 1, 256), 256, 0, s>>>(nd, 1, nCoarse, need);
         CK_LAUNCH();
-        k_coarse_corner_values<<<grid_for(8 * nCoarse, 128, 1ll << 30), 128, 0, s>>>(ea, nCoarse, c.iso, need, ccv);
+        k_coarse_corner_values<<<grid_for(nCoarse, 128, 1ll << 30), 128, 0, s>>>(ea, nCoarse, c.iso, need, ccv);
         CK_LAUNCH();
         k_coarse_leaves<<<grid_for(nCoarse - 1, 128, 1ll << 30), 128, 0, s>>>(ea, 1, nCoarse, ccv, fflag, has_tri,
                                                                              has_int, is_root);
