@@ -297,7 +297,7 @@ def main():
         "cg_iters": stats.get("cg_iters"),
         "kernels": stats.get("kernels"),
         "subdivision": {k: stats.get(k) for k in ("roots_per_depth", "virtual_cells", "bricks", "live_bricks",
-                                                  "foreign_corners")},
+                                                  "foreign_corners", "foreign_evaluated")},
         "nodes": stats.get("nodes"),
         "mesh": {"vertices": nv, "triangles": nt},
     }

@@ -446,9 +446,9 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
     }
     snprintf(tmp, sizeof tmp,
              "],\"virtual_cells\":%lld,\"bricks\":%lld,\"live_bricks\":%lld,\"foreign_corners\":%lld,"
-             "\"kernel_launches\":%llu",
+             "\"foreign_evaluated\":%lld,\"kernel_launches\":%llu",
              (long long)c->virtual_cells, (long long)c->total_bricks, (long long)c->live_bricks,
-             (long long)c->foreign_corners,
+             (long long)c->foreign_corners, (long long)c->foreign_slow,
              (unsigned long long)g_kernel_launches);
     js += tmp;
     js += ",\"cg_iters\":[";

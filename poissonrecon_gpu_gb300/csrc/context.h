@@ -126,6 +126,7 @@ struct Ctx {
     i64 virtual_cells = 0;
     i64 total_bricks = 0, live_bricks = 0;   // subdivided leaves: bricks, and those not culled
     i64 foreign_corners = 0;                 // brick corners owned by another leaf of the batch
+    i64 foreign_slow = 0;                    // of those, evaluated because the owner's brick was culled
 
     StageTimes t;
     bool profile = false;

@@ -1166,7 +1166,8 @@ template <int EB, int NT>
 __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, const int* __restrict__ root_of,
                                                    const LiveBrick* __restrict__ live, const int* __restrict__ list,
                                                    i64 nlist, float* __restrict__ blat,
-                                                   unsigned long long* __restrict__ nforeign) {
+                                                   unsigned long long* __restrict__ nforeign,
+                                                   int2* __restrict__ foreign, i64 foreign_cap) {
     __shared__ BrickShared<EB> sm;
     constexpr int K1 = BrickShared<EB>::K1;
     const EvalArgs& a = v.e;
@@ -1188,7 +1189,7 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
             bool cross = false;
             for (int ax = 0; ax < 3; ++ax) {
                 bool c;
-                window_axis(g0[ax], E, Lc[ax], r, d, D, fposs ? 1 : 0, wl[ax], we[ax], c);
+                window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wl[ax], we[ax], c);
                 cross |= c;
             }
             if (threadIdx.x == 0) {
@@ -1243,30 +1244,53 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
             int oc[3] = {qc[0] - 1 + (uu == 0), qc[1] - 1 + (ww == 0), qc[2] - 1 + (zz == 0)};
             int own = L;
             if (fposs && (uu == 0 || ww == 0 || zz == 0)) own = lower_face_owner(v, R, Lc, qc, oc);
-            float val = brick_virtual(sm, D, r, oc, qc, kk);
-            if (own == L) {
-                val = brick_leaf_levels(sm, r, kk, val);
-            } else {
-                // the owner leaf (same depth r) and its ancestors: walk_up_u(own), with the
-                // owner's neighbour x from its row of the leaves' table
-                atomicAdd(nforeign, 1ull);
-                const float* xo = bix.xl + (i64)root_of[own] * BR_LEVELS * 27;
-                int oc3[3];
-                key_coords(a.nd.key[own], r, D, oc3);
-                for (int l = r; l >= 0; --l) {
-                    float bv[3][3];
-                    for (int ax = 0; ax < 3; ++ax)
-                        for (int t = 0; t < 3; ++t) {
-                            const int n = (oc3[ax] >> (r - l)) + t - 1;
-                            bv[ax][t] = (n >= 0 && n < (1 << l)) ? lattice_basis(a, l, n, qc[ax]) : 0.f;
-                        }
-                    const float* xs = xo + 27 * l;
-                    for (int j = 0; j < 27; ++j)
-                        val = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
-                }
+            if (own != L) {   // owned by another leaf of the batch: filled by k_foreign_fill
+                const unsigned long long f = atomicAdd(nforeign, 1ull);
+                if ((i64)f < foreign_cap) foreign[f] = make_int2((int)li, e);
+                continue;
             }
-            out[e] = val - v.iso;
+            out[e] = brick_leaf_levels(sm, r, kk, brick_virtual(sm, D, r, oc, qc, kk)) - v.iso;
         }
+    }
+}
+
+// corners on a leaf's lower faces owned by a cell of another leaf L' of the
+// batch: the same value is a corner of L''s brick holding the owner cell, where
+// L' owns it -- copied when that brick is live, evaluated otherwise
+__global__ void k_foreign_fill(VArgs v, BrickIndex bix, const int* __restrict__ root_of,
+                               const LiveBrick* __restrict__ live, const unsigned char* __restrict__ culled,
+                               const int* __restrict__ live_pos, const int2* __restrict__ foreign, i64 n,
+                               float* __restrict__ blat, unsigned long long* __restrict__ nslow) {
+    const int D = v.e.D;
+    for (i64 f = (i64)blockIdx.x * blockDim.x + threadIdx.x; f < n; f += (i64)gridDim.x * blockDim.x) {
+        const int2 fe = foreign[f];
+        const LiveBrick lb = live[fe.x];
+        const VRoot R = v.roots[lb.root];
+        const int r = R.depth, S = 1 << (D - r), E = brick_edge(D, r), E1 = E + 1, nb = S / E;
+        int Lc[3];
+        key_coords(v.e.nd.key[R.node], r, D, Lc);
+        const int e = fe.y;
+        const int qc[3] = {Lc[0] * S + lb.b[0] * E + e / (E1 * E1), Lc[1] * S + lb.b[1] * E + (e / E1) % E1,
+                           Lc[2] * S + lb.b[2] * E + e % E1};
+        int oc[3] = {0, 0, 0};
+        const int own = lower_face_owner(v, R, Lc, qc, oc);
+        const int k2 = root_of[own];
+        int Lc2[3];
+        key_coords(v.e.nd.key[own], r, D, Lc2);
+        int b2[3], kk2[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            b2[ax] = (oc[ax] - Lc2[ax] * S) / E;
+            kk2[ax] = qc[ax] - (Lc2[ax] * S + b2[ax] * E);
+        }
+        const i64 bi2 = bix.prefix[k2] + ((i64)b2[0] * nb + b2[1]) * nb + b2[2];
+        float val;
+        if (!culled[bi2]) {
+            val = blat[live[live_pos[bi2]].lat + (kk2[0] * E1 + kk2[1]) * E1 + kk2[2]];
+        } else {
+            atomicAdd(nslow, 1ull);
+            val = virtual_corner_value(v, own, r, oc, qc) - v.iso;
+        }
+        blat[lb.lat + e] = val;
     }
 }
 
@@ -1663,6 +1687,7 @@ void stage_mesh(Ctx& c) {
     c.total_bricks = 0;
     c.live_bricks = 0;
     c.foreign_corners = 0;
+    c.foreign_slow = 0;
     VRoot* droots = nullptr;
     i64 *act_virt = nullptr, *tri_virt = nullptr;
     unsigned char* vcat = nullptr;
@@ -1752,10 +1777,13 @@ void stage_mesh(Ctx& c) {
             total_cells = read_scalar(cpos + nlive, s);
             lat_brick = dalloc<float>(lat_total, s);
             // bricks of edge 8 and the smaller ones go to the two instances of the evaluation
-            // big, small, foreign corners, window layout overflows
-            unsigned long long* cnt3 = dalloc<unsigned long long>(4, s);
+            // big, small, foreign corners, window layout overflows, foreign corners evaluated
+            unsigned long long* cnt3 = dalloc<unsigned long long>(5, s);
             int* lists = dalloc<int>(2 * nlive, s);
-            CK(cudaMemsetAsync(cnt3, 0, 4 * sizeof(unsigned long long), s));
+            CK(cudaMemsetAsync(cnt3, 0, 5 * sizeof(unsigned long long), s));
+            // corners owned by another leaf: at most the lower-face corners of the live bricks
+            const i64 fcap = std::min<i64>(lat_total, nlive * (BR_CORNERS - BR * BR * BR));
+            int2* foreign = dalloc<int2>(std::max<i64>(fcap, 1), s);
             k_live_split<<<grid_for(nlive, 256), 256, 0, s>>>(va, live, nlive, lists, lists + nlive, cnt3);
             CK_LAUNCH();
             unsigned long long hc[2];
@@ -1765,14 +1793,14 @@ void stage_mesh(Ctx& c) {
             const int ke = c.kbegin("brick_eval", (double)hc[0] * BR_CORNERS * 4);
             if (hc[0] > 0) {
                 k_brick_eval<BR, BR_BLOCK><<<grid_for((i64)hc[0], 1, (i64)c.sms * 16), BR_BLOCK, 0, s>>>(
-                    va, bix, root_of, live, lists, (i64)hc[0], lat_brick, cnt3 + 2);
+                    va, bix, root_of, live, lists, (i64)hc[0], lat_brick, cnt3 + 2, foreign, fcap);
                 CK_LAUNCH();
             }
             c.kend(ke);
             const int ks = c.kbegin("brick_eval_small", (double)(lat_total - (i64)hc[0] * BR_CORNERS) * 4);
             if (hc[1] > 0) {
                 k_brick_eval<4, 64><<<grid_for((i64)hc[1], 1, (i64)c.sms * 24), 64, 0, s>>>(
-                    va, bix, root_of, live, lists + nlive, (i64)hc[1], lat_brick, cnt3 + 2);
+                    va, bix, root_of, live, lists + nlive, (i64)hc[1], lat_brick, cnt3 + 2, foreign, fcap);
                 CK_LAUNCH();
             }
             c.kend(ks);
@@ -1780,12 +1808,25 @@ void stage_mesh(Ctx& c) {
             CK(cudaMemcpyAsync(hf, cnt3 + 2, sizeof hf, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             c.foreign_corners = (i64)hf[0];
-            dfree(cnt3, s);
-            dfree(lists, s);
             if (hf[1]) {
                 set_last_error("brick window layout overflow in %llu bricks", hf[1]);
                 throw Error{PRGPU_ERR_LIMIT, {0}};
             }
+            if ((i64)hf[0] > fcap) {
+                set_last_error("foreign corner list overflow (%llu > %lld)", hf[0], (long long)fcap);
+                throw Error{PRGPU_ERR_LIMIT, {0}};
+            }
+            if (hf[0] > 0) {
+                const int kf = c.kbegin("foreign_fill", (double)hf[0] * 8);
+                k_foreign_fill<<<grid_for((i64)hf[0], 128, 1ll << 30), 128, 0, s>>>(
+                    va, bix, root_of, live, culled, bp, foreign, (i64)hf[0], lat_brick, cnt3 + 4);
+                CK_LAUNCH();
+                c.kend(kf);
+                c.foreign_slow = (i64)read_scalar(cnt3 + 4, s);
+            }
+            dfree(cnt3, s);
+            dfree(lists, s);
+            dfree(foreign, s);
             dfree(lsz, s);
             dfree(csz, s);
             dfree(lpos, s);
