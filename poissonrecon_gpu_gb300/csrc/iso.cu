@@ -855,13 +855,28 @@ __device__ __forceinline__ int outside_boxes(const int wlo[3], const int ext[3],
 }
 
 // one thread per (brick row, depth)
-__global__ void k_brick_rows(VArgs v, const int4* __restrict__ rowdesc, i64 nrows, float* __restrict__ rows) {
+// root k's batch id on its node (depth >= 3; shallower roots are single-root batches)
+__global__ void k_batch_flags(const VRoot* __restrict__ roots, int nroots, int* __restrict__ bflag) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nroots; k += gridDim.x * blockDim.x)
+        if (roots[k].depth >= 3) bflag[roots[k].node] = roots[k].batch;
+}
+
+// one thread per (brick row, depth); rows numbered root by root (row_prefix), 3 x bricks-per-edge each
+__global__ void k_brick_rows(VArgs v, const i64* __restrict__ row_prefix, int nroots, i64 nrows,
+                             float* __restrict__ rows) {
     const EvalArgs& a = v.e;
     const int D = a.D;
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < nrows * (D + 1); e += (i64)gridDim.x * blockDim.x) {
         const i64 row = e / (D + 1);
         const int d = (int)(e % (D + 1));
-        const int4 rd = rowdesc[row];             // root, axis, brick index
+        int lo = 0, hi = nroots - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (row_prefix[mid] <= row) lo = mid; else hi = mid - 1;
+        }
+        const int nbk = (1 << (D - v.roots[lo].depth)) / brick_edge(D, v.roots[lo].depth);
+        const int rl = (int)(row - row_prefix[lo]);
+        const int4 rd = make_int4(lo, rl / nbk, rl % nbk, 0);   // root, axis, brick index
         const VRoot R = v.roots[rd.x];
         const int ax = rd.y, r = R.depth, S = 1 << (D - r), B = brick_edge(D, r);
         int Lc[3];
@@ -1641,7 +1656,6 @@ void stage_mesh(Ctx& c) {
     dfree(is_root, s);
     // batches: one per root above depth 3, one per depth from 3
     std::vector<VRoot> roots;
-    std::vector<int> bflag_host;   // filled lazily below
     int nb = 0;
     std::vector<int> depth_batch(D + 1, 0);
     for (const int2& hr : hroots) {
@@ -1701,38 +1715,36 @@ void stage_mesh(Ctx& c) {
     va.nroots = (int)roots.size();
     VirtCells vc{};
     if (!roots.empty()) {
-        bflag_host.assign(M, 0);
-        for (auto& R : roots) if (R.depth >= 3) bflag_host[R.node] = R.batch;
-        droots = dalloc<VRoot>((i64)roots.size(), s);
+        const int nr = (int)roots.size();
+        droots = dalloc<VRoot>(nr, s);
         bflag = dalloc<int>(M, s);
-        CK(cudaMemcpyAsync(droots, roots.data(), roots.size() * sizeof(VRoot), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(bflag, bflag_host.data(), M * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(droots, roots.data(), nr * sizeof(VRoot), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(bflag, 0, M * sizeof(int), s));
+        k_batch_flags<<<grid_for(nr, 256), 256, 0, s>>>(droots, nr, bflag);
+        CK_LAUNCH();
         va.roots = droots;
         va.batch_root_flag = bflag;
-        const int nr = (int)roots.size();
-        std::vector<i64> brick_prefix(nr), row_prefix(nr);
-        std::vector<int4> rowdesc;
-        i64 nbricks = 0;
+        // bricks and brick rows, numbered root by root (prefix table: 2 x 8 bytes per root)
+        std::vector<i64> pre(2 * (i64)nr + 2);
+        i64 nbricks = 0, nrows = 0;
         for (int k = 0; k < nr; ++k) {
             const int S = 1 << (D - roots[k].depth), E = std::min(S, BR), nbk = S / E;
-            brick_prefix[k] = nbricks;
-            row_prefix[k] = (i64)rowdesc.size();
+            pre[k] = nbricks;
+            pre[nr + 1 + k] = nrows;
             nbricks += (i64)nbk * nbk * nbk;
-            for (int ax = 0; ax < 3; ++ax)
-                for (int b = 0; b < nbk; ++b) rowdesc.push_back(make_int4(k, ax, b, 0));
+            nrows += 3 * nbk;
         }
-        const i64 nrows = (i64)rowdesc.size();
-        i64* dbpre = dalloc<i64>(nr, s);
-        i64* drpre = dalloc<i64>(nr, s);
-        int4* drd = dalloc<int4>(nrows, s);
+        pre[nr] = nbricks;
+        pre[2 * (i64)nr + 1] = nrows;
+        i64* dpre = dalloc<i64>(2 * (i64)nr + 2, s);
+        CK(cudaMemcpyAsync(dpre, pre.data(), pre.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+        i64* dbpre = dpre;
+        i64* drpre = dpre + nr + 1;
         float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
         float* xl = dalloc<float>((i64)nr * BR_LEVELS * 27, s);
-        CK(cudaMemcpyAsync(dbpre, brick_prefix.data(), nr * sizeof(i64), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(drpre, row_prefix.data(), nr * sizeof(i64), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(drd, rowdesc.data(), nrows * sizeof(int4), cudaMemcpyHostToDevice, s));
         BrickIndex bix{dbpre, drpre, nr, rows, xl};
         const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
-        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drd, nrows, rows);
+        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drpre, nr, nrows, rows);
         CK_LAUNCH();
         k_brick_xl<<<grid_for((i64)nr * BR_LEVELS * 27, 256), 256, 0, s>>>(va, nr, xl);
         CK_LAUNCH();
@@ -1836,9 +1848,7 @@ void stage_mesh(Ctx& c) {
         dfree(bp, s);
         dfree(culled, s);
         dfree(root_of, s);
-        dfree(dbpre, s);
-        dfree(drpre, s);
-        dfree(drd, s);
+        dfree(dpre, s);
         dfree(rows, s);
         dfree(xl, s);
         vc.live = live;
