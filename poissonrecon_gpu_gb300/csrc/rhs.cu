@@ -188,7 +188,19 @@ __global__ void __launch_bounds__(DIV_WARPS * 32) k_div_chunks(NodeArrays nd, Di
         for (; j < 27 && pre[w][j] < hi; ++j) {
             const int a0 = max(lo, pre[w][j]), a1 = min(hi, pre[w][j + 1]);
             const i64 base = (i64)sidx[w][j] - pre[w][j];
-            for (int t = a0 + lane; t < a1; t += 32) {
+            int t = a0 + lane;
+            // two terms per step: their loads are issued together
+            for (; t + 32 < a1; t += 64) {
+                const float t1 = div_term(a, r0, r1, r2, t0, base + t);
+                const float t2 = div_term(a, r0, r1, r2, t0, base + t + 32);
+                float s = sh + t1;
+                sl += (fabsf(sh) >= fabsf(t1)) ? (sh - s) + t1 : (t1 - s) + sh;
+                sh = s;
+                s = sh + t2;
+                sl += (fabsf(sh) >= fabsf(t2)) ? (sh - s) + t2 : (t2 - s) + sh;
+                sh = s;
+            }
+            if (t < a1) {
                 const float term = div_term(a, r0, r1, r2, t0, base + t);
                 const float s = sh + term;
                 sl += (fabsf(sh) >= fabsf(term)) ? (sh - s) + term : (term - s) + sh;
