@@ -861,8 +861,14 @@ __global__ void k_batch_flags(const VRoot* __restrict__ roots, int nroots, int* 
         if (roots[k].depth >= 3) bflag[roots[k].node] = roots[k].batch;
 }
 
+// edge of the bricks (super == 0) or of the super-bricks (super == 1: 4^3 bricks of 8^3
+// cells, in leaves with lattice edge >= 64; 0 elsewhere)
+__device__ __forceinline__ int row_edge(int D, int r, int super) {
+    return super ? ((D - r >= 6) ? 4 * BR : 0) : brick_edge(D, r);
+}
+
 // one thread per (brick row, depth); rows numbered root by root (row_prefix), 3 x bricks-per-edge each
-__global__ void k_brick_rows(VArgs v, const i64* __restrict__ row_prefix, int nroots, i64 nrows,
+__global__ void k_brick_rows(VArgs v, const i64* __restrict__ row_prefix, int nroots, i64 nrows, int super,
                              float* __restrict__ rows) {
     const EvalArgs& a = v.e;
     const int D = a.D;
@@ -874,11 +880,11 @@ __global__ void k_brick_rows(VArgs v, const i64* __restrict__ row_prefix, int nr
             const int mid = (lo + hi + 1) >> 1;
             if (row_prefix[mid] <= row) lo = mid; else hi = mid - 1;
         }
-        const int nbk = (1 << (D - v.roots[lo].depth)) / brick_edge(D, v.roots[lo].depth);
+        const int nbk = (1 << (D - v.roots[lo].depth)) / row_edge(D, v.roots[lo].depth, super);
         const int rl = (int)(row - row_prefix[lo]);
         const int4 rd = make_int4(lo, rl / nbk, rl % nbk, 0);   // root, axis, brick index
         const VRoot R = v.roots[rd.x];
-        const int ax = rd.y, r = R.depth, S = 1 << (D - r), B = brick_edge(D, r);
+        const int ax = rd.y, r = R.depth, S = 1 << (D - r), B = row_edge(D, r, super);
         int Lc[3];
         key_coords(a.nd.key[R.node], r, D, Lc);
         const int g0 = Lc[ax] * S + rd.z * B;
@@ -952,10 +958,113 @@ __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, 
     return own;
 }
 
+// one warp per super-brick (4^3 bricks of leaves with lattice edge >= 64): the
+// same bound over all its corners; decided only when every window it needs fits
+// the row tables (away from the leaf's boundary).  ssign = 1, -1 or 0.
+__global__ void __launch_bounds__(256) k_super_bound(VArgs v, const i64* __restrict__ sprefix,
+                                                     const i64* __restrict__ srow_prefix, int nroots,
+                                                     const float* __restrict__ srows, const float* __restrict__ xl_all,
+                                                     i64 nsuper, signed char* __restrict__ ssign) {
+    const EvalArgs& a = v.e;
+    const int D = a.D;
+    const int lane = threadIdx.x & 31;
+    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    const double u = 5.9604644775390625e-08;   // 2^-24
+    for (i64 si = warp; si < nsuper; si += nwarps) {
+        int lo = 0, hi = nroots - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sprefix[mid] <= si) lo = mid; else hi = mid - 1;
+        }
+        const VRoot R = v.roots[lo];
+        const int r = R.depth, S = 1 << (D - r), E = 4 * BR, ns = S / E, L = R.node;
+        const i64 l = si - sprefix[lo];
+        const int sb[3] = {(int)(l / ((i64)ns * ns)), (int)((l / ns) % ns), (int)(l % ns)};
+        int Lc[3];
+        key_coords(a.nd.key[L], r, D, Lc);
+        const int g0[3] = {Lc[0] * S + sb[0] * E, Lc[1] * S + sb[1] * E, Lc[2] * S + sb[2] * E};
+        const float* row[3];
+        for (int ax = 0; ax < 3; ++ax)
+            row[ax] = srows + (srow_prefix[lo] + (i64)ax * ns + sb[ax]) * (i64)(ROW_PER_DEPTH * (D + 1));
+        const float* xl = xl_all + (i64)lo * BR_LEVELS * 27;
+        float flo = 0.f, fhi = 0.f, amax = 0.f;
+        int cnt = 0;
+        bool decided = true;
+        for (int t = lane; t < 27 * (r + 1); t += 32) {
+            const int lv = r - t / 27, j = t % 27;
+            const float x = xl[27 * lv + j];
+            if (x == 0.f) continue;
+            const int tt[3] = {j / 9, (j / 3) % 3, j % 3};
+            float blo[3], bhi[3];
+            for (int ax = 0; ax < 3; ++ax) {
+                blo[ax] = row[ax][ROW_RA * (D + 1) + (lv * 3 + tt[ax]) * 2];
+                bhi[ax] = row[ax][ROW_RA * (D + 1) + (lv * 3 + tt[ax]) * 2 + 1];
+            }
+            float tl, th;
+            term_interval(x, blo, bhi, tl, th);
+            flo += tl; fhi += th;
+            amax += fmaxf(fabsf(tl), fabsf(th));
+            ++cnt;
+        }
+        for (int d = r + 1; d <= D && decided; ++d) {
+            int wlo[3], ext[3];
+            bool cross = false;
+            for (int ax = 0; ax < 3; ++ax) {
+                bool c;
+                window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wlo[ax], ext[ax], c);
+                cross |= c;
+            }
+            if (!cross) continue;
+            if (ext[0] > BR_WEXT || ext[1] > BR_WEXT || ext[2] > BR_WEXT) { decided = false; break; }
+            const int span = 1 << (d - r);
+            const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
+            Box3 bxs[6];
+            const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
+            for (int q = 0; q < nbx; ++q) {
+                const Box3& bx = bxs[q];
+                const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+                for (int t = lane; t < ncell; t += 32) {
+                    const int i0 = t / n12, rem = t - i0 * n12, i1 = rem / bx.n[2], i2 = rem - i1 * bx.n[2];
+                    const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
+                    const i64 node = shell_node(v, L, r, Lc, d, N);
+                    if (node < 0) continue;
+                    float blo[3], bhi[3];
+                    for (int ax = 0; ax < 3; ++ax) {
+                        const int n = N[ax] - wlo[ax];
+                        blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2];
+                        bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2 + 1];
+                    }
+                    float tl, th;
+                    term_interval(a.x[node], blo, bhi, tl, th);
+                    flo += tl; fhi += th;
+                    amax += fmaxf(fabsf(tl), fabsf(th));
+                    ++cnt;
+                }
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            flo += __shfl_xor_sync(0xffffffffu, flo, o);
+            fhi += __shfl_xor_sync(0xffffffffu, fhi, o);
+            amax += __shfl_xor_sync(0xffffffffu, amax, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0) {
+            const double iso = (double)v.iso, A = (double)amax * 1.01;
+            const double margin = (2.0 * cnt + 8.0) * u * A +
+                                  4.0 * u * (fabs((double)flo) + fabs((double)fhi) + 2.0 * fabs(iso)) + 1e-30;
+            const bool above = (double)flo - margin > iso, below = (double)fhi + margin < iso;
+            ssign[si] = !decided ? 0 : (above ? 1 : (below ? -1 : 0));
+        }
+    }
+}
+
 // one warp per brick: the bound over the corners the brick's leaf owns;
 // sign[bi] = 1 (all above iso), -1 (all below) or 0 (not proven)
 constexpr int BB_BLOCK = 256;
-__global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bix, i64 nbricks,
+__global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bix, i64 first, i64 nbricks,
+                                                          const i64* __restrict__ sprefix,
+                                                          const signed char* __restrict__ ssign,
                                                           signed char* __restrict__ sign) {
     const EvalArgs& a = v.e;
     const int D = a.D;
@@ -963,9 +1072,17 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
     const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
     const double u = 5.9604644775390625e-08;   // 2^-24
-    for (i64 bi = warp; bi < nbricks; bi += nwarps) {
+    for (i64 bi = first + warp; bi < nbricks; bi += nwarps) {
         const VBrick B = brick_of(v, bix, bi);
         const VRoot R = v.roots[B.root];
+        if (ssign && v.e.D - R.depth >= 6) {   // decided by its super-brick?
+            const int ns = (1 << (v.e.D - R.depth)) / (4 * BR);
+            const signed char sg = ssign[sprefix[B.root] + ((i64)(B.b[0] >> 2) * ns + (B.b[1] >> 2)) * ns + (B.b[2] >> 2)];
+            if (sg != 0) {
+                if (lane == 0) sign[bi] = sg;
+                continue;
+            }
+        }
         const int r = R.depth, S = 1 << (D - r), L = R.node, E = brick_edge(D, r), nb = S / E;
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
@@ -1725,27 +1842,43 @@ void stage_mesh(Ctx& c) {
         va.roots = droots;
         va.batch_root_flag = bflag;
         // bricks and brick rows, numbered root by root (prefix table: 2 x 8 bytes per root)
-        std::vector<i64> pre(2 * (i64)nr + 2);
-        i64 nbricks = 0, nrows = 0;
+        // prefix tables: bricks, brick rows, super-bricks, super rows (nr + 1 entries each)
+        std::vector<i64> pre(4 * ((i64)nr + 1));
+        i64 nbricks = 0, nrows = 0, nsuper = 0, nsrows = 0;
         for (int k = 0; k < nr; ++k) {
             const int S = 1 << (D - roots[k].depth), E = std::min(S, BR), nbk = S / E;
+            const int ns = (D - roots[k].depth >= 6) ? S / (4 * BR) : 0;
             pre[k] = nbricks;
-            pre[nr + 1 + k] = nrows;
+            pre[(nr + 1) + k] = nrows;
+            pre[2 * (nr + 1) + k] = nsuper;
+            pre[3 * (nr + 1) + k] = nsrows;
             nbricks += (i64)nbk * nbk * nbk;
             nrows += 3 * nbk;
+            nsuper += (i64)ns * ns * ns;
+            nsrows += 3 * ns;
         }
         pre[nr] = nbricks;
-        pre[2 * (i64)nr + 1] = nrows;
-        i64* dpre = dalloc<i64>(2 * (i64)nr + 2, s);
+        pre[2 * nr + 1] = nrows;
+        pre[3 * nr + 2] = nsuper;
+        pre[4 * nr + 3] = nsrows;
+        i64* dpre = dalloc<i64>(4 * ((i64)nr + 1), s);
         CK(cudaMemcpyAsync(dpre, pre.data(), pre.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
         i64* dbpre = dpre;
         i64* drpre = dpre + nr + 1;
+        i64* dspre = dpre + 2 * (nr + 1);
+        i64* dsrpre = dpre + 3 * (nr + 1);
         float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
         float* xl = dalloc<float>((i64)nr * BR_LEVELS * 27, s);
         BrickIndex bix{dbpre, drpre, nr, rows, xl};
         const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
-        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drpre, nr, nrows, rows);
+        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drpre, nr, nrows, 0, rows);
         CK_LAUNCH();
+        float* srows = nullptr;
+        if (nsrows > 0) {
+            srows = dalloc<float>(nsrows * ROW_PER_DEPTH * (D + 1), s);
+            k_brick_rows<<<grid_for(nsrows * (D + 1), 128), 128, 0, s>>>(va, dsrpre, nr, nsrows, 1, srows);
+            CK_LAUNCH();
+        }
         k_brick_xl<<<grid_for((i64)nr * BR_LEVELS * 27, 256), 256, 0, s>>>(va, nr, xl);
         CK_LAUNCH();
         c.kend(kr);
@@ -1759,12 +1892,33 @@ void stage_mesh(Ctx& c) {
         // sign written and read, the culled flag written
         const int kb = c.kbegin("brick_bound", (double)nrows * (6 + 2 * BR_WEXT) * (D + 1) * 4 +
                                                    (double)nr * BR_LEVELS * 27 * 4 + (double)nbricks * 3);
-        k_brick_bound<<<grid_for(nbricks * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, nbricks, bsign);
-        CK_LAUNCH();
-        k_brick_cull<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, root_of, bsign, nbricks, culled);
+        signed char* ssign = nullptr;
+        if (nsuper > 0) {
+            ssign = dalloc<signed char>(nsuper, s);
+            k_super_bound<<<grid_for(nsuper * 32, 256, (i64)c.sms * 8), 256, 0, s>>>(va, dspre, dsrpre, nr, srows, xl,
+                                                                                    nsuper, ssign);
+            CK_LAUNCH();
+        }
+        // bricks of leaves with lattice edge >= 16 come first (roots are in depth order)
+        i64 nbig = 0;
+        for (int k = 0; k < nr; ++k)
+            if (D - roots[k].depth >= 4) nbig = pre[k + 1];
+        k_brick_bound<<<grid_for(nbig * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, 0, nbig, dspre,
+                                                                                         ssign, bsign);
         CK_LAUNCH();
         c.kend(kb);
+        const int kb2 = c.kbegin("brick_bound_small", (double)(nbricks - nbig) * 3);
+        if (nbricks > nbig) {
+            k_brick_bound<<<grid_for((nbricks - nbig) * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(
+                va, bix, nbig, nbricks, dspre, ssign, bsign);
+            CK_LAUNCH();
+        }
+        k_brick_cull<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, root_of, bsign, nbricks, culled);
+        CK_LAUNCH();
+        c.kend(kb2);
         dfree(bsign, s);
+        dfree(ssign, s);
+        dfree(srows, s);
         int* bf = dalloc<int>(nbricks, s);
         int* bp = dalloc<int>(nbricks + 1, s);
         k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
