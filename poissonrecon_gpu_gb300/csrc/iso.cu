@@ -797,8 +797,9 @@ __device__ __forceinline__ bool brick_foreign_possible(const VArgs& v, const VRo
 __device__ __forceinline__ void window_axis(int g0, int B, int Lc_ax, int r, int d, int D, int extra, int& wlo,
                                             int& ext, bool& cross) {
     const int sh = D - d, span = 1 << (d - r);
-    const int Vlo = (g0 - 1) >> sh, Vhi = (g0 + B - 1) >> sh;
     const int llo = Lc_ax * span;
+    // the first corner's owner cell: the one below it, or its own on the leaf's lower face
+    const int Vlo = (g0 == (llo << sh)) ? (g0 >> sh) : ((g0 - 1) >> sh), Vhi = (g0 + B - 1) >> sh;
     cross = (Vlo - 1 < llo || Vhi + 1 >= llo + span);
     wlo = Vlo - 1;
     ext = Vhi - Vlo + 3 + extra;
@@ -911,8 +912,9 @@ __global__ void k_brick_rows(VArgs v, const i64* __restrict__ row_prefix, int nr
                 float mn = 0.f, mx = 0.f;             // 0: corners without this term
                 if (n < ext && N >= 0 && N < lim) {
                     for (int k = 0; k <= B; ++k) {
-                        const int Va = (g0 + k - 1) >> sh;
-                        const int Vb = (k == 0 && c0 == 0) ? (g0 >> sh) : Va;   // lower-face owner cell
+                        // owner cell of corner k: the lower-face corner owns its own cell
+                        const int Va = (k == 0 && c0 == 0) ? (g0 >> sh) : ((g0 + k - 1) >> sh);
+                        const int Vb = Va;
                         if (N < Va - 1 || N > Vb + 1) continue;
                         const float b = lattice_basis(a, d, N, g0 + k);
                         mn = fminf(mn, b);
