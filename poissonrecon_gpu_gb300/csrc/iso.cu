@@ -369,14 +369,10 @@ __device__ __forceinline__ void walk_up_corners(const EvalArgs& a, i64 node, int
 }
 
 // finest-depth corners: each corner evaluated by its owner.  A node owns a
-// corner when no other existing node of the 8 around it has a smaller key; the
-// owned corners of a node share one walk to the root (the same levels and
-// neighbour x, each corner with its own basis values and FMA chain, in the
-// order of owner_corner_value).
-__global__ void __launch_bounds__(128, 6) k_finest_corner_values(EvalArgs a, i64 lo, i64 hi, float iso,
-                                                                 float* __restrict__ cval) {
-    const NodeArrays& nd = a.nd;
-    const int D = a.D;
+// corner when no other existing node of the 8 around it has a smaller key.
+// Pass 1 (one thread per node): the mask of owned corners and their count.
+__global__ void k_finest_owned(NodeArrays nd, i64 lo, i64 hi, unsigned char* __restrict__ owned_mask,
+                               int* __restrict__ owned_count) {
     const i64 M = nd.M;
     for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
         const u64 ki = nd.key[i];
@@ -390,23 +386,48 @@ __global__ void __launch_bounds__(128, 6) k_finest_corner_values(EvalArgs a, i64
         unsigned owned = 0;
 #pragma unroll
         for (int kind = 0; kind < 8; ++kind) {
-            const int sx = kind & 1, sy = (kind >> 1) & 1, sz = (kind >> 2) & 1;
+            const int sx = kind & 1, sy = (kind >> 1) & 1, sz = kind >> 2;
             bool own = true;
 #pragma unroll
             for (int e = 1; e < 8; ++e) {
-                const int j = 9 * (sx - (e & 1) + 1) + 3 * (sy - ((e >> 1) & 1) + 1) + (sz - ((e >> 2) & 1) + 1);
+                const int j = 9 * (sx - (e & 1) + 1) + 3 * (sy - ((e >> 1) & 1) + 1) + (sz - (e >> 2) + 1);
                 if ((smaller >> j) & 1) own = false;
             }
             if (own) owned |= 1u << kind;
         }
-        if (!owned) continue;
+        owned_mask[i - lo] = (unsigned char)owned;
+        owned_count[i - lo] = __popc(owned);
+    }
+}
+
+// the owned corners as a list: (finest slot << 3) | corner
+__global__ void k_finest_list(const unsigned char* __restrict__ owned_mask, const int* __restrict__ first, i64 nD,
+                              int* __restrict__ list) {
+    for (i64 l = (i64)blockIdx.x * blockDim.x + threadIdx.x; l < nD; l += (i64)gridDim.x * blockDim.x) {
+        unsigned m = owned_mask[l];
+        int q = first[l];
+        while (m) {
+            const int kind = __ffs(m) - 1;
+            list[q++] = (int)(l << 3) | kind;
+            m &= m - 1;
+        }
+    }
+}
+
+// pass 2 (one thread per owned corner): walk_up_u from the owner at the corner,
+// the value of owner_corner_value (no descent at the finest depth)
+__global__ void __launch_bounds__(128, 8) k_finest_corner_values(EvalArgs a, i64 lo, const int* __restrict__ list,
+                                                                 i64 ncorner, float iso, float* __restrict__ cval) {
+    const int D = a.D;
+    for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < ncorner; q += (i64)gridDim.x * blockDim.x) {
+        const int lk = list[q];
+        const i64 l = lk >> 3;
+        const int kind = lk & 7;
+        const i64 i = lo + l;
         int xyz[3];
-        key_coords(ki, D, D, xyz);
-        float val[8];
-        walk_up_corners(a, i, D, xyz, 0, owned, val);
-#pragma unroll
-        for (int kind = 0; kind < 8; ++kind)
-            if ((owned >> kind) & 1) cval[8 * (i - lo) + kind] = val[kind] - iso;
+        key_coords(a.nd.key[i], D, D, xyz);
+        const int u[3] = {xyz[0] + (kind & 1), xyz[1] + ((kind >> 1) & 1), xyz[2] + (kind >> 2)};
+        cval[8 * l + kind] = walk_up_u(a, i, u, 0.f) - iso;
     }
 }
 
@@ -528,6 +549,25 @@ __global__ void __launch_bounds__(128, 6) k_coarse_corner_values(EvalArgs a, i64
 #pragma unroll
         for (int k = 0; k < 8; ++k)
             if ((mask >> k) & 1) cval[8 * i + k] = val[k] - iso;
+    }
+}
+
+// needed corners of each coarse node as a mask and a count
+__global__ void k_need_mask(const unsigned char* __restrict__ need, i64 n, unsigned char* __restrict__ mask,
+                            int* __restrict__ count) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        unsigned m = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) m |= need[8 * i + k] ? (1u << k) : 0u;
+        mask[i] = (unsigned char)m;
+        count[i] = __popc(m);
+    }
+}
+__global__ void __launch_bounds__(128, 8) k_coarse_corner_list(EvalArgs a, const int* __restrict__ list, i64 n,
+                                                               float iso, float* __restrict__ cval) {
+    for (i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (i64)gridDim.x * blockDim.x) {
+        const int lk = list[q];
+        cval[lk] = owner_corner_value(a, lk >> 3, lk & 7, iso);   // cval index = 8 node + corner
     }
 }
 
@@ -1715,8 +1755,30 @@ void stage_mesh(Ctx& c) {
     unsigned char* cat = dalloc<unsigned char>(nD, s);
     int* ntri = dalloc<int>(nD, s);
     int kt = c.kbegin("corner_values", (double)M * (108 + 8 + 4 + 4) + (double)nD * 8 * 4);
-    k_finest_corner_values<<<grid_for(nD, 128, 1ll << 30), 128, 0, s>>>(ea, lo, M, c.iso, cval);
-    CK_LAUNCH();
+    {
+        if (nD >= (1ll << 28)) {
+            set_last_error("%lld finest nodes exceed the corner list's 2^28", (long long)nD);
+            throw Error{PRGPU_ERR_LIMIT, {0}};
+        }
+        unsigned char* omask = dalloc<unsigned char>(nD, s);
+        int* ocnt = dalloc<int>(nD, s);
+        int* ofirst = dalloc<int>(nD + 1, s);
+        k_finest_owned<<<grid_for(nD, 256), 256, 0, s>>>(nd, lo, M, omask, ocnt);
+        CK_LAUNCH();
+        exclusive_scan<int, int>(ocnt, ofirst, nD, ofirst + nD, s);
+        const i64 nown = read_scalar(ofirst + nD, s);
+        if (nown > 0) {
+            int* olist = dalloc<int>(nown, s);
+            k_finest_list<<<grid_for(nD, 256), 256, 0, s>>>(omask, ofirst, nD, olist);
+            CK_LAUNCH();
+            k_finest_corner_values<<<grid_for(nown, 128, 1ll << 30), 128, 0, s>>>(ea, lo, olist, nown, c.iso, cval);
+            CK_LAUNCH();
+            dfree(olist, s);
+        }
+        dfree(omask, s);
+        dfree(ocnt, s);
+        dfree(ofirst, s);
+    }
     c.kend(kt);
     kt = c.kbegin("cells", (double)nD * (8 * 4 + 108 + 8 * 4 + 1 + 4));
     k_finest_cells<<<grid_for(nD, 128, 1ll << 30), 128, 0, s>>>(nd, lo, M, cval, cell_v, cat, ntri);
@@ -1747,8 +1809,27 @@ void stage_mesh(Ctx& c) {
         CK(cudaMemsetAsync(need, 0, 8 * nCoarse, s));
         k_coarse_need<<<grid_for(nCoarse - 1, 256), 256, 0, s>>>(nd, 1, nCoarse, need);
         CK_LAUNCH();
-        k_coarse_corner_values<<<grid_for(nCoarse, 128, 1ll << 30), 128, 0, s>>>(ea, nCoarse, c.iso, need, ccv);
-        CK_LAUNCH();
+        {
+            // one thread per needed corner (list of (node << 3) | corner)
+            unsigned char* nmask = dalloc<unsigned char>(nCoarse, s);
+            int* ncnt = dalloc<int>(nCoarse, s);
+            int* nfirst = dalloc<int>(nCoarse + 1, s);
+            k_need_mask<<<grid_for(nCoarse, 256), 256, 0, s>>>(need, nCoarse, nmask, ncnt);
+            CK_LAUNCH();
+            exclusive_scan<int, int>(ncnt, nfirst, nCoarse, nfirst + nCoarse, s);
+            const i64 nneed = read_scalar(nfirst + nCoarse, s);
+            if (nneed > 0) {
+                int* nlist = dalloc<int>(nneed, s);
+                k_finest_list<<<grid_for(nCoarse, 256), 256, 0, s>>>(nmask, nfirst, nCoarse, nlist);
+                CK_LAUNCH();
+                k_coarse_corner_list<<<grid_for(nneed, 128, 1ll << 30), 128, 0, s>>>(ea, nlist, nneed, c.iso, ccv);
+                CK_LAUNCH();
+                dfree(nlist, s);
+            }
+            dfree(nmask, s);
+            dfree(ncnt, s);
+            dfree(nfirst, s);
+        }
         k_coarse_leaves<<<grid_for(nCoarse - 1, 128, 1ll << 30), 128, 0, s>>>(ea, 1, nCoarse, ccv, fflag, has_tri,
                                                                              has_int, is_root);
         CK_LAUNCH();
