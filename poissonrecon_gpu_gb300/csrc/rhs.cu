@@ -189,7 +189,18 @@ __global__ void __launch_bounds__(DIV_WARPS * 32) k_div_chunks(NodeArrays nd, Di
             const int a0 = max(lo, pre[w][j]), a1 = min(hi, pre[w][j + 1]);
             const i64 base = (i64)sidx[w][j] - pre[w][j];
             int t = a0 + lane;
-            // two terms per step: their loads are issued together
+            // four terms per step: their loads are issued together
+            for (; t + 96 < a1; t += 128) {
+                float tv[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) tv[q] = div_term(a, r0, r1, r2, t0, base + t + 32 * q);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float s = sh + tv[q];
+                    sl += (fabsf(sh) >= fabsf(tv[q])) ? (sh - s) + tv[q] : (tv[q] - s) + sh;
+                    sh = s;
+                }
+            }
             for (; t + 32 < a1; t += 64) {
                 const float t1 = div_term(a, r0, r1, r2, t0, base + t);
                 const float t2 = div_term(a, r0, r1, r2, t0, base + t + 32);

@@ -113,6 +113,19 @@ __device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok) {
     return *sh_ok != 0;
 }
 
+// per-thread partial dot product: a compensated float pair (Neumaier), exact to
+// about 2u|sum| + n u^2 sum|term| -- FP64 accuracy for a thread's few dozen rows
+// without FP64 arithmetic per row
+struct FSum {
+    float h = 0.f, l = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float t = h + v;
+        l += (fabsf(h) >= fabsf(v)) ? (h - t) + v : (v - t) + h;
+        h = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
 // per sibling group: first child of each of the parent's 27 neighbours (-1: none or a leaf)
 __global__ void k_group_table(NodeArrays nd, i64 ngroups, int* __restrict__ gn) {
     const i64 M = nd.M;
@@ -159,16 +172,16 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     };
 
     // x = 0, r = b  (the host-side initialisation of CG_CUDA.cuh:435-439)
-    double loc = 0;
+    FSum loc;
     for (i64 t = start; t < dp.n; t += stride) {
         const i64 i = dp.lo + t;
         const float bi = a.b[i];
         a.x[i] = 0.f;
         a.r[i] = bi;
-        loc += (double)(bi * bi);
+        loc.add(bi * bi);
     }
     bool ok = true;
-    const double bb = preduce(loc, ok);   // ||b||^2 in double (relative mode)
+    const double bb = preduce(loc.value(), ok);   // ||b||^2 in double (relative mode)
     float r1 = (float)bb;
     float r0 = 0.f;
     int k = 1;
@@ -183,7 +196,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
         const float beta = first ? 0.f : r1 / r0;
         auto pdir = [&](i64 i) -> float { return first ? a.r[i] : fmaf(beta, pold[i], a.r[i]); };
         // q = A p, partial p.q
-        loc = 0;
+        loc = FSum();
         if (d == 0) {
             for (i64 t = start; t < dp.n; t += stride) {
                 const i64 i = dp.lo + t;
@@ -196,7 +209,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                 const float pi = pdir(i);
                 pnew[i] = pi;
                 a.q[i] = o;
-                loc += (double)(pi * o);
+                loc.add(pi * o);
             }
         } else {
             // one warp per CG_WARP_TILES tiles of 4 groups (32 rows each); warps run independently.
@@ -242,16 +255,16 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                         const float pi = blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
                         pnew[dp.lo + 8 * g + ch] = pi;
                         a.q[dp.lo + 8 * g + ch] = o;
-                        loc += (double)(pi * o);
+                        loc.add(pi * o);
                     }
                 }
             }
         }
-        const double pq = preduce(loc, ok);
+        const double pq = preduce(loc.value(), ok);
         if (!ok) break;
         const float al = (float)((double)r1 / pq);
         const float nal = -al;
-        loc = 0;
+        loc = FSum();
         {
             // four rows per thread per step, loads first (independent requests in flight)
             i64 t = start;
@@ -268,7 +281,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                     a.x[i] = fmaf(al, pv[u], xv[u]);
                     const float ri = fmaf(nal, qv[u], rv[u]);
                     a.r[i] = ri;
-                    loc += (double)(ri * ri);
+                    loc.add(ri * ri);
                 }
             }
             for (; t < dp.n; t += stride) {
@@ -276,11 +289,11 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                 a.x[i] = fmaf(al, pnew[i], a.x[i]);
                 const float ri = fmaf(nal, a.q[i], a.r[i]);
                 a.r[i] = ri;
-                loc += (double)(ri * ri);
+                loc.add(ri * ri);
             }
         }
         r0 = r1;
-        r1 = (float)preduce(loc, ok);
+        r1 = (float)preduce(loc.value(), ok);
         ++k;
         pold = pnew;
         pnew = (pnew == a.p) ? a.p2 : a.p;
