@@ -29,7 +29,11 @@ def _torus(n, seed=0):
 NODE_FIELDS = ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum", "point_node")
 
 
-@pytest.fixture(scope="module", params=[("sphere", 5000, 6), ("torus", 30000, 7)], ids=["sphere5k-d6", "torus30k-d7"])
+# torus30k-d8 has subdivided leaves of every lattice edge from 2 to 64 (bricks of 8^3 cells, their
+# 4^3-brick super-bricks, and the small single-brick leaves), adjacent leaves of the same depth
+# batch (corners owned by another leaf) and culled bricks next to live ones
+@pytest.fixture(scope="module", params=[("sphere", 5000, 6), ("torus", 30000, 7), ("torus", 30000, 8)],
+                ids=["sphere5k-d6", "torus30k-d7", "torus30k-d8"])
 def staged(request, lib_built, oracle_mod):
     import poissonrecon_gpu_gb300 as pg
     kind, n, depth = request.param
