@@ -95,6 +95,19 @@ int prgpu_get_mesh(void* ctx, prgpu_mesh* out);
  * without file I/O. */
 int prgpu_reconstruct(void* ctx, const float* xyz, const float* nrm, int64_t n, prgpu_mesh* out);
 
+/* Several point clouds, one after the other on the context's stream: cloud k is
+ * points [offsets[k], offsets[k+1]) of xyz/nrm, reconstructed at maxDepth
+ * depths[k] (the context's depth when depths is NULL).  outs[k] receives a copy
+ * of the mesh in memory the caller releases with prgpu_mesh_free.  The reference
+ * has no counterpart (one cloud per process run, main.cu:3247-4573); it is the
+ * batched form of prgpu_reconstruct.  On error, the meshes already produced are
+ * released and the error names the cloud. */
+int prgpu_reconstruct_batch(void* ctx, const float* xyz, const float* nrm, const int64_t* offsets,
+                            const int32_t* depths, int32_t ncloud, prgpu_mesh* outs);
+
+/* Releases a mesh returned by prgpu_reconstruct_batch and zeroes it. */
+int prgpu_mesh_free(prgpu_mesh* mesh);
+
 /* Copy an internal array to host memory.  Names: "key","pidx","pnum","parent",
  * "children","neighs","didx","dnum","base","count","points","normals",
  * "point_node","vfield","divergence","x","point_value","stencil","cg_iters",

@@ -75,6 +75,8 @@ SIGNATURES = {
     "prgpu_extract_mesh": (ctypes.c_int, [_VP]),
     "prgpu_get_mesh": (ctypes.c_int, [_VP, ctypes.POINTER(Mesh)]),
     "prgpu_reconstruct": (ctypes.c_int, [_VP, _VP, _VP, _I64, ctypes.POINTER(Mesh)]),
+    "prgpu_reconstruct_batch": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int32, ctypes.POINTER(Mesh)]),
+    "prgpu_mesh_free": (ctypes.c_int, [ctypes.POINTER(Mesh)]),
     "prgpu_get_array": (ctypes.c_int, [_VP, ctypes.c_char_p, _VP, _I64, ctypes.POINTER(_I64)]),
     "prgpu_set_array": (ctypes.c_int, [_VP, ctypes.c_char_p, _VP, _I64]),
     "prgpu_stats_json": (ctypes.c_int, [_VP, ctypes.c_char_p, _I64]),
@@ -190,6 +192,29 @@ class Reconstructor:
         self.eval_points()
         self.extract_mesh()
         return self.mesh()
+
+    def reconstruct_batch(self, clouds, depths=None):
+        """Reconstruct several (xyz, nrm) clouds in one call (prgpu_reconstruct_batch);
+        returns a list of (vertices, triangles)."""
+        xyz = np.ascontiguousarray(np.concatenate([np.asarray(c[0], np.float32).reshape(-1, 3) for c in clouds]))
+        nrm = np.ascontiguousarray(np.concatenate([np.asarray(c[1], np.float32).reshape(-1, 3) for c in clouds]))
+        offsets = np.zeros(len(clouds) + 1, np.int64)
+        offsets[1:] = np.cumsum([len(c[0]) for c in clouds])
+        dep = None if depths is None else np.ascontiguousarray(depths, dtype=np.int32)
+        outs = (Mesh * max(len(clouds), 1))()
+        _check(_lib().prgpu_reconstruct_batch(self._h, xyz.ctypes.data, nrm.ctypes.data, offsets.ctypes.data,
+                                              None if dep is None else dep.ctypes.data, len(clouds), outs),
+               "prgpu_reconstruct_batch")
+        result = []
+        for k in range(len(clouds)):
+            m = outs[k]
+            v = np.ctypeslib.as_array(m.vertices, shape=(m.n_vertices * 3,)).reshape(-1, 3).copy() \
+                if m.n_vertices else np.zeros((0, 3), np.float32)
+            f = np.ctypeslib.as_array(m.triangles, shape=(m.n_triangles * 3,)).reshape(-1, 3).copy() \
+                if m.n_triangles else np.zeros((0, 3), np.int32)
+            _lib().prgpu_mesh_free(ctypes.byref(m))
+            result.append((v, f))
+        return result
 
     # ---- arrays
     def get(self, name: str) -> np.ndarray:

@@ -295,6 +295,69 @@ int prgpu_reconstruct(void* h, const float* xyz, const float* nrm, int64_t n, pr
     return PRGPU_OK;
 }
 
+int prgpu_mesh_free(prgpu_mesh* m) {
+    if (!m) return PRGPU_ERR_ARG;
+    free((void*)m->vertices);
+    free((void*)m->triangles);
+    m->vertices = nullptr;
+    m->triangles = nullptr;
+    m->n_vertices = m->n_triangles = 0;
+    return PRGPU_OK;
+}
+
+int prgpu_reconstruct_batch(void* h, const float* xyz, const float* nrm, const int64_t* offsets,
+                            const int32_t* depths, int32_t ncloud, prgpu_mesh* outs) {
+    Ctx* c = as_ctx(h);
+    if (!c || !xyz || !nrm || !offsets || !outs || ncloud < 0) {
+        set_last_error("prgpu_reconstruct_batch: invalid argument");
+        return PRGPU_ERR_ARG;
+    }
+    for (int k = 0; k < ncloud; ++k) {
+        outs[k].vertices = nullptr;
+        outs[k].triangles = nullptr;
+        outs[k].n_vertices = outs[k].n_triangles = 0;
+    }
+    const int D0 = c->D;
+    int rc = PRGPU_OK;
+    for (int k = 0; k < ncloud && rc == PRGPU_OK; ++k) {
+        const int64_t n = offsets[k + 1] - offsets[k];
+        const int d = depths ? depths[k] : D0;
+        if (n <= 0 || offsets[k] < 0 || d < 2 || d > 15) {
+            set_last_error("prgpu_reconstruct_batch: cloud %d: %lld points at depth %d", k, (long long)n, d);
+            rc = PRGPU_ERR_ARG;
+            break;
+        }
+        c->D = d;
+        prgpu_mesh m;
+        rc = prgpu_reconstruct(h, xyz + 3 * offsets[k], nrm + 3 * offsets[k], n, &m);
+        if (rc) {
+            char msg[512];
+            snprintf(msg, sizeof msg, "%s", last_error());
+            set_last_error("prgpu_reconstruct_batch: cloud %d: %s", k, msg);
+            break;
+        }
+        float* vv = (float*)malloc(sizeof(float) * 3 * (size_t)std::max<int64_t>(m.n_vertices, 1));
+        int32_t* ff = (int32_t*)malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(m.n_triangles, 1));
+        if (!vv || !ff) {
+            free(vv);
+            free(ff);
+            set_last_error("prgpu_reconstruct_batch: cloud %d: host allocation failed", k);
+            rc = PRGPU_ERR_NOMEM;
+            break;
+        }
+        memcpy(vv, m.vertices, sizeof(float) * 3 * (size_t)m.n_vertices);
+        memcpy(ff, m.triangles, sizeof(int32_t) * 3 * (size_t)m.n_triangles);
+        outs[k].vertices = vv;
+        outs[k].triangles = ff;
+        outs[k].n_vertices = m.n_vertices;
+        outs[k].n_triangles = m.n_triangles;
+    }
+    c->D = D0;
+    if (rc)
+        for (int k = 0; k < ncloud; ++k) prgpu_mesh_free(&outs[k]);
+    return rc;
+}
+
 // ----------------------------- array access ---------------------------------
 namespace {
 __global__ void k_expand_children(const int* __restrict__ child0, i64 M, int* __restrict__ out) {

@@ -216,3 +216,26 @@ def test_cg_csr_matches_dense_solve(lib_built):
     x = np.linalg.solve(A, b.astype(np.float64))
     assert it > 0 and ms > 0
     assert np.abs(tx.cpu().numpy() - x).max() <= 1e-4 * np.abs(x).max()
+
+
+def test_reconstruct_batch_matches_single(lib_built):
+    """prgpu_reconstruct_batch: clouds of different sizes and depths in one call give the meshes of
+    separate reconstructions; a bad cloud is reported by index and nothing leaks."""
+    import poissonrecon_gpu_gb300 as pg
+    clouds = [sphere(3000, seed=4), _torus(6000, seed=6), sphere(1500, seed=8)]
+    depths = [5, 6, 4]
+    single = []
+    for (xyz, nrm), d in zip(clouds, depths):
+        r = pg.Reconstructor(depth=d)
+        single.append(r.reconstruct(xyz, nrm))
+        r.close()
+    r = pg.Reconstructor(depth=7)
+    batch = r.reconstruct_batch(clouds, depths)
+    for (v1, f1), (v2, f2) in zip(single, batch):
+        assert np.array_equal(v1, v2) and np.array_equal(f1, f2)
+    with pytest.raises(pg.PrgpuError, match="cloud 1"):
+        r.reconstruct_batch([clouds[0], clouds[1]], [5, 1])
+    # the context keeps its own depth
+    v, f = r.reconstruct(*clouds[0])
+    assert len(f) > 0
+    r.close()
