@@ -176,6 +176,15 @@ def measured_traffic(args):
     return out
 
 
+def max_over_ranks(values, device):
+    """Replicas: every rank times its own reconstruction; the job's time is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def roofline(stats, peaks, traffic):
     ks = stats.get("kernels", {})
     if not ks:
@@ -278,9 +287,7 @@ def main():
     t_dev = float(np.mean(dev_ms))
     t_e2e = float(np.mean(e2e_ms))
     if world > 1:
-        t = torch.tensor([t_dev, t_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev, t_e2e = float(t[0]), float(t[1])
+        t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], dev)
     if rank != 0:
         return
     out = {
