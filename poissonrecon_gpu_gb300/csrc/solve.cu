@@ -43,6 +43,18 @@ struct PartState {          // one per depth, in global memory, zero-initialised
     int pad;
 };
 
+// reduction barrier of one depth's partition in k_cg_all: arrival counter, release
+// generation and result on separate cache lines (the blocks poll 'gen' while the
+// last one sums)
+struct alignas(128) PartSync {
+    unsigned count;
+    unsigned pad0[31];
+    unsigned gen;
+    unsigned pad1[31];
+    double res[2];
+    double pad2[14];
+};
+
 struct CgDepth {
     i64 lo, n;              // global row range
     int first_block, nblocks;
@@ -66,6 +78,8 @@ struct CgArgs {
     float* p2;
     float* q;
     PartState* state;
+    PartSync* sync;         // one per depth
+    double* partial;        // one per block
     int* err;
 };
 
@@ -113,6 +127,54 @@ __device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok) {
     return *sh_ok != 0;
 }
 
+// sum of v over the blocks of a partition, returned to every thread: each block
+// stores its partial, the last to arrive sums them all in a fixed order (so the
+// result does not depend on arrival order) and releases the others.  Waits spin
+// with a limit; on expiry the error flag is set and false returned.
+__device__ double part_reduce(PartSync* ps, double* partial, int first_block, int nblocks, int slot, double v,
+                              int* err, double* sh, int* sh_flag, double* sh_val, bool& ok) {
+    const double s = block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = s;
+        __threadfence();
+        const unsigned g = *(volatile unsigned*)&ps->gen;
+        const unsigned arrived = atomicAdd(&ps->count, 1u);
+        sh_flag[0] = (arrived == (unsigned)nblocks - 1) ? 1 : 0;
+        sh_flag[1] = (int)g;
+    }
+    __syncthreads();
+    if (sh_flag[0]) {
+        __threadfence();
+        double t = 0.0;
+        for (int k = threadIdx.x; k < nblocks; k += blockDim.x) t += *(volatile double*)&partial[first_block + k];
+        t = block_sum(t, sh);
+        if (threadIdx.x == 0) {
+            ps->res[slot] = t;
+            atomicExch(&ps->count, 0u);
+            __threadfence();
+            atomicAdd(&ps->gen, 1u);
+            *sh_val = t;
+            sh_flag[2] = 1;
+        }
+    } else if (threadIdx.x == 0) {
+        const unsigned g = (unsigned)sh_flag[1];
+        volatile unsigned* vgen = &ps->gen;
+        long long spins = 0;
+        int good = 1;
+        while (*vgen == g) {
+            if (++spins > SPIN_LIMIT || *(volatile int*)err) { good = 0; break; }
+            __nanosleep(64);
+        }
+        __threadfence();
+        if (!good) atomicExch(err, PRGPU_ERR_TIMEOUT);
+        *sh_val = *(volatile double*)&ps->res[slot];
+        sh_flag[2] = good && !*(volatile int*)err;
+    }
+    __syncthreads();
+    ok = sh_flag[2] != 0;
+    return *sh_val;
+}
+
 // per-thread partial dot product: a compensated float pair (Neumaier), exact to
 // about 2u|sum| + n u^2 sum|term| -- FP64 accuracy for a thread's few dozen rows
 // without FP64 arithmetic per row
@@ -146,7 +208,6 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     __shared__ float sp[CG_TILE_GROUPS * 64 * CG_WARP_TILES];
     __shared__ float sst[27];
     __shared__ double sh[CG_BLOCK / 32];
-    __shared__ int sh_ok;
     __shared__ double sh_val;
     const int d = block_depth[blockIdx.x];
     const CgDepth& dp = deps[d];
@@ -159,14 +220,10 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     int red = 0;   // reduction counter selects the accumulator slot
 
     // reduce a per-thread double over the partition; every thread gets the sum
+    __shared__ int sh_flag[3];
     auto preduce = [&](double v, bool& ok) -> double {
-        double s = block_sum(v, sh);
-        if (threadIdx.x == 0) atomicAdd(&ps->acc[red % 3], s);
-        ok = part_barrier(ps, dp.nblocks, a.err, &sh_ok);
-        if (threadIdx.x == 0) sh_val = *(volatile double*)&ps->acc[red % 3];
-        __syncthreads();
-        double res = sh_val;
-        if (rank == 0 && threadIdx.x == 0) ps->acc[(red + 2) % 3] = 0.0;
+        const double res = part_reduce(&a.sync[d], a.partial, dp.first_block, dp.nblocks, red & 1, v, a.err, sh,
+                                       sh_flag, &sh_val, ok);
         ++red;
         return res;
     };
@@ -370,6 +427,9 @@ void stage_solve(Ctx& c) {
     CgDepth* ddeps = dalloc<CgDepth>(D + 1, s);
     int* dbd = dalloc<int>((i64)block_depth.size(), s);
     PartState* st = dalloc<PartState>(D + 1, s);
+    PartSync* psync = dalloc<PartSync>(D + 1, s);
+    double* partial = dalloc<double>((i64)block_depth.size(), s);
+    CK(cudaMemsetAsync(psync, 0, (D + 1) * sizeof(PartSync), s));
     int* err = dalloc<int>(1, s);
     CK(cudaMemcpyAsync(ddeps, deps.data(), (D + 1) * sizeof(CgDepth), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(dbd, block_depth.data(), block_depth.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -393,6 +453,8 @@ void stage_solve(Ctx& c) {
     a.p2 = p2;
     a.q = q;
     a.state = st;
+    a.sync = psync;
+    a.partial = partial;
     a.err = err;
     void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
     const int kt = c.kbegin("cg", 0.0);
@@ -416,7 +478,7 @@ void stage_solve(Ctx& c) {
         c.kpending[kt].bytes = bytes;
     }
     dfree(r, s); dfree(p, s); dfree(p2, s); dfree(q, s); dfree(gn, s);
-    dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(err, s);
+    dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(psync, s); dfree(partial, s); dfree(err, s);
     if (herr) {
         set_last_error("solver barrier timed out");
         throw Error{PRGPU_ERR_TIMEOUT, {0}};
