@@ -304,7 +304,8 @@ def main():
         "cg_iters": stats.get("cg_iters"),
         "kernels": stats.get("kernels"),
         "subdivision": {k: stats.get(k) for k in ("roots_per_depth", "virtual_cells", "bricks", "live_bricks",
-                                                  "foreign_corners", "foreign_evaluated")},
+                                                  "foreign_corners", "foreign_evaluated", "super_bricks",
+                                                  "super_decided")},
         "nodes": stats.get("nodes"),
         "mesh": {"vertices": nv, "triangles": nt},
     }

@@ -493,7 +493,7 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
     Ctx* c = as_ctx(h);
     if (!c || !buf || len <= 0) return PRGPU_ERR_ARG;
     std::string js = "{";
-    char tmp[256];
+    char tmp[1024];
     snprintf(tmp, sizeof tmp, "\"points\":%lld,\"depth\":%d,\"nodes\":%lld,", (long long)c->N, c->D,
              (long long)c->nodes.M);
     js += tmp;
@@ -509,9 +509,10 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
     }
     snprintf(tmp, sizeof tmp,
              "],\"virtual_cells\":%lld,\"bricks\":%lld,\"live_bricks\":%lld,\"foreign_corners\":%lld,"
-             "\"foreign_evaluated\":%lld,\"kernel_launches\":%llu",
+             "\"foreign_evaluated\":%lld,\"super_bricks\":%lld,\"super_decided\":%lld,\"kernel_launches\":%llu",
              (long long)c->virtual_cells, (long long)c->total_bricks, (long long)c->live_bricks,
-             (long long)c->foreign_corners, (long long)c->foreign_slow,
+             (long long)c->foreign_corners, (long long)c->foreign_slow, (long long)c->super_bricks,
+             (long long)c->super_decided,
              (unsigned long long)g_kernel_launches);
     js += tmp;
     js += ",\"cg_iters\":[";

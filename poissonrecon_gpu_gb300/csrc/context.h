@@ -127,6 +127,7 @@ struct Ctx {
     i64 total_bricks = 0, live_bricks = 0;   // subdivided leaves: bricks, and those not culled
     i64 foreign_corners = 0;                 // brick corners owned by another leaf of the batch
     i64 foreign_slow = 0;                    // of those, evaluated because the owner's brick was culled
+    i64 super_bricks = 0, super_decided = 0; // 4^3-brick groups bounded first, and those proven (profiling)
 
     StageTimes t;
     bool profile = false;

@@ -858,6 +858,11 @@ __device__ __forceinline__ float brick_bt(const EvalArgs& a, int r, int Lc_ax, i
     return a.lb[lattice_basis_offset(a.D, d) + (i64)n * (3 * w + 1) + kk];
 }
 
+// a / n for 0 <= a < 2^14 and 1 <= n <= 2^10 through the reciprocal inv = 1/n:
+// (a + 0.5)/n lies at least 0.5/n from an integer and the float product is
+// within 2^-9 of it, so truncation gives the quotient
+__device__ __forceinline__ int small_div(int a, float inv) { return __float2int_rz(((float)a + 0.5f) * inv); }
+
 // the part of a window box [wlo, wlo+ext) outside the leaf's box [llo, llo+span)
 // (per axis, at one depth) as at most 6 disjoint boxes
 struct Box3 {
@@ -1066,8 +1071,10 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, const i64* __restr
             for (int q = 0; q < nbx; ++q) {
                 const Box3& bx = bxs[q];
                 const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+                const float inv12 = 1.0f / (float)n12, inv2 = 1.0f / (float)bx.n[2];
                 for (int t = lane; t < ncell; t += 32) {
-                    const int i0 = t / n12, rem = t - i0 * n12, i1 = rem / bx.n[2], i2 = rem - i1 * bx.n[2];
+                    const int i0 = small_div(t, inv12), rem = t - i0 * n12, i1 = small_div(rem, inv2),
+                              i2 = rem - i1 * bx.n[2];
                     const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
                     const i64 node = shell_node(v, L, r, Lc, d, N);
                     if (node < 0) continue;
@@ -1169,8 +1176,10 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             for (int q = 0; q < nbx; ++q) {
                 const Box3& bx = bxs[q];
                 const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+                const float inv12 = 1.0f / (float)n12, inv2 = 1.0f / (float)bx.n[2];
                 for (int t = lane; t < ncell; t += 32) {
-                    const int i0 = t / n12, rem = t - i0 * n12, i1 = rem / bx.n[2], i2 = rem - i1 * bx.n[2];
+                    const int i0 = small_div(t, inv12), rem = t - i0 * n12, i1 = small_div(rem, inv2),
+                              i2 = rem - i1 * bx.n[2];
                     const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
                     const i64 node = shell_node(v, L, r, Lc, d, N);
                     if (node < 0) continue;
@@ -1398,8 +1407,10 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
             for (int q = 0; q < nbx; ++q) {
                 const Box3& bx = bxs[q];
                 const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+                const float inv12 = 1.0f / (float)n12, inv2 = 1.0f / (float)bx.n[2];
                 for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-                    const int i0 = t / n12, rem = t - i0 * n12, i1 = rem / bx.n[2], i2 = rem - i1 * bx.n[2];
+                    const int i0 = small_div(t, inv12), rem = t - i0 * n12, i1 = small_div(rem, inv2),
+                              i2 = rem - i1 * bx.n[2];
                     const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
                     const i64 node = shell_node(v, L, r, Lc, d, N);
                     if (node >= 0)
@@ -1981,6 +1992,14 @@ void stage_mesh(Ctx& c) {
             k_super_bound<<<grid_for(nsuper * 32, 256, (i64)c.sms * 8), 256, 0, s>>>(va, dspre, dsrpre, nr, srows, xl,
                                                                                     nsuper, ssign);
             CK_LAUNCH();
+            if (c.profile) {   // statistics only
+                std::vector<signed char> hs(nsuper);
+                CK(cudaMemcpyAsync(hs.data(), ssign, nsuper, cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                c.super_bricks = nsuper;
+                c.super_decided = 0;
+                for (signed char v : hs) c.super_decided += (v != 0);
+            }
         }
         // bricks of leaves with lattice edge >= 16 come first (roots are in depth order)
         i64 nbig = 0;
