@@ -24,6 +24,7 @@ void Ctx::free_nodes() {
     dfree(nodes.key, s); dfree(nodes.pidx, s); dfree(nodes.pnum, s); dfree(nodes.didx, s);
     dfree(nodes.dnum, s); dfree(nodes.parent, s); dfree(nodes.child0, s); dfree(nodes.depth, s);
     dfree(nodes.neigh, s);
+    dfree(gn, s);
     nodes.M = 0;
 }
 void Ctx::free_all() {

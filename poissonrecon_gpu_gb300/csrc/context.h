@@ -124,6 +124,7 @@ struct Ctx {
     std::vector<i64> batch_tri;
     std::vector<i64> roots_per_depth;   // subdivided leaves by depth
     i64 virtual_cells = 0;
+    int* gn = nullptr;                  // sibling-group table (ensure_group_table), freed with the nodes
     i64 total_bricks = 0, live_bricks = 0;   // subdivided leaves: bricks, and those not culled
     i64 foreign_corners = 0;                 // brick corners owned by another leaf of the batch
     i64 foreign_slow = 0;                    // of those, evaluated because the owner's brick was culled
@@ -152,6 +153,7 @@ void stage_full_tables(Ctx& c);
 void stage_splat(Ctx& c);
 void stage_divergence(Ctx& c);
 void stage_solve(Ctx& c);
+void ensure_group_table(Ctx& c);
 void stage_points(Ctx& c);
 void stage_mesh(Ctx& c);
 

@@ -121,6 +121,69 @@ __global__ void k_div_thread(NodeArrays nd, DivArgs a, i64 lo, i64 hi, float* __
     }
 }
 
+// finest depth by sibling groups: the 27 neighbours of the 8 children of a node
+// are the 4x4x4 block of the children of the parent's 27 neighbours (the solve's
+// group table).  One warp stages the V of the blocks of 4 groups in shared
+// memory; each row then sums its 27 terms in neighbour order in FP64, as
+// k_div_thread does.  Every finest node has exactly one finest descendant
+// (itself), and the neighbour at offset j = (jx,jy,jz) reads the row entries
+// jx, jy, jz of the node's 3-entry rows.
+__global__ void __launch_bounds__(256) k_div_finest(NodeArrays nd, DivArgs a, const int* __restrict__ gn,
+                                                    i64 ngroups_all, i64 gfirst, i64 ng, i64 lo,
+                                                    float* __restrict__ out) {
+    __shared__ float4 cells[8][4 * 64];   // per warp: V of the 4x4x4 block of 4 groups, w = 1 if the cell exists
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int ch = lane & 7, gl = lane >> 3;
+    const int sx = ch >> 2, sy = (ch >> 1) & 1, sz = ch & 1;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    float4* blk = cells[wib];
+    for (i64 tile = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile * 4 < ng; tile += nwarps) {
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int e = lane + 32 * m;
+            const i64 g = tile * 4 + (e >> 6);
+            const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
+            float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (g < ng) {
+                const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
+                const int cn = gn[(i64)jp * ngroups_all + gfirst + g];
+                if (cn != -1) {
+                    const i64 o = cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)) - lo;
+                    val = make_float4(a.vfield[3 * o], a.vfield[3 * o + 1], a.vfield[3 * o + 2], 1.f);
+                }
+            }
+            blk[e] = val;
+        }
+        __syncwarp();
+        const i64 g = tile * 4 + gl;
+        if (g < ng) {
+            const i64 i = lo + 8 * g + ch;
+            int xyz[3];
+            key_coords(nd.key[i], a.D, a.D, xyz);
+            const float* rr = a.rows + a.row_start[a.D];
+            float R[3][3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+                for (int t = 0; t < 3; ++t) R[ax][t] = rr[xyz[ax] * 3 + t];
+            const float4* b = blk + gl * 64;
+            double val = 0.0;
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                const int jx = j / 9, jy = (j / 3) % 3, jz = j % 3;
+                const float4 c = b[(sx + jx) * 16 + (sy + jy) * 4 + (sz + jz)];
+                if (c.w == 0.f) continue;   // no neighbour
+                float t = c.x * R[0][jx];
+                t = fmaf(c.y, R[1][jy], t);
+                t = fmaf(c.z, R[2][jz], t);
+                val += (double)t;
+            }
+            out[i] = (float)val;
+        }
+    }
+}
+
 // nodes with many terms (depths < D-1): the node's terms, in neighbour order,
 // are cut into chunks of DIV_CHUNK; one warp sums a chunk and the chunk sums are
 // added per node in FP64 in chunk order (deterministic).  Within a chunk each
@@ -270,9 +333,21 @@ void stage_divergence(Ctx& c) {
     const int split = D >= 1 ? D - 1 : 0;
     // compulsory: every node's key, depth, neighbours and b; V and coordinates of the finest slots
     const int kt = c.kbegin("divergence", (double)M * (8 + 1 + 108 + 4) + (double)nD * (12 + 8));
-    k_div_thread<<<grid_for(M - c.base[split], 128, 1ll << 30), 128, 0, s>>>(c.nodes, a, c.base[split], M,
-                                                                             c.divergence);
+    // depth D - 1 one thread per node; depth D by sibling groups
+    const int kt1 = c.kbegin("divergence_d1", 0.0);
+    k_div_thread<<<grid_for(c.base[D] - c.base[split], 128, 1ll << 30), 128, 0, s>>>(c.nodes, a, c.base[split],
+                                                                                      c.base[D], c.divergence);
     CK_LAUNCH();
+    c.kend(kt1);
+    ensure_group_table(c);
+    const int kt2 = c.kbegin("divergence_d", 0.0);
+    {
+        const i64 ngroups_all = (M - 1) / 8, gfirst = (lo - 1) / 8, ng = nD / 8;
+        k_div_finest<<<grid_for(ng * 8, 256, (i64)c.sms * 8 * 8), 256, 0, s>>>(c.nodes, a, c.gn, ngroups_all, gfirst,
+                                                                               ng, lo, c.divergence);
+        CK_LAUNCH();
+    }
+    c.kend(kt2);
     const i64 nc = c.base[split];   // nodes at depths < D-1
     if (nc > 0) {
         int* nch = dalloc<int>(nc, s);

@@ -362,6 +362,17 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     }
 }
 
+// the sibling-group table of the current octree, built once
+void ensure_group_table(Ctx& c) {
+    if (c.gn) return;
+    const i64 ngroups = (c.nodes.M - 1) / 8;
+    c.gn = dalloc<int>(std::max<i64>(ngroups * 27, 1), c.stream);
+    if (ngroups > 0) {
+        k_group_table<<<grid_for(ngroups * 27, 256), 256, 0, c.stream>>>(c.nodes, ngroups, c.gn);
+        CK_LAUNCH();
+    }
+}
+
 void stage_solve(Ctx& c) {
     cudaStream_t s = c.stream;
     const int D = c.D;
@@ -374,11 +385,8 @@ void stage_solve(Ctx& c) {
     float* p2 = dalloc<float>(M, s);
     // sibling-group table for the matrix-vector products
     const i64 ngroups = (M - 1) / 8;
-    int* gn = dalloc<int>(std::max<i64>(ngroups * 27, 1), s);
-    if (ngroups > 0) {
-        k_group_table<<<grid_for(ngroups * 27, 256), 256, 0, s>>>(c.nodes, ngroups, gn);
-        CK_LAUNCH();
-    }
+    ensure_group_table(c);
+    const int* gn = c.gn;
     // co-resident capacity
     int dev = c.device, sms = 0, per_sm = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -477,7 +485,7 @@ void stage_solve(Ctx& c) {
         for (int d = 0; d <= D; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 8 * 4);
         c.kpending[kt].bytes = bytes;
     }
-    dfree(r, s); dfree(p, s); dfree(p2, s); dfree(q, s); dfree(gn, s);
+    dfree(r, s); dfree(p, s); dfree(p2, s); dfree(q, s);
     dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(psync, s); dfree(partial, s); dfree(err, s);
     if (herr) {
         set_last_error("solver barrier timed out");
