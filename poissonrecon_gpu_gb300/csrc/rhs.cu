@@ -184,9 +184,9 @@ __global__ void __launch_bounds__(256) k_div_finest(NodeArrays nd, DivArgs a, co
     }
 }
 
-// nodes with many terms (depths < D-1): the node's terms, in neighbour order,
+// the root (all finest nodes are its terms): the node's terms, in neighbour order,
 // are cut into chunks of DIV_CHUNK; one warp sums a chunk and the chunk sums are
-// added per node in FP64 in chunk order (deterministic).  Within a chunk each
+// added per node in FP64 in a fixed order (k_div_sum: deterministic).  Within a chunk each
 // lane keeps a compensated float pair (hi + lo, Neumaier's summation), whose
 // error is at most 2u|sum| + O(n u^2) sum|term| -- FP64 accuracy for these
 // lengths without FP64 arithmetic per term.
@@ -288,12 +288,147 @@ __global__ void __launch_bounds__(DIV_WARPS * 32) k_div_chunks(NodeArrays nd, Di
     }
 }
 
-__global__ void k_div_final(const int* __restrict__ nchunks, const int* __restrict__ first,
-                            const double* __restrict__ partial, i64 n, float* __restrict__ out) {
-    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-        double s = 0.0;
-        for (int c = 0; c < nchunks[i]; ++c) s += partial[first[i] + c];
-        out[i] = (float)s;
+// Depths 1..D-2 by sibling groups.  The 27-neighbourhoods of the 8 children of a
+// node are the 4x4x4 block of the children of the parent's 27 neighbours (the
+// group table), and in x-major block order every child meets its own neighbours
+// in neighbour order.  A group's terms are the finest descendants of the block's
+// cells, concatenated in block order and cut into chunks of DIV_CHUNK finest
+// nodes; one warp reads each finest node of a chunk once and adds its term to
+// every child whose neighbourhood holds the cell (1, 2, 4 or 8 children), each
+// child in its own compensated pair.  The term is the one k_div_chunks forms:
+// child b on an axis reads the row of coordinate 2P+b at offset c - (2P+b-1)S,
+// which is the row of 2P at offset (c - (2P-1)S) + 2bS.
+__device__ __forceinline__ void neu_add(float& sh, float& sl, float t) {
+    const float s = sh + t;
+    sl += (fabsf(sh) >= fabsf(t)) ? (sh - s) + t : (t - s) + sh;
+    sh = s;
+}
+
+__device__ __forceinline__ int group_cell_node(const int* __restrict__ gn, i64 ngroups_all, i64 g, int cell) {
+    const int bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
+    const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
+    const int cn = gn[(i64)jp * ngroups_all + g];
+    return cn == -1 ? -1 : cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1));
+}
+
+__global__ void k_div_group_count(NodeArrays nd, const int* __restrict__ gn, i64 ngroups_all, i64 ng,
+                                  int* __restrict__ nchunks) {
+    for (i64 g = (i64)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (i64)gridDim.x * blockDim.x) {
+        i64 T = 0;
+        for (int cell = 0; cell < 64; ++cell) {
+            const int n = group_cell_node(gn, ngroups_all, g, cell);
+            if (n != -1) T += nd.dnum[n];
+        }
+        nchunks[g] = (int)((T + DIV_CHUNK - 1) / DIV_CHUNK);
+    }
+}
+
+__global__ void __launch_bounds__(DIV_WARPS * 32) k_div_groups(NodeArrays nd, DivArgs a, const int* __restrict__ gn,
+                                                               i64 ngroups_all, const int* __restrict__ item_group,
+                                                               const int* __restrict__ first, i64 nitems,
+                                                               double* __restrict__ partial) {
+    __shared__ int pre[DIV_WARPS][65];
+    __shared__ int sidx[DIV_WARPS][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    for (i64 it = warp; it < nitems; it += nwarps) {
+        const i64 g = item_group[it];
+        const int chunk = (int)(it - first[g]);
+        // prefix of the block cells' finest-descendant counts, two cells per lane
+        int cnt[2], sx[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int n = group_cell_node(gn, ngroups_all, g, 2 * lane + q);
+            cnt[q] = n == -1 ? 0 : nd.dnum[n];
+            sx[q] = n == -1 ? 0 : nd.didx[n];
+        }
+        const int pair = cnt[0] + cnt[1];
+        int inc = pair;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        __syncwarp();
+        pre[w][2 * lane] = inc - pair;
+        pre[w][2 * lane + 1] = inc - pair + cnt[0];
+        sidx[w][2 * lane] = sx[0];
+        sidx[w][2 * lane + 1] = sx[1];
+        if (lane == 31) pre[w][64] = inc;
+        __syncwarp();
+        // child 0 of the group has the even coordinates 2P
+        const i64 i0 = 1 + 8 * g;
+        const int d = nd.depth[i0];
+        int xyz[3];
+        key_coords(nd.key[i0], d, a.D, xyz);
+        const int S = 1 << (a.D - d), W = 3 * S;
+        const float* R[3];
+        int t0[3];
+        const i64 rs = a.row_start[d];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            R[ax] = a.rows + rs + (i64)xyz[ax] * W;
+            t0[ax] = (xyz[ax] - 1) * S;
+        }
+        const int total = pre[w][64];
+        const int lo = chunk * DIV_CHUNK, hi = min(total, lo + DIV_CHUNK);
+        float sh[8], sl[8];
+#pragma unroll
+        for (int s = 0; s < 8; ++s) { sh[s] = 0.f; sl[s] = 0.f; }
+        // lanes run over the chunk across cell boundaries; each lane tracks its
+        // cell (empty cells are skipped by the prefix)
+        int j = 0;
+        while (j < 63 && pre[w][j + 1] <= lo + lane) ++j;
+        for (int t = lo + lane; t < hi; t += 32) {
+            while (pre[w][j + 1] <= t) ++j;
+            const i64 o = (i64)sidx[w][j] - pre[w][j] + t;
+            const int bx = j >> 4, by = (j >> 2) & 3, bz = j & 3;
+            // which children hold this cell, per axis: b = 0 for block 0..2, b = 1 for 1..3
+            const bool x0 = bx <= 2, x1 = bx >= 1, y0 = by <= 2, y1 = by >= 1, z0 = bz <= 2, z1 = bz >= 1;
+            const short4 c = a.fc[o];
+            const float vx = a.vfield[3 * o], vy = a.vfield[3 * o + 1], vz = a.vfield[3 * o + 2];
+            const int ox = c.x - t0[0], oy = c.y - t0[1], oz = c.z - t0[2];
+            const float ux0 = x0 ? R[0][ox] : 0.f, ux1 = x1 ? R[0][ox + 2 * S] : 0.f;
+            const float uy0 = y0 ? R[1][oy] : 0.f, uy1 = y1 ? R[1][oy + 2 * S] : 0.f;
+            const float uz0 = z0 ? R[2][oz] : 0.f, uz1 = z1 ? R[2][oz + 2 * S] : 0.f;
+            const float px[2] = {vx * ux0, vx * ux1};
+            const float uy[2] = {uy0, uy1}, uz[2] = {uz0, uz1};
+            const bool hx[2] = {x0, x1}, hy[2] = {y0, y1}, hz[2] = {z0, z1};
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                const int bsx = s >> 2, bsy = (s >> 1) & 1, bsz = s & 1;
+                if (hx[bsx] && hy[bsy] && hz[bsz]) {
+                    float term = fmaf(vy, uy[bsy], px[bsx]);
+                    term = fmaf(vz, uz[bsz], term);
+                    neu_add(sh[s], sl[s], term);
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            double val = (double)sh[s] + (double)sl[s];
+            for (int o = 16; o; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+            if (lane == 0) partial[it * 8 + s] = val;
+        }
+        __syncwarp();
+    }
+}
+
+// one warp per node: the node's chunk partials (per entity of `per` nodes, node
+// s of the entity at offset s) summed lane-strided in FP64 and then by a fixed
+// butterfly, so the result does not depend on the schedule
+__global__ void k_div_sum(const int* __restrict__ nchunks, const int* __restrict__ first,
+                          const double* __restrict__ partial, i64 lo, i64 hi, int per, float* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    for (i64 i = lo + (((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < hi; i += nwarps) {
+        const i64 g = (i - lo) / per;
+        const int s = (int)((i - lo) % per), n = nchunks[g];
+        const i64 f = first[g];
+        double v = 0.0;
+        for (int q = lane; q < n; q += 32) v += partial[(f + q) * per + s];
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) out[i] = (float)v;
     }
 }
 
@@ -339,7 +474,9 @@ void stage_divergence(Ctx& c) {
                                                                                       c.base[D], c.divergence);
     CK_LAUNCH();
     c.kend(kt1);
+    const int ktg = c.kbegin("group_table", 0.0);
     ensure_group_table(c);
+    c.kend(ktg);
     const int kt2 = c.kbegin("divergence_d", 0.0);
     {
         const i64 ngroups_all = (M - 1) / 8, gfirst = (lo - 1) / 8, ng = nD / 8;
@@ -350,23 +487,49 @@ void stage_divergence(Ctx& c) {
     c.kend(kt2);
     const i64 nc = c.base[split];   // nodes at depths < D-1
     if (nc > 0) {
-        int* nch = dalloc<int>(nc, s);
-        int* first = dalloc<int>(nc + 1, s);
-        k_div_count<<<grid_for(nc, 256), 256, 0, s>>>(c.nodes, nc, nch);
+        // the root: its terms in chunks; depths 1..D-2: sibling groups in chunks
+        const i64 ngroups_all = (M - 1) / 8, ngc = (nc - 1) / 8;
+        int* nch = dalloc<int>(1 + ngc, s);
+        int* first = dalloc<int>(1 + 1 + ngc + 1, s);
+        int* gfirst = first + 2;
+        k_div_count<<<1, 32, 0, s>>>(c.nodes, 1, nch);
         CK_LAUNCH();
-        exclusive_scan<int, int>(nch, first, nc, first + nc, s);
-        const i64 nitems = read_scalar(first + nc, s);
-        int* item_node = dalloc<int>(std::max<i64>(nitems, 1), s);
-        double* partial = dalloc<double>(std::max<i64>(nitems, 1), s);
-        k_div_items<<<grid_for(nc, 256), 256, 0, s>>>(nch, first, nc, item_node);
-        CK_LAUNCH();
-        if (nitems > 0) {
-            k_div_chunks<<<grid_for(nitems * 32, DIV_WARPS * 32, (i64)c.sms * 8), DIV_WARPS * 32, 0, s>>>(
-                c.nodes, a, item_node, first, nitems, partial);
+        exclusive_scan<int, int>(nch, first, 1, first + 1, s);
+        if (ngc > 0) {
+            k_div_group_count<<<grid_for(ngc, 256), 256, 0, s>>>(c.nodes, c.gn, ngroups_all, ngc, nch + 1);
+            CK_LAUNCH();
+            exclusive_scan<int, int>(nch + 1, gfirst, ngc, gfirst + ngc, s);
+        }
+        const i64 nroot = read_scalar(first + 1, s);
+        const i64 ngitems = ngc > 0 ? read_scalar(gfirst + ngc, s) : 0;
+        int* item_node = dalloc<int>(std::max<i64>(nroot + ngitems, 1), s);
+        double* partial = dalloc<double>(std::max<i64>(nroot + 8 * ngitems, 1), s);
+        const int ktr = c.kbegin("divergence_root", 0.0);
+        if (nroot > 0) {
+            k_div_items<<<1, 32, 0, s>>>(nch, first, 1, item_node);
+            CK_LAUNCH();
+            k_div_chunks<<<grid_for(nroot * 32, DIV_WARPS * 32, (i64)c.sms * 8), DIV_WARPS * 32, 0, s>>>(
+                c.nodes, a, item_node, first, nroot, partial);
             CK_LAUNCH();
         }
-        k_div_final<<<grid_for(nc, 256), 256, 0, s>>>(nch, first, partial, nc, c.divergence);
+        k_div_sum<<<1, 32, 0, s>>>(nch, first, partial, 0, 1, 1, c.divergence);
         CK_LAUNCH();
+        c.kend(ktr);
+        if (ngc > 0) {
+            int* item_group = item_node + nroot;
+            double* gpartial = partial + nroot;
+            k_div_items<<<grid_for(ngc, 256), 256, 0, s>>>(nch + 1, gfirst, ngc, item_group);
+            CK_LAUNCH();
+            if (ngitems > 0) {
+                const int kt3 = c.kbegin("divergence_groups", 0.0);
+                k_div_groups<<<grid_for(ngitems * 32, DIV_WARPS * 32, (i64)c.sms * 8), DIV_WARPS * 32, 0, s>>>(
+                    c.nodes, a, c.gn, ngroups_all, item_group, gfirst, ngitems, gpartial);
+                CK_LAUNCH();
+                c.kend(kt3);
+            }
+            k_div_sum<<<grid_for((nc - 1) * 32, 256), 256, 0, s>>>(nch + 1, gfirst, gpartial, 1, nc, 8, c.divergence);
+            CK_LAUNCH();
+        }
         dfree(nch, s);
         dfree(first, s);
         dfree(item_node, s);
