@@ -1720,6 +1720,42 @@ __global__ void k_root_list(NodeArrays nd, const int* __restrict__ is_root, cons
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
         if (is_root[i]) out[pos[i]] = make_int2((int)i, (int)nd.depth[i]);
 }
+// subdivision roots are in node order, hence in depth order: the index of the
+// first root at depth d is the root prefix at the first node of depth d, and
+// every per-root count (bricks, rows, batch) is a closed form of the depth
+struct DepthStarts {
+    i64 base[17];
+};
+__global__ void k_depth_firsts(const int* __restrict__ rpos, DepthStarts b, int D, int* __restrict__ out) {
+    const int d = threadIdx.x;
+    if (d <= D) out[d] = rpos[b.base[d]];
+}
+struct RootLayout {
+    int first[17];    // first root at depth d
+    int batch[17];    // batch of the roots at depth d >= 3
+    i64 off[4][17];   // bricks, brick rows, super-bricks, super rows of the roots above depth d
+    i64 per[4][17];   // the same per root at depth d
+};
+__global__ void k_make_roots(const int2* __restrict__ dr, int nr, int D, RootLayout L, VRoot* __restrict__ roots,
+                             i64* __restrict__ pre) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nr; k += gridDim.x * blockDim.x) {
+        const int2 r = dr[k];
+        const int d = r.y;
+        VRoot R;
+        R.node = r.x;
+        R.depth = d;
+        R.batch = d < 3 ? k + 1 : L.batch[d];   // one batch per root above depth 3, one per depth from 3
+        R.pad = 0;
+        roots[k] = R;
+        const i64 local = k - L.first[d];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pre[(i64)q * (nr + 1) + k] = L.off[q][d] + local * L.per[q][d];
+        if (k == 0)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) pre[(i64)q * (nr + 1) + nr] = L.off[q][D];
+    }
+}
+
 __global__ void k_key_heads(const u64* __restrict__ keys, i64 n, int* __restrict__ f) {
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
         f[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1 : 0;
@@ -1750,6 +1786,7 @@ void stage_mesh(Ctx& c) {
     const int D = c.D;
     const NodeArrays& nd = c.nodes;
     const i64 M = nd.M, lo = c.base[D], nD = c.count[D];
+    const int kx = c.kbegin("mesh_tables", 0.0);
     float* x27 = build_x27(c, lo);
     EvalArgs ea{c.nodes, D, c.basis, c.x, x27, x27 ? lo : 0, nullptr};
     float* lb = nullptr;
@@ -1760,6 +1797,7 @@ void stage_mesh(Ctx& c) {
         CK_LAUNCH();
         ea.lb = lb;
     }
+    c.kend(kx);
     // ---- finest corner values, categories
     float* cval = dalloc<float>(8 * nD, s);
     float* cell_v = dalloc<float>(8 * nD, s);
@@ -1849,42 +1887,55 @@ void stage_mesh(Ctx& c) {
         dfree(ccv, s);
     }
     dfree(fflag, s);
-    // subdivision roots in node order, compacted on the device
-    std::vector<int2> hroots;
+    int kg = c.kbegin("mesh_lists", 0.0);
+    // subdivision roots in node order, compacted on the device; the host reads only
+    // the index of the first root of every depth
+    int2* droot_list = nullptr;
+    int nr = 0;
+    RootLayout layout{};
+    i64 tot[4] = {0, 0, 0, 0}, nbig = 0;
+    int nbatches = 1;
     {
         int* rpos = dalloc<int>(nCoarse + 1, s);
         exclusive_scan<int, int>(is_root, rpos, nCoarse, rpos + nCoarse, s);
-        const i64 nr = read_scalar(rpos + nCoarse, s);
-        int2* dr = dalloc<int2>(std::max<i64>(nr, 1), s);
-        k_root_list<<<grid_for(nCoarse, 256), 256, 0, s>>>(nd, is_root, rpos, nCoarse, dr);
+        DepthStarts ds{};
+        for (int d = 0; d <= D; ++d) ds.base[d] = c.base[d];
+        int* dfirst = dalloc<int>(D + 1, s);
+        k_depth_firsts<<<1, 32, 0, s>>>(rpos, ds, D, dfirst);
         CK_LAUNCH();
-        hroots.resize(nr);
-        if (nr > 0) CK(cudaMemcpyAsync(hroots.data(), dr, nr * sizeof(int2), cudaMemcpyDeviceToHost, s));
+        int hfirst[17];
+        CK(cudaMemcpyAsync(hfirst, dfirst, (D + 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+        dfree(dfirst, s);
+        nr = hfirst[D];   // roots are coarse nodes (depth < D)
+        droot_list = dalloc<int2>(std::max(nr, 1), s);
+        k_root_list<<<grid_for(nCoarse, 256), 256, 0, s>>>(nd, is_root, rpos, nCoarse, droot_list);
+        CK_LAUNCH();
         dfree(rpos, s);
-        dfree(dr, s);
+        c.roots_per_depth.assign(D + 1, 0);
+        int nb = 0;
+        for (int d = 0; d <= D; ++d) {
+            const int cnt = d < D ? hfirst[d + 1] - hfirst[d] : 0;
+            c.roots_per_depth[d] = cnt;
+            const int S = 1 << (D - d), E = std::min(S, BR), nbk = S / E;
+            const int ns = (D - d >= 6) ? S / (4 * BR) : 0;
+            layout.first[d] = hfirst[d];
+            layout.per[0][d] = (i64)nbk * nbk * nbk;
+            layout.per[1][d] = 3 * nbk;
+            layout.per[2][d] = (i64)ns * ns * ns;
+            layout.per[3][d] = 3 * ns;
+            for (int q = 0; q < 4; ++q) {
+                layout.off[q][d] = tot[q];
+                tot[q] += (i64)cnt * layout.per[q][d];
+            }
+            if (D - d >= 4) nbig = tot[0];   // bricks of leaves with lattice edge >= 16 come first
+            if (d < 3) nb += cnt;
+            else if (cnt > 0) layout.batch[d] = ++nb;
+        }
+        nbatches = nb + 1;
     }
     dfree(is_root, s);
-    // batches: one per root above depth 3, one per depth from 3
-    std::vector<VRoot> roots;
-    int nb = 0;
-    std::vector<int> depth_batch(D + 1, 0);
-    for (const int2& hr : hroots) {
-        VRoot R;
-        R.node = hr.x;
-        R.depth = hr.y;
-        R.pad = 0;
-        if (R.depth < 3) R.batch = ++nb;
-        else {
-            if (!depth_batch[R.depth]) depth_batch[R.depth] = ++nb;
-            R.batch = depth_batch[R.depth];
-        }
-        roots.push_back(R);
-    }
-    c.subdivide_roots = (i64)roots.size();
-    c.roots_per_depth.assign(D + 1, 0);
-    for (auto& R : roots) c.roots_per_depth[R.depth]++;
-    const int nbatches = nb + 1;
+    c.subdivide_roots = nr;
     // ---- real cells: active list, triangle bases
     int* flags = dalloc<int>(std::max<i64>(nD, 1), s);
     int* fpos = dalloc<int>(nD + 1, s);
@@ -1906,6 +1957,7 @@ void stage_mesh(Ctx& c) {
     const i64 ntri_real = read_scalar(tri_real + nact_real, s);
     dfree(flags, s);
     dfree(fpos, s);
+    c.kend(kg);
     // ---- virtual cells: every subdivided leaf cut into bricks, bounded and culled
     // before evaluation
     i64 ntri_virt = 0, nact_virt = 0, total_cells = 0;
@@ -1923,40 +1975,22 @@ void stage_mesh(Ctx& c) {
     VArgs va;
     va.e = ea;
     va.iso = c.iso;
-    va.nroots = (int)roots.size();
+    va.nroots = nr;
     VirtCells vc{};
-    if (!roots.empty()) {
-        const int nr = (int)roots.size();
+    if (nr > 0) {
+        kg = c.kbegin("mesh_lists", 0.0);
         droots = dalloc<VRoot>(nr, s);
         bflag = dalloc<int>(M, s);
-        CK(cudaMemcpyAsync(droots, roots.data(), nr * sizeof(VRoot), cudaMemcpyHostToDevice, s));
+        // prefix tables: bricks, brick rows, super-bricks, super rows (nr + 1 entries each)
+        i64* dpre = dalloc<i64>(4 * ((i64)nr + 1), s);
+        k_make_roots<<<grid_for(nr, 256), 256, 0, s>>>(droot_list, nr, D, layout, droots, dpre);
+        CK_LAUNCH();
         CK(cudaMemsetAsync(bflag, 0, M * sizeof(int), s));
         k_batch_flags<<<grid_for(nr, 256), 256, 0, s>>>(droots, nr, bflag);
         CK_LAUNCH();
         va.roots = droots;
         va.batch_root_flag = bflag;
-        // bricks and brick rows, numbered root by root (prefix table: 2 x 8 bytes per root)
-        // prefix tables: bricks, brick rows, super-bricks, super rows (nr + 1 entries each)
-        std::vector<i64> pre(4 * ((i64)nr + 1));
-        i64 nbricks = 0, nrows = 0, nsuper = 0, nsrows = 0;
-        for (int k = 0; k < nr; ++k) {
-            const int S = 1 << (D - roots[k].depth), E = std::min(S, BR), nbk = S / E;
-            const int ns = (D - roots[k].depth >= 6) ? S / (4 * BR) : 0;
-            pre[k] = nbricks;
-            pre[(nr + 1) + k] = nrows;
-            pre[2 * (nr + 1) + k] = nsuper;
-            pre[3 * (nr + 1) + k] = nsrows;
-            nbricks += (i64)nbk * nbk * nbk;
-            nrows += 3 * nbk;
-            nsuper += (i64)ns * ns * ns;
-            nsrows += 3 * ns;
-        }
-        pre[nr] = nbricks;
-        pre[2 * nr + 1] = nrows;
-        pre[3 * nr + 2] = nsuper;
-        pre[4 * nr + 3] = nsrows;
-        i64* dpre = dalloc<i64>(4 * ((i64)nr + 1), s);
-        CK(cudaMemcpyAsync(dpre, pre.data(), pre.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+        const i64 nbricks = tot[0], nrows = tot[1], nsuper = tot[2], nsrows = tot[3];
         i64* dbpre = dpre;
         i64* drpre = dpre + nr + 1;
         i64* dspre = dpre + 2 * (nr + 1);
@@ -1964,6 +1998,7 @@ void stage_mesh(Ctx& c) {
         float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
         float* xl = dalloc<float>((i64)nr * BR_LEVELS * 27, s);
         BrickIndex bix{dbpre, drpre, nr, rows, xl};
+        c.kend(kg);
         const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
         k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drpre, nr, nrows, 0, rows);
         CK_LAUNCH();
@@ -2002,9 +2037,6 @@ void stage_mesh(Ctx& c) {
             }
         }
         // bricks of leaves with lattice edge >= 16 come first (roots are in depth order)
-        i64 nbig = 0;
-        for (int k = 0; k < nr; ++k)
-            if (D - roots[k].depth >= 4) nbig = pre[k + 1];
         k_brick_bound<<<grid_for(nbig * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, 0, nbig, dspre,
                                                                                          ssign, bsign);
         CK_LAUNCH();
@@ -2021,6 +2053,7 @@ void stage_mesh(Ctx& c) {
         dfree(bsign, s);
         dfree(ssign, s);
         dfree(srows, s);
+        kg = c.kbegin("mesh_lists", 0.0);
         int* bf = dalloc<int>(nbricks, s);
         int* bp = dalloc<int>(nbricks + 1, s);
         k_live_flags<<<grid_for(nbricks, 256), 256, 0, s>>>(culled, nbricks, bf);
@@ -2029,7 +2062,9 @@ void stage_mesh(Ctx& c) {
         const i64 nlive = read_scalar(bp + nbricks, s);
         c.total_bricks = nbricks;
         c.live_bricks = nlive;
+        c.kend(kg);
         if (nlive > 0) {
+            kg = c.kbegin("mesh_lists", 0.0);
             live = dalloc<LiveBrick>(nlive, s);
             i64* lsz = dalloc<i64>(nlive, s);
             i64* csz = dalloc<i64>(nlive, s);
@@ -2057,6 +2092,7 @@ void stage_mesh(Ctx& c) {
             unsigned long long hc[2];
             CK(cudaMemcpyAsync(hc, cnt3, sizeof hc, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
+            c.kend(kg);
             // compulsory: the corner values written (bricks of edge 8: 729 each)
             const int ke = c.kbegin("brick_eval", (double)hc[0] * BR_CORNERS * 4);
             if (hc[0] > 0) {
@@ -2117,6 +2153,7 @@ void stage_mesh(Ctx& c) {
             k_virtual_cells<<<grid_for(total_cells, 256, 1ll << 30), 256, 0, s>>>(va, vc, total_cells, vcat, vntri);
             CK_LAUNCH();
             c.kend(kc2);
+            kg = c.kbegin("mesh_lists", 0.0);
             int* vf = dalloc<int>(total_cells, s);
             int* vp = dalloc<int>(total_cells + 1, s);
             k_active_flags<<<grid_for(total_cells, 256), 256, 0, s>>>(vntri, total_cells, vf);
@@ -2135,6 +2172,7 @@ void stage_mesh(Ctx& c) {
             exclusive_scan<i64, i64>(tmp, tri_virt, nact_virt, tri_virt + nact_virt, s);
             dfree(tmp, s);
             ntri_virt = read_scalar(tri_virt + nact_virt, s);
+            c.kend(kg);
         }
     }
     c.virtual_cells = total_cells;
@@ -2199,17 +2237,19 @@ void stage_mesh(Ctx& c) {
                                                         tri_vid, vpos);
         CK_LAUNCH();
         c.kend(kvi);
+        const int kd = c.kbegin("mesh_d2h", (double)(3 * nvert + nem) * 4);
         c.mesh_v.resize(3 * nvert);
         c.mesh_f.resize(nem);
         CK(cudaMemcpyAsync(c.mesh_v.data(), vpos, 3 * nvert * sizeof(float), cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(c.mesh_f.data(), tri_vid, nem * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        c.kend(kd);
         CK(cudaStreamSynchronize(s));
         dfree(hf, s); dfree(hp, s); dfree(tri_vid, s); dfree(vpos, s);
         dfree(em.keys, s); dfree(em.slot, s); dfree(em.pos, s);
     }
     dfree(act_real, s);
     dfree(tri_real, s);
-    dfree(droots, s); dfree(act_virt, s); dfree(tri_virt, s);
+    dfree(droots, s); dfree(droot_list, s); dfree(act_virt, s); dfree(tri_virt, s);
     dfree(vcat, s); dfree(vntri, s); dfree(bflag, s);
     dfree(lat_brick, s); dfree(live, s);
     dfree(cell_v, s);
