@@ -173,11 +173,16 @@ __device__ __host__ inline double ddot_entry(const BasePack& bp, int a, int b, d
 }
 
 // compact rows: entry (d, x, u) holds ddot[a + res*b] for a = 2^d-1+x and the
-// finest index b = 2^D-1+t, t = (x-1)*2^(D-d)+u, 0 <= u < 3*2^(D-d)
-__global__ void k_ddot_rows(BasePack bp, int D, int d, i64 row_start, double t1, double t2, float* __restrict__ out) {
-    const i64 W = 3ll << (D - d);
-    const i64 n = (1ll << d) * W;
-    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) {
+// finest index b = 2^D-1+t, t = (x-1)*2^(D-d)+u, 0 <= u < 3*2^(D-d).  Every depth
+// has 2^d rows of 3*2^(D-d) entries, 3*2^D in all, so depth d starts at d*3*2^D;
+// all depths in one launch.
+__global__ void k_ddot_rows(BasePack bp, int D, double t1, double t2, float* __restrict__ out) {
+    const i64 per_depth = 3ll << D;
+    const i64 n = (i64)(D + 1) * per_depth;
+    for (i64 g = (i64)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (i64)gridDim.x * blockDim.x) {
+        const int d = (int)(g / per_depth);
+        const i64 e = g - (i64)d * per_depth;
+        const i64 W = 3ll << (D - d);
         const i64 x = e / W, u = e - x * W;
         const i64 t = (x - 1) * (1ll << (D - d)) + u;
         float v = 0.f;
@@ -185,7 +190,7 @@ __global__ void k_ddot_rows(BasePack bp, int D, int d, i64 row_start, double t1,
             int a = (int)((1ll << d) - 1 + x), b = (int)((1ll << D) - 1 + t);
             v = (float)ddot_entry(bp, a, b, t1, t2);
         }
-        out[row_start + e] = v;
+        out[g] = v;
     }
 }
 
@@ -239,11 +244,8 @@ void stage_basis(Ctx& c) {
     dfree(c.ddot_div, s);
     c.ddot_div = dalloc<float>(c.ddot_row_start[D + 1], s);
     const double t1 = g_B.p[0].start, t2 = g_B.p[g_B.n - 1].start;
-    for (int d = 0; d <= D; ++d) {
-        i64 n = (1ll << d) * (3ll << (D - d));
-        k_ddot_rows<<<grid_for(n, 128), 128, 0, s>>>(bp, D, d, c.ddot_row_start[d], t1, t2, c.ddot_div);
-        CK_LAUNCH();
-    }
+    k_ddot_rows<<<grid_for(c.ddot_row_start[D + 1], 64, 1ll << 20), 64, 0, s>>>(bp, D, t1, t2, c.ddot_div);
+    CK_LAUNCH();
     host_stencils(D, c.stencil);
 }
 

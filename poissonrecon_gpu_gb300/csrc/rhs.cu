@@ -24,12 +24,23 @@ __global__ void k_splat(NodeArrays nd, i64 lo, i64 hi, int D, CPoly f, const flo
         key_coords(nd.key[i], D, D, xyz);
         const float oc0 = finest_center(xyz[0], D), oc1 = finest_center(xyz[1], D), oc2 = finest_center(xyz[2], D);
         float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+        // the 27 neighbours' indices, then their point ranges, loaded together; the
+        // points then in neighbour order (one copy of the point loop)
+        int p0s[27], pns[27];
+        {
+            int nbs[27];
+#pragma unroll
+            for (int j = 0; j < 27; ++j) nbs[j] = nd.neigh[(i64)j * M + i];
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                p0s[j] = nbs[j] == -1 ? 0 : nd.pidx[nbs[j]];
+                pns[j] = nbs[j] == -1 ? 0 : nd.pnum[nbs[j]];
+            }
+        }
+#pragma unroll 1
         for (int j = 0; j < 27; ++j) {
-            const int nb = nd.neigh[(i64)j * M + i];
-            if (nb == -1) continue;
-            const int p0 = nd.pidx[nb], pn = nd.pnum[nb];
-            for (int k = 0; k < pn; ++k) {
-                const i64 pt = (i64)p0 + k;
+            for (int k = 0; k < pns[j]; ++k) {
+                const i64 pt = (i64)p0s[j] + k;
                 const float px = pts[3 * pt], py = pts[3 * pt + 1], pz = pts[3 * pt + 2];
                 CPoly sx, sy, sz;
                 cpoly_shift<2>(f, px, sx);
@@ -432,6 +443,20 @@ __global__ void k_div_sum(const int* __restrict__ nchunks, const int* __restrict
     }
 }
 
+// the same sum of sibling-group partials (node i is child (i-1) % per of group
+// (i-1) / per) for nodes with few chunks: one thread per node, in chunk order
+__global__ void k_div_sum_thread(const int* __restrict__ nchunks, const int* __restrict__ first,
+                                 const double* __restrict__ partial, i64 lo, i64 hi, int per, float* __restrict__ out) {
+    for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
+        const i64 g = (i - 1) / per;
+        const int s = (int)((i - 1) % per), n = nchunks[g];
+        const i64 f = first[g];
+        double v = 0.0;
+        for (int q = 0; q < n; ++q) v += partial[(f + q) * per + s];
+        out[i] = (float)v;
+    }
+}
+
 void stage_splat(Ctx& c) {
     cudaStream_t s = c.stream;
     const int D = c.D;
@@ -527,7 +552,16 @@ void stage_divergence(Ctx& c) {
                 CK_LAUNCH();
                 c.kend(kt3);
             }
-            k_div_sum<<<grid_for((nc - 1) * 32, 256), 256, 0, s>>>(nch + 1, gfirst, gpartial, 1, nc, 8, c.divergence);
+            // depths 1..3 (up to 584 nodes, thousands of chunks each at depths 1-2): a warp per
+            // node; deeper nodes have few chunks: a thread per node
+            const i64 wide = std::min<i64>(nc, c.base[std::min(4, D)]);
+            k_div_sum<<<grid_for((wide - 1) * 32, 256), 256, 0, s>>>(nch + 1, gfirst, gpartial, 1, wide, 8,
+                                                                     c.divergence);
+            CK_LAUNCH();
+            if (nc > wide) {
+                k_div_sum_thread<<<grid_for(nc - wide, 256), 256, 0, s>>>(nch + 1, gfirst, gpartial, wide, nc, 8,
+                                                                           c.divergence);
+            }
             CK_LAUNCH();
         }
         dfree(nch, s);
