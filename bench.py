@@ -49,16 +49,25 @@ def parse():
     ap.add_argument("--points", type=int, default=1_000_000)
     ap.add_argument("--depth", type=int, default=10)
     ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--shape", default="torus", choices=["torus", "sphere", "displaced_sphere"],
+                    help="torus: density 1+7x, noise (default workload); sphere: uniform; displaced_sphere: "
+                         "4-octave value-noise displacement (the 30M-point, maxDepth 12 configuration)")
     return ap.parse_args()
 
 
-def workload(n):
+def workload(args):
     from poissonrecon_gpu_gb300 import shapes
-    return shapes.torus(n, seed=0)
+    if args.shape == "sphere":
+        return shapes.sphere(args.points, seed=0)
+    if args.shape == "displaced_sphere":
+        return shapes.displaced_sphere(args.points, seed=0)
+    return shapes.torus(args.points, seed=0)
 
 
 def config(args, l2):
-    return {"workload": "torus %d points, maxDepth %d, CG to relative residual %g" % (args.points, args.depth, args.tol),
+    shape = args.shape.replace("_", " ")
+    return {"workload": "%s %d points, maxDepth %d, CG to relative residual %g" % (shape, args.points, args.depth,
+                                                                                   args.tol),
             "points": args.points, "depth": args.depth, "solve": "per-depth CG, rel residual %g, FP64 dots" % args.tol,
             "l2": l2, "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
@@ -118,7 +127,7 @@ def cpu_reference(args, steps, warmup):
     """The reference path on the host cores: the oracle, subdivision sampled."""
     import oracle
     oracle.build()
-    xyz, nrm = workload(args.points)
+    xyz, nrm = workload(args)
     threads = os.cpu_count() or 1
     o = oracle.Oracle(args.depth, threads=threads)
     o.set_points(xyz, nrm)
@@ -166,7 +175,7 @@ TRAFFIC = os.path.join(REPO, "profiles", "dram_traffic_torus1M_d10.md")
 
 def measured_traffic(args):
     """DRAM bytes per launch of each kernel timer, from the committed ncu summary of this workload."""
-    if args.points != 1_000_000 or args.depth != 10 or not os.path.exists(TRAFFIC):
+    if args.shape != "torus" or args.points != 1_000_000 or args.depth != 10 or not os.path.exists(TRAFFIC):
         return {}
     out = {}
     for line in open(TRAFFIC):
@@ -226,7 +235,7 @@ def main():
     dev = torch.device("cuda", local)
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
 
-    xyz, nrm = workload(args.points)
+    xyz, nrm = workload(args)
     n = len(xyz)
     h_xyz = torch.from_numpy(xyz).pin_memory()
     h_nrm = torch.from_numpy(nrm).pin_memory()

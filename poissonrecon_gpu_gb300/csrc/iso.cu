@@ -1270,7 +1270,8 @@ __global__ void k_root_of(const VRoot* __restrict__ roots, int nroots, int* __re
 template <int EB>
 struct BrickShared {
     static constexpr int K1 = EB + 1;         // corners per axis
-    static constexpr int XW = (EB == BR) ? BR_XW : 728;
+    // edge 2 (leaves one depth above the finest): one virtual depth, at most 5^3 window cells
+    static constexpr int XW = (EB == BR) ? BR_XW : (EB == 4 ? 728 : 128);
     float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
     float Bt[3 * BR_LEVELS * 4 * K1];         // [axis][depth][t][k]
     float Xw[XW];                             // window coefficients, virtual depths (0: none or inside the leaf)
@@ -1506,11 +1507,14 @@ __global__ void k_live_offsets(LiveBrick* __restrict__ live, const i64* __restri
     }
 }
 // live bricks split by edge: 8 (first list) and 2 or 4 (second list)
+// live bricks by edge: 8 (cnt[0]), 4 (cnt[1]) and 2 (cnt[5])
 __global__ void k_live_split(VArgs v, const LiveBrick* __restrict__ live, i64 n, int* __restrict__ big,
-                             int* __restrict__ small, unsigned long long* __restrict__ cnt) {
+                             int* __restrict__ mid, int* __restrict__ small, unsigned long long* __restrict__ cnt) {
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        if (brick_edge(v.e.D, v.roots[live[k].root].depth) == BR) big[atomicAdd(&cnt[0], 1ull)] = (int)k;
-        else small[atomicAdd(&cnt[1], 1ull)] = (int)k;
+        const int E = brick_edge(v.e.D, v.roots[live[k].root].depth);
+        if (E == BR) big[atomicAdd(&cnt[0], 1ull)] = (int)k;
+        else if (E == 4) mid[atomicAdd(&cnt[1], 1ull)] = (int)k;
+        else small[atomicAdd(&cnt[5], 1ull)] = (int)k;
     }
 }
 __global__ void k_live_flags(const unsigned char* __restrict__ culled, i64 n, int* __restrict__ f) {
@@ -2079,17 +2083,19 @@ void stage_mesh(Ctx& c) {
             const i64 lat_total = read_scalar(lpos + nlive, s);
             total_cells = read_scalar(cpos + nlive, s);
             lat_brick = dalloc<float>(lat_total, s);
-            // bricks of edge 8 and the smaller ones go to the two instances of the evaluation
-            // big, small, foreign corners, window layout overflows, foreign corners evaluated
-            unsigned long long* cnt3 = dalloc<unsigned long long>(5, s);
-            int* lists = dalloc<int>(2 * nlive, s);
-            CK(cudaMemsetAsync(cnt3, 0, 5 * sizeof(unsigned long long), s));
+            // bricks of edge 8, 4 and 2 go to three instances of the evaluation
+            // counters: edge 8, edge 4, foreign corners, window layout overflows, foreign corners
+            // evaluated, edge 2
+            unsigned long long* cnt3 = dalloc<unsigned long long>(6, s);
+            int* lists = dalloc<int>(3 * nlive, s);
+            CK(cudaMemsetAsync(cnt3, 0, 6 * sizeof(unsigned long long), s));
             // corners owned by another leaf: at most the lower-face corners of the live bricks
             const i64 fcap = std::min<i64>(lat_total, nlive * (BR_CORNERS - BR * BR * BR));
             int2* foreign = dalloc<int2>(std::max<i64>(fcap, 1), s);
-            k_live_split<<<grid_for(nlive, 256), 256, 0, s>>>(va, live, nlive, lists, lists + nlive, cnt3);
+            k_live_split<<<grid_for(nlive, 256), 256, 0, s>>>(va, live, nlive, lists, lists + nlive,
+                                                              lists + 2 * nlive, cnt3);
             CK_LAUNCH();
-            unsigned long long hc[2];
+            unsigned long long hc[6];
             CK(cudaMemcpyAsync(hc, cnt3, sizeof hc, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             c.kend(kg);
@@ -2105,6 +2111,11 @@ void stage_mesh(Ctx& c) {
             if (hc[1] > 0) {
                 k_brick_eval<4, 64><<<grid_for((i64)hc[1], 1, (i64)c.sms * 24), 64, 0, s>>>(
                     va, bix, root_of, live, lists + nlive, (i64)hc[1], lat_brick, cnt3 + 2, foreign, fcap);
+                CK_LAUNCH();
+            }
+            if (hc[5] > 0) {   // 27 corners: one warp per brick
+                k_brick_eval<2, 32><<<grid_for((i64)hc[5], 1, (i64)c.sms * 32), 32, 0, s>>>(
+                    va, bix, root_of, live, lists + 2 * nlive, (i64)hc[5], lat_brick, cnt3 + 2, foreign, fcap);
                 CK_LAUNCH();
             }
             c.kend(ks);
