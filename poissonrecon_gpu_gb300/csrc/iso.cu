@@ -806,6 +806,43 @@ __device__ __forceinline__ void term_interval(float x, const float* lo, const fl
     thi = b;
 }
 
+// the leaf's ancestor levels l <= r of a bound, factored by axis: for every
+// (l, jx, jy) the three z terms x[j] * Z[jz] (scalar times interval) are summed,
+// then multiplied by the intervals Y[jy] and X[jx].  Interval arithmetic is
+// subdistributive, so this encloses every corner's exact ancestor sum as the
+// term-by-term form does, with a third of its interval products.  Each end is
+// within 5u of the exact factored end per row (3 terms, 2 products), against
+// 3u per term in the term-by-term form; the margins allow 2 BR_WEXT u A more.
+// amax gains sum |x| |Z| |Y| |X| >= sum |term| over the corners.
+__device__ __forceinline__ void ancestor_bound(const float* xl, const float* const row[3], int r, int D, int lane,
+                                               float& lo, float& hi, float& amax, int& cnt) {
+    const int ra = ROW_RA * (D + 1);
+    for (int t = lane; t < 9 * (r + 1); t += 32) {
+        const int l = r - t / 9, jx = (t % 9) / 3, jy = t % 3;
+        const float* xs = xl + 27 * l + 9 * jx + 3 * jy;
+        float slo = 0.f, shi = 0.f, sabs = 0.f;
+        for (int jz = 0; jz < 3; ++jz) {
+            const float x = xs[jz];
+            if (x == 0.f) continue;
+            const float zl = row[2][ra + (l * 3 + jz) * 2], zh = row[2][ra + (l * 3 + jz) * 2 + 1];
+            const float p0 = x * zl, p1 = x * zh;
+            slo += fminf(p0, p1);
+            shi += fmaxf(p0, p1);
+            sabs += fabsf(x) * fmaxf(fabsf(zl), fabsf(zh));
+            ++cnt;
+        }
+        if (sabs == 0.f) continue;
+        const float yl = row[1][ra + (l * 3 + jy) * 2], yh = row[1][ra + (l * 3 + jy) * 2 + 1];
+        const float xl0 = row[0][ra + (l * 3 + jx) * 2], xh0 = row[0][ra + (l * 3 + jx) * 2 + 1];
+        float c0 = slo * yl, c1 = slo * yh, c2 = shi * yl, c3 = shi * yh;
+        const float alo = fminf(fminf(c0, c1), fminf(c2, c3)), ahi = fmaxf(fmaxf(c0, c1), fmaxf(c2, c3));
+        c0 = alo * xl0; c1 = alo * xh0; c2 = ahi * xl0; c3 = ahi * xh0;
+        lo += fminf(fminf(c0, c1), fminf(c2, c3));
+        hi += fmaxf(fmaxf(c0, c1), fmaxf(c2, c3));
+        amax += sabs * fmaxf(fabsf(yl), fabsf(yh)) * fmaxf(fabsf(xl0), fabsf(xh0));
+    }
+}
+
 // can a corner of brick b[] (nb bricks per edge) be owned by a cell of another
 // leaf of the batch?  The candidate cells of a corner lie in the leaf or in a
 // neighbour at offset (dx,dy,dz): -1 on an axis only for corners on the leaf's
@@ -1038,22 +1075,7 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, const i64* __restr
         float flo = 0.f, fhi = 0.f, amax = 0.f;
         int cnt = 0;
         bool decided = true;
-        for (int t = lane; t < 27 * (r + 1); t += 32) {
-            const int lv = r - t / 27, j = t % 27;
-            const float x = xl[27 * lv + j];
-            if (x == 0.f) continue;
-            const int tt[3] = {j / 9, (j / 3) % 3, j % 3};
-            float blo[3], bhi[3];
-            for (int ax = 0; ax < 3; ++ax) {
-                blo[ax] = row[ax][ROW_RA * (D + 1) + (lv * 3 + tt[ax]) * 2];
-                bhi[ax] = row[ax][ROW_RA * (D + 1) + (lv * 3 + tt[ax]) * 2 + 1];
-            }
-            float tl, th;
-            term_interval(x, blo, bhi, tl, th);
-            flo += tl; fhi += th;
-            amax += fmaxf(fabsf(tl), fabsf(th));
-            ++cnt;
-        }
+        ancestor_bound(xl, row, r, D, lane, flo, fhi, amax, cnt);
         for (int d = r + 1; d <= D && decided; ++d) {
             int wlo[3], ext[3];
             bool cross = false;
@@ -1100,7 +1122,7 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, const i64* __restr
         }
         if (lane == 0) {
             const double iso = (double)v.iso, A = (double)amax * 1.01;
-            const double margin = (2.0 * cnt + 8.0) * u * A +
+            const double margin = (2.0 * cnt + 2.0 * BR_WEXT + 8.0) * u * A +
                                   4.0 * u * (fabs((double)flo) + fabs((double)fhi) + 2.0 * fabs(iso)) + 1e-30;
             const bool above = (double)flo - margin > iso, below = (double)fhi + margin < iso;
             ssign[si] = !decided ? 0 : (above ? 1 : (below ? -1 : 0));
@@ -1142,22 +1164,7 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
         float lo = 0.f, hi = 0.f, amax = 0.f;
         int cnt = 0;
         // the leaf and its ancestors
-        for (int t = lane; t < 27 * (r + 1); t += 32) {
-            const int l = r - t / 27, j = t % 27;
-            const float x = xl[27 * l + j];
-            if (x == 0.f) continue;
-            const int tt[3] = {j / 9, (j / 3) % 3, j % 3};
-            float blo[3], bhi[3];
-            for (int ax = 0; ax < 3; ++ax) {
-                blo[ax] = row[ax][ROW_RA * (D + 1) + (l * 3 + tt[ax]) * 2];
-                bhi[ax] = row[ax][ROW_RA * (D + 1) + (l * 3 + tt[ax]) * 2 + 1];
-            }
-            float tl, th;
-            term_interval(x, blo, bhi, tl, th);
-            lo += tl; hi += th;
-            amax += fmaxf(fabsf(tl), fabsf(th));
-            ++cnt;
-        }
+        ancestor_bound(xl, row, r, D, lane, lo, hi, amax, cnt);
         // real nodes around the leaf, at the virtual depths
         for (int d = r + 1; d <= D; ++d) {
             int wlo[3], ext[3];
@@ -1205,10 +1212,11 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
         }
         if (lane == 0) {
             // rounding of the evaluation's FMA chain, (cnt + 4) u sum|term|, plus that of
-            // this bound's own float products and sums, (cnt + 3) u sum|term|
+            // this bound's own float products and sums, at most (cnt + 5) u sum|term|
+            // (factored ancestor rows) -- allowed (cnt + 2 BR_WEXT + 4)
             const double iso = (double)v.iso, A = (double)amax * 1.01;
-            const double margin = (2.0 * cnt + 8.0) * u * A + 4.0 * u * (fabs((double)lo) + fabs((double)hi) + 2.0 * fabs(iso)) +
-                                  1e-30;
+            const double margin = (2.0 * cnt + 2.0 * BR_WEXT + 8.0) * u * A +
+                                  4.0 * u * (fabs((double)lo) + fabs((double)hi) + 2.0 * fabs(iso)) + 1e-30;
             const bool above = (double)lo - margin > iso, below = (double)hi + margin < iso;
             sign[bi] = above ? 1 : (below ? -1 : 0);
         }
