@@ -747,31 +747,39 @@ constexpr int ROW_RA = 0, ROW_RW = 6, ROW_PER_DEPTH = 30;
 
 __device__ __forceinline__ int brick_edge(int D, int r) { return min(1 << (D - r), BR); }
 
+// Roots are in depth order and every root of depth d has the same number of bricks
+// (8^lg[d]) and super-bricks (8^slg[d]), so the root of a brick follows from the
+// per-depth counts without a search.
+struct DepthLayout {
+    int first[17];                 // first root of depth d
+    int lg[17], slg[17];           // log2 of bricks (super-bricks) per leaf edge at depth d
+    i64 boff[17], soff[17];        // bricks (super-bricks) of the roots above depth d
+};
 struct BrickIndex {                // bricks of all subdivided leaves, numbered root by root
     const i64* prefix;             // first brick of each root
     const i64* row_prefix;         // first brick row of each root (3 * bricks per edge rows each)
     int nroots;
     const float* rows;             // brick-row tables, 30 (D+1) floats each
     const float* xl;               // per root: x of the 27 neighbours of each ancestor, 16 x 27
+    DepthLayout dl;
 };
 struct VBrick {
     int root;                      // index into roots
     int b[3];                      // brick coordinates in the leaf
 };
 __device__ __forceinline__ VBrick brick_of(const VArgs& v, const BrickIndex& bx, i64 g) {
-    int lo = 0, hi = bx.nroots - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (bx.prefix[mid] <= g) lo = mid; else hi = mid - 1;
-    }
+    const DepthLayout& L = bx.dl;
+    int d = 0;
+    while (d < v.e.D - 1 && L.boff[d + 1] <= g) ++d;   // roots are coarse nodes: depth < D
+    const i64 loc = g - L.boff[d];
+    const int lg = L.lg[d];
     VBrick b;
-    b.root = lo;
-    const int r = v.roots[lo].depth;
-    const int nb = (1 << (v.e.D - r)) / brick_edge(v.e.D, r);
-    const i64 l = g - bx.prefix[lo];
-    b.b[0] = (int)(l / ((i64)nb * nb));
-    b.b[1] = (int)((l / nb) % nb);
-    b.b[2] = (int)(l % nb);
+    b.root = L.first[d] + (int)(loc >> (3 * lg));
+    const i64 l = loc & ((1ll << (3 * lg)) - 1);
+    const int m = (1 << lg) - 1;
+    b.b[0] = (int)(l >> (2 * lg));
+    b.b[1] = (int)(l >> lg) & m;
+    b.b[2] = (int)l & m;
     return b;
 }
 __device__ __forceinline__ const float* brick_row(const BrickIndex& bx, int D, int root, int nb, int ax, int b) {
@@ -1045,8 +1053,8 @@ __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, 
 // one warp per super-brick (4^3 bricks of leaves with lattice edge >= 64): the
 // same bound over all its corners; decided only when every window it needs fits
 // the row tables (away from the leaf's boundary).  ssign = 1, -1 or 0.
-__global__ void __launch_bounds__(256) k_super_bound(VArgs v, const i64* __restrict__ sprefix,
-                                                     const i64* __restrict__ srow_prefix, int nroots,
+__global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
+                                                     const i64* __restrict__ srow_prefix,
                                                      const float* __restrict__ srows, const float* __restrict__ xl_all,
                                                      i64 nsuper, signed char* __restrict__ ssign) {
     const EvalArgs& a = v.e;
@@ -1056,15 +1064,15 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, const i64* __restr
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
     const double u = 5.9604644775390625e-08;   // 2^-24
     for (i64 si = warp; si < nsuper; si += nwarps) {
-        int lo = 0, hi = nroots - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (sprefix[mid] <= si) lo = mid; else hi = mid - 1;
-        }
+        int dd = 0;
+        while (dd < D - 1 && dl.soff[dd + 1] <= si) ++dd;
+        const i64 loc = si - dl.soff[dd];
+        const int slg = dl.slg[dd];
+        const int lo = dl.first[dd] + (int)(loc >> (3 * slg));
         const VRoot R = v.roots[lo];
         const int r = R.depth, S = 1 << (D - r), E = 4 * BR, ns = S / E, L = R.node;
-        const i64 l = si - sprefix[lo];
-        const int sb[3] = {(int)(l / ((i64)ns * ns)), (int)((l / ns) % ns), (int)(l % ns)};
+        const i64 l = loc & ((1ll << (3 * slg)) - 1);
+        const int sb[3] = {(int)(l >> (2 * slg)), (int)(l >> slg) & (ns - 1), (int)l & (ns - 1)};
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
         const int g0[3] = {Lc[0] * S + sb[0] * E, Lc[1] * S + sb[1] * E, Lc[2] * S + sb[2] * E};
@@ -2009,7 +2017,14 @@ void stage_mesh(Ctx& c) {
         i64* dsrpre = dpre + 3 * (nr + 1);
         float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
         float* xl = dalloc<float>((i64)nr * BR_LEVELS * 27, s);
-        BrickIndex bix{dbpre, drpre, nr, rows, xl};
+        BrickIndex bix{dbpre, drpre, nr, rows, xl, {}};
+        for (int d = 0; d <= D; ++d) {
+            bix.dl.first[d] = layout.first[d];
+            bix.dl.lg[d] = std::max(D - d - 3, 0);          // bricks per edge 2^(D-d) / min(2^(D-d), 8)
+            bix.dl.slg[d] = std::max(D - d - 5, 0);         // super-bricks per edge 2^(D-d) / 32 (D-d >= 6)
+            bix.dl.boff[d] = layout.off[0][d];
+            bix.dl.soff[d] = layout.off[2][d];
+        }
         c.kend(kg);
         const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
         k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drpre, nr, nrows, 0, rows);
@@ -2036,7 +2051,7 @@ void stage_mesh(Ctx& c) {
         signed char* ssign = nullptr;
         if (nsuper > 0) {
             ssign = dalloc<signed char>(nsuper, s);
-            k_super_bound<<<grid_for(nsuper * 32, 256, (i64)c.sms * 8), 256, 0, s>>>(va, dspre, dsrpre, nr, srows, xl,
+            k_super_bound<<<grid_for(nsuper * 32, 256, (i64)c.sms * 8), 256, 0, s>>>(va, bix.dl, dsrpre, srows, xl,
                                                                                     nsuper, ssign);
             CK_LAUNCH();
             if (c.profile) {   // statistics only
