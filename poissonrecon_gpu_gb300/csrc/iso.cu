@@ -754,6 +754,7 @@ struct DepthLayout {
     int first[17];                 // first root of depth d
     int lg[17], slg[17];           // log2 of bricks (super-bricks) per leaf edge at depth d
     i64 boff[17], soff[17];        // bricks (super-bricks) of the roots above depth d
+    i64 roff[17], sroff[17];       // brick rows (super-brick rows) of the roots above depth d
 };
 struct BrickIndex {                // bricks of all subdivided leaves, numbered root by root
     const i64* prefix;             // first brick of each root
@@ -959,21 +960,21 @@ __device__ __forceinline__ int row_edge(int D, int r, int super) {
 }
 
 // one thread per (brick row, depth); rows numbered root by root (row_prefix), 3 x bricks-per-edge each
-__global__ void k_brick_rows(VArgs v, const i64* __restrict__ row_prefix, int nroots, i64 nrows, int super,
-                             float* __restrict__ rows) {
+__global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, float* __restrict__ rows) {
     const EvalArgs& a = v.e;
     const int D = a.D;
+    const i64* off = super ? dl.sroff : dl.roff;
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < nrows * (D + 1); e += (i64)gridDim.x * blockDim.x) {
         const i64 row = e / (D + 1);
         const int d = (int)(e % (D + 1));
-        int lo = 0, hi = nroots - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (row_prefix[mid] <= row) lo = mid; else hi = mid - 1;
-        }
-        const int nbk = (1 << (D - v.roots[lo].depth)) / row_edge(D, v.roots[lo].depth, super);
-        const int rl = (int)(row - row_prefix[lo]);
-        const int4 rd = make_int4(lo, rl / nbk, rl % nbk, 0);   // root, axis, brick index
+        // the root from the per-depth layout: 3 * 2^lg rows per root of depth dd
+        int dd = 0;
+        while (dd < D - 1 && off[dd + 1] <= row) ++dd;
+        const int nbk = 1 << (super ? dl.slg[dd] : dl.lg[dd]);
+        const i64 loc = row - off[dd];
+        const int root = dl.first[dd] + (int)(loc / (3 * nbk));
+        const int rl = (int)(loc % (3 * nbk));
+        const int4 rd = make_int4(root, rl / nbk, rl % nbk, 0);   // root, axis, brick index
         const VRoot R = v.roots[rd.x];
         const int ax = rd.y, r = R.depth, S = 1 << (D - r), B = row_edge(D, r, super);
         int Lc[3];
@@ -2024,15 +2025,17 @@ void stage_mesh(Ctx& c) {
             bix.dl.slg[d] = std::max(D - d - 5, 0);         // super-bricks per edge 2^(D-d) / 32 (D-d >= 6)
             bix.dl.boff[d] = layout.off[0][d];
             bix.dl.soff[d] = layout.off[2][d];
+            bix.dl.roff[d] = layout.off[1][d];
+            bix.dl.sroff[d] = layout.off[3][d];
         }
         c.kend(kg);
         const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
-        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, drpre, nr, nrows, 0, rows);
+        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nrows, 0, rows);
         CK_LAUNCH();
         float* srows = nullptr;
         if (nsrows > 0) {
             srows = dalloc<float>(nsrows * ROW_PER_DEPTH * (D + 1), s);
-            k_brick_rows<<<grid_for(nsrows * (D + 1), 128), 128, 0, s>>>(va, dsrpre, nr, nsrows, 1, srows);
+            k_brick_rows<<<grid_for(nsrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nsrows, 1, srows);
             CK_LAUNCH();
         }
         k_brick_xl<<<grid_for((i64)nr * BR_LEVELS * 27, 256), 256, 0, s>>>(va, nr, xl);
