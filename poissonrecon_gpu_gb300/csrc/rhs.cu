@@ -24,9 +24,10 @@ __global__ void k_splat(NodeArrays nd, i64 lo, i64 hi, int D, CPoly f, const flo
         key_coords(nd.key[i], D, D, xyz);
         const float oc0 = finest_center(xyz[0], D), oc1 = finest_center(xyz[1], D), oc2 = finest_center(xyz[2], D);
         float v0 = 0.f, v1 = 0.f, v2 = 0.f;
-        // the 27 neighbours' indices, then their point ranges, loaded together; the
-        // points then in neighbour order (one copy of the point loop)
-        int p0s[27], pns[27];
+        // the 27 neighbours' indices, then their point ranges, loaded together; then the
+        // node's (neighbour, point) pairs in neighbour order by one flat loop, so that a
+        // warp's lanes run the same iteration whatever their neighbours' point counts
+        int p0s[27], pns[27], T = 0;
         {
             int nbs[27];
 #pragma unroll
@@ -35,25 +36,26 @@ __global__ void k_splat(NodeArrays nd, i64 lo, i64 hi, int D, CPoly f, const flo
             for (int j = 0; j < 27; ++j) {
                 p0s[j] = nbs[j] == -1 ? 0 : nd.pidx[nbs[j]];
                 pns[j] = nbs[j] == -1 ? 0 : nd.pnum[nbs[j]];
+                T += pns[j];
             }
         }
-#pragma unroll 1
-        for (int j = 0; j < 27; ++j) {
-            for (int k = 0; k < pns[j]; ++k) {
-                const i64 pt = (i64)p0s[j] + k;
-                const float px = pts[3 * pt], py = pts[3 * pt + 1], pz = pts[3 * pt + 2];
-                CPoly sx, sy, sz;
-                cpoly_shift<2>(f, px, sx);
-                cpoly_shift<2>(f, py, sy);
-                cpoly_shift<2>(f, pz, sz);
-                const float wx = cpoly_value<2>(sx, oc0);
-                const float wy = cpoly_value<2>(sy, oc1);
-                const float wz = cpoly_value<2>(sz, oc2);
-                const float w = wx * wy * wz;
-                v0 = fmaf(w, nrm[3 * pt], v0);
-                v1 = fmaf(w, nrm[3 * pt + 1], v1);
-                v2 = fmaf(w, nrm[3 * pt + 2], v2);
-            }
+        int j = 0, k = 0;
+        for (int t = 0; t < T; ++t) {
+            while (k >= pns[j]) { ++j; k = 0; }
+            const i64 pt = (i64)p0s[j] + k;
+            ++k;
+            const float px = pts[3 * pt], py = pts[3 * pt + 1], pz = pts[3 * pt + 2];
+            CPoly sx, sy, sz;
+            cpoly_shift<2>(f, px, sx);
+            cpoly_shift<2>(f, py, sy);
+            cpoly_shift<2>(f, pz, sz);
+            const float wx = cpoly_value<2>(sx, oc0);
+            const float wy = cpoly_value<2>(sy, oc1);
+            const float wz = cpoly_value<2>(sz, oc2);
+            const float w = wx * wy * wz;
+            v0 = fmaf(w, nrm[3 * pt], v0);
+            v1 = fmaf(w, nrm[3 * pt + 1], v1);
+            v2 = fmaf(w, nrm[3 * pt + 2], v2);
         }
         const i64 o = i - lo;
         vfield[3 * o] = v0;
