@@ -44,7 +44,12 @@ typedef struct {
     double cg_tol;        /* 1e-5 absolute (reference) or relative tolerance */
     int32_t cg_max_iter;  /* 10000 in the reference (CG_CUDA.cuh:263) */
     int32_t device;       /* CUDA device ordinal */
-    int32_t reserved[8];
+    int32_t weld;         /* 0: a vertex per lattice edge and subdivision batch, as the reference
+                             (its batches share no vertices, main.cu:3799-4564); 1: one vertex per
+                             lattice edge across batches (no cracks at batch boundaries; the
+                             triangles are the same, a vertex on a batch boundary takes the
+                             position computed by one of its batches) */
+    int32_t reserved[7];
 } prgpu_params;
 
 typedef struct {

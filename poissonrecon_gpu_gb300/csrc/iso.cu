@@ -1584,6 +1584,7 @@ __global__ void k_virtual_cells(VArgs v, VirtCells vc, i64 total, unsigned char*
 struct EmitArgs {
     int D;
     int local_bits;
+    int weld;           // 1: keys without the batch (vertices shared across batches)
     i64 tri_offset;     // first global triangle of this emission
     u64* keys;          // 3 per triangle
     uint32_t* slot;     // payload: 3*t+q
@@ -1709,7 +1710,7 @@ __global__ void k_emit_virtual(VArgs v, EmitArgs em, VirtCells vc, const i64* __
             float p[3];
             crossing(lp, o, rev, cv[ev0], cv[ev1], D, p);
             const i64 slot = 3 * (tb + k / 3) + (k % 3);
-            em.keys[slot] = edge_key(lp, o, D, R.batch, em.local_bits);
+            em.keys[slot] = edge_key(lp, o, D, em.weld ? 0 : R.batch, em.local_bits);
             em.slot[slot] = (uint32_t)slot;
             em.pos[3 * slot] = p[0];
             em.pos[3 * slot + 1] = p[1];
@@ -2226,7 +2227,7 @@ void stage_mesh(Ctx& c) {
         while ((double)(1ull << local_bits) < lat_edges) ++local_bits;
     }
     int batch_bits = 0;
-    while ((1 << batch_bits) < nbatches) ++batch_bits;
+    while (!c.params.weld && (1 << batch_bits) < nbatches) ++batch_bits;
     c.mesh_v.clear();
     c.mesh_f.clear();
     c.batch_tri.assign(1, ntri_real);
@@ -2235,6 +2236,7 @@ void stage_mesh(Ctx& c) {
         EmitArgs em;
         em.D = D;
         em.local_bits = local_bits;
+        em.weld = c.params.weld ? 1 : 0;
         em.tri_offset = 0;
         em.keys = dalloc<u64>(nem, s);
         em.slot = dalloc<uint32_t>(nem, s);

@@ -239,3 +239,35 @@ def test_reconstruct_batch_matches_single(lib_built):
     v, f = r.reconstruct(*clouds[0])
     assert len(f) > 0
     r.close()
+
+
+def _open_edges(f):
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+    _, cnt = np.unique(e, axis=0, return_counts=True)
+    return int((cnt == 1).sum())
+
+
+@pytest.mark.parametrize("kind,n,depth", [("sphere", 50000, 8), ("torus", 30000, 8)], ids=["sphere50k-d8", "torus30k-d8"])
+def test_weld_shares_vertices_across_batches(lib_built, kind, n, depth):
+    """weld = 1: one vertex per lattice edge across subdivision batches.  The triangles are the
+    same (same count, same emission order); each welded vertex is a vertex of the unwelded mesh
+    (the position one of its batches computed), and the batch seams close (open edges remain only
+    where the batches on either side disagree on a corner's sign)."""
+    import poissonrecon_gpu_gb300 as pg
+    xyz, nrm = sphere(n, seed=0) if kind == "sphere" else _torus(n, seed=0)
+    meshes = []
+    for weld in (False, True):
+        r = pg.Reconstructor(depth=depth, weld=weld)
+        meshes.append(r.reconstruct(xyz, nrm))
+        r.close()
+    (v0, f0), (v1, f1) = meshes
+    assert len(f1) == len(f0) and len(v1) < len(v0)
+    # every welded vertex position occurs in the unwelded mesh
+    p0 = np.unique(v0.view([("", np.float32)] * 3).ravel())
+    p1 = np.unique(v1.view([("", np.float32)] * 3).ravel())
+    assert np.all(np.isin(p1, p0))
+    # triangle by triangle, a corner moves along its own lattice edge: less than one finest cell
+    # (the batches on either side of a seam compute the crossing from their own corner values)
+    cell = 1.25 * float((xyz.max(0) - xyz.min(0)).max()) / (1 << depth)
+    assert np.abs(v1[f1] - v0[f0]).max() <= cell
+    assert _open_edges(f1) * 50 < _open_edges(f0)
