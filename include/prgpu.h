@@ -49,7 +49,11 @@ typedef struct {
                              lattice edge across batches (no cracks at batch boundaries; the
                              triangles are the same, a vertex on a batch boundary takes the
                              position computed by one of its batches) */
-    int32_t reserved[7];
+    int32_t density_weights; /* 0: every sample weighs 1, as the reference; 1: each sample's normal
+                                and its share of the iso-value are weighted by the inverse of the
+                                sampling density around it, estimated at depth maxDepth-2 (Kazhdan's
+                                adaptive weighting of non-uniform samples; not in the reference) */
+    int32_t reserved[6];
 } prgpu_params;
 
 typedef struct {

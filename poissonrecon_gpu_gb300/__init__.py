@@ -38,7 +38,7 @@ ARRAY_DTYPES = {
     "count": np.int64, "center": np.float32, "scale": np.float32, "vfield": np.float32,
     "divergence": np.float32, "stencil": np.float32, "ddot_rows": np.float32, "dot": np.float64,
     "ddot": np.float64, "d2dot": np.float64, "x": np.float32, "cg_iters": np.int32, "cg_rr": np.float32,
-    "point_value": np.float32, "iso": np.float32, "has_tri": np.int32, "has_int": np.int32,
+    "point_value": np.float32, "point_weight": np.float32, "iso": np.float32, "has_tri": np.int32, "has_int": np.int32,
     "batch_tri": np.int64, "subdivide_roots": np.int64,
 }
 
@@ -53,7 +53,7 @@ class PrgpuError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("depth", ctypes.c_int32), ("solve_mode", ctypes.c_int32), ("cg_tol", ctypes.c_double),
                 ("cg_max_iter", ctypes.c_int32), ("device", ctypes.c_int32), ("weld", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("density_weights", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
 
 
 class Mesh(ctypes.Structure):
@@ -125,12 +125,13 @@ class Reconstructor:
     """One reconstruction context on one GPU (its own CUDA stream)."""
 
     def __init__(self, depth: int = 8, solve_mode: int = SOLVE_REFERENCE, cg_tol: float = 1e-5,
-                 cg_max_iter: int = 10000, device: int = 0, weld: bool = False):
+                 cg_max_iter: int = 10000, device: int = 0, weld: bool = False, density_weights: bool = False):
         L = _lib()
         p = Params()
         L.prgpu_params_default(ctypes.byref(p))
         p.depth, p.solve_mode, p.cg_tol, p.cg_max_iter, p.device = depth, solve_mode, cg_tol, cg_max_iter, device
         p.weld = 1 if weld else 0
+        p.density_weights = 1 if density_weights else 0
         self.params = p
         self._h = _VP()
         _check(L.prgpu_create(ctypes.byref(p), ctypes.byref(self._h)), "prgpu_create")

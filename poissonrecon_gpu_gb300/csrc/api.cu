@@ -33,6 +33,7 @@ void Ctx::free_all() {
     dfree(in_xyz, s); dfree(in_nrm, s); dfree(pts, s); dfree(nrm, s); dfree(sort_idx, s);
     dfree(point_node, s); dfree(basis, s); dfree(ddot_div, s); dfree(full_tables, s);
     dfree(vfield, s); dfree(divergence, s); dfree(x, s); dfree(point_value, s);
+    dfree(point_weight, s); dfree(wnrm, s);
     dfree(d_cg_iters, s); dfree(d_cg_rr, s);
     dfree(d_has_tri, s); dfree(d_has_int, s);
     n_coarse = 0;
@@ -449,6 +450,7 @@ int prgpu_get_array(void* h, const char* name, void* dst, int64_t max_bytes, int
     }
     if (c->stage >= 5) {
         if (n == "point_value") return copy_out(c, c->point_value, c->N * 4, dst, max_bytes, nbytes);
+        if (n == "point_weight") return copy_out(c, c->point_weight, c->point_weight ? c->N * 4 : 0, dst, max_bytes, nbytes);
         if (n == "iso") return copy_out(c, &c->iso, 4, dst, max_bytes, nbytes, true);
     }
     if (c->stage >= 6) {

@@ -103,6 +103,8 @@ struct Ctx {
 
     // rhs / solve
     float* vfield = nullptr;         // 3 x count[D]
+    float* point_weight = nullptr;   // N: density weights (params.density_weights), mean 1
+    float* wnrm = nullptr;           // 3N: the normals times the density weights
     float* divergence = nullptr;     // M
     float* x = nullptr;              // M
     std::vector<int> cg_iters;

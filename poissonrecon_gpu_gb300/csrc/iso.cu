@@ -227,14 +227,16 @@ __device__ __forceinline__ float walk_up(const EvalArgs& a, i64 node, const floa
     return val;
 }
 
+// the iso-value sum: sum of f(p), or of w(p) f(p) with density weights (mean 1)
 __global__ void k_point_values(EvalArgs a, const float* __restrict__ pts, const int* __restrict__ point_node, i64 n,
-                               float* __restrict__ out, double* __restrict__ sum) {
+                               const float* __restrict__ weight, float* __restrict__ out, double* __restrict__ sum) {
     double loc = 0;
     for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
         const float q[3] = {pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]};
         const float v = walk_up(a, point_node[k], q, 0.f);
         out[k] = v;
-        loc += (double)v;
+        if (weight) loc += (double)v * (double)weight[k];
+        else loc += (double)v;
     }
     for (int o = 16; o; o >>= 1) loc += __shfl_xor_sync(0xffffffffu, loc, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, loc);
@@ -249,7 +251,8 @@ void stage_points(Ctx& c) {
     float* x27 = build_x27(c, c.base[c.D]);
     EvalArgs a{c.nodes, c.D, c.basis, c.x, x27, x27 ? c.base[c.D] : 0, nullptr};
     const int kt = c.kbegin("point_values", (double)c.N * (12 + 4 + 4) + (double)c.nodes.M * (4 + 4 + 8 + 108));
-    k_point_values<<<grid_for(c.N, 128, 1ll << 30), 128, 0, s>>>(a, c.pts, c.point_node, c.N, c.point_value, sum);
+    k_point_values<<<grid_for(c.N, 128, 1ll << 30), 128, 0, s>>>(a, c.pts, c.point_node, c.N, c.point_weight,
+                                                                 c.point_value, sum);
     CK_LAUNCH();
     c.kend(kt);
     double h = read_scalar(sum, s);

@@ -459,15 +459,116 @@ __global__ void k_div_sum_thread(const int* __restrict__ nchunks, const int* __r
     }
 }
 
+// ---- density weights (params.density_weights; not in the reference)
+// Kazhdan's weighting of non-uniform samples: at the kernel depth k, node o
+// collects w_o = sum over the points p around it of B_o(p) (B_o the depth-k basis
+// function of o, a product of its three axis functions); a point's density is
+// W(s) = sum over the 27 depth-k nodes around it of B_o(s) w_o, and its weight
+// 1/W(s), scaled to mean 1, multiplies its normal and its share of the iso-value.
+__device__ __forceinline__ float node_basis_at(const CPoly* basis, int d, const int c[3], const float p[3]) {
+    const int off = (1 << d) - 1;
+    return cpoly_value<3>(basis[off + c[0]], p[0]) * cpoly_value<3>(basis[off + c[1]], p[1]) *
+           cpoly_value<3>(basis[off + c[2]], p[2]);
+}
+
+__global__ void k_density_nodes(NodeArrays nd, i64 lo, i64 hi, int k, int D, const CPoly* __restrict__ basis,
+                                const float* __restrict__ pts, float* __restrict__ w) {
+    const i64 M = nd.M;
+    for (i64 o = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; o < hi; o += (i64)gridDim.x * blockDim.x) {
+        int c[3];
+        key_coords(nd.key[o], k, D, c);
+        float sum = 0.f;
+        for (int j = 0; j < 27; ++j) {
+            const int nb = nd.neigh[(i64)j * M + o];
+            if (nb == -1) continue;
+            const int p0 = nd.pidx[nb], pn = nd.pnum[nb];
+            for (int q = 0; q < pn; ++q) {
+                const float p[3] = {pts[3 * ((i64)p0 + q)], pts[3 * ((i64)p0 + q) + 1], pts[3 * ((i64)p0 + q) + 2]};
+                sum += node_basis_at(basis, k, c, p);
+            }
+        }
+        w[o - lo] = sum;
+    }
+}
+
+__global__ void k_density_points(NodeArrays nd, i64 n, const int* __restrict__ point_node, int k, int D, i64 lo_k,
+                                 const CPoly* __restrict__ basis, const float* __restrict__ pts,
+                                 const float* __restrict__ w, float* __restrict__ inv, double* __restrict__ sum) {
+    const i64 M = nd.M;
+    double loc = 0.0;
+    for (i64 s = (i64)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (i64)gridDim.x * blockDim.x) {
+        i64 node = point_node[s];
+        for (int d = D; d > k; --d) node = nd.parent[node];
+        const float p[3] = {pts[3 * s], pts[3 * s + 1], pts[3 * s + 2]};
+        float W = 0.f;
+        for (int j = 0; j < 27; ++j) {
+            const int nb = nd.neigh[(i64)j * M + node];
+            if (nb == -1) continue;
+            int c[3];
+            key_coords(nd.key[nb], k, D, c);
+            W += node_basis_at(basis, k, c, p) * w[nb - lo_k];
+        }
+        const float iw = W > 0.f ? 1.0f / W : 0.f;
+        inv[s] = iw;
+        loc += (double)iw;
+    }
+    for (int o = 16; o; o >>= 1) loc += __shfl_xor_sync(0xffffffffu, loc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, loc);
+}
+
+__global__ void k_weight_normals(i64 n, const double* __restrict__ sum, const float* __restrict__ nrm,
+                                 float* __restrict__ weight, float* __restrict__ wnrm) {
+    const float scale = (float)((double)n / *sum);
+    for (i64 s = (i64)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (i64)gridDim.x * blockDim.x) {
+        const float a = weight[s] * scale;
+        weight[s] = a;
+        wnrm[3 * s] = a * nrm[3 * s];
+        wnrm[3 * s + 1] = a * nrm[3 * s + 1];
+        wnrm[3 * s + 2] = a * nrm[3 * s + 2];
+    }
+}
+
+static void density_weights(Ctx& c) {
+    cudaStream_t s = c.stream;
+    const int D = c.D, k = std::max(D - 2, 1);
+    const i64 lo_k = c.base[k], hi_k = c.base[k + 1];
+    float* w = dalloc<float>(hi_k - lo_k, s);
+    double* sum = dalloc<double>(1, s);
+    CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
+    dfree(c.point_weight, s);
+    dfree(c.wnrm, s);
+    c.point_weight = dalloc<float>(c.N, s);
+    c.wnrm = dalloc<float>(3 * c.N, s);
+    const int kt = c.kbegin("density_weights", (double)c.N * (12 + 12 + 4 + 12) + (double)(hi_k - lo_k) * 120);
+    k_density_nodes<<<grid_for(hi_k - lo_k, 128), 128, 0, s>>>(c.nodes, lo_k, hi_k, k, D, c.basis, c.pts, w);
+    CK_LAUNCH();
+    k_density_points<<<grid_for(c.N, 128, (i64)c.sms * 32), 128, 0, s>>>(c.nodes, c.N, c.point_node, k, D, lo_k,
+                                                                         c.basis, c.pts, w, c.point_weight, sum);
+    CK_LAUNCH();
+    k_weight_normals<<<grid_for(c.N, 256), 256, 0, s>>>(c.N, sum, c.nrm, c.point_weight, c.wnrm);
+    CK_LAUNCH();
+    c.kend(kt);
+    dfree(w, s);
+    dfree(sum, s);
+}
+
 void stage_splat(Ctx& c) {
     cudaStream_t s = c.stream;
     const int D = c.D;
     const i64 lo = c.base[D], hi = c.base[D + 1];
     dfree(c.vfield, s);
     c.vfield = dalloc<float>(3 * (hi - lo), s);
+    const float* nrm = c.nrm;
+    if (c.params.density_weights) {
+        density_weights(c);
+        nrm = c.wnrm;
+    } else {
+        dfree(c.point_weight, s);
+        dfree(c.wnrm, s);
+    }
     // compulsory: points+normals once, finest keys and neighbour tables, V written
     const int kt = c.kbegin("splat", (double)c.N * 24 + (double)(hi - lo) * (8 + 108 + 12));
-    k_splat<<<grid_for(hi - lo, 128, 1ll << 30), 128, 0, s>>>(c.nodes, lo, hi, D, c.basis_maxdepth, c.pts, c.nrm,
+    k_splat<<<grid_for(hi - lo, 128, 1ll << 30), 128, 0, s>>>(c.nodes, lo, hi, D, c.basis_maxdepth, c.pts, nrm,
                                                                c.vfield);
     CK_LAUNCH();
     c.kend(kt);
