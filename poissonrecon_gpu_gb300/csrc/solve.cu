@@ -59,7 +59,18 @@ struct CgDepth {
     i64 lo, n;              // global row range
     int first_block, nblocks;
     float st[27];
+    // The Laplacian stencil is symmetric under the reflections and permutations of the
+    // axes (a product of symmetric 1-D tables), so entry j depends only on how many of
+    // its offsets are nonzero: cls[0] centre, [1] faces, [2] edges, [3] corners.  sym = 1
+    // when the float entries are exactly so; the matrix-vector product then keeps the
+    // four values in registers (the same values in the same FMA order).
+    float cls[4];
+    int sym;
 };
+
+__host__ __device__ constexpr int stencil_class(int j) {
+    return (j / 9 != 1) + ((j / 3) % 3 != 1) + (j % 3 != 1);
+}
 
 struct CgArgs {
     int ndepth;
@@ -212,6 +223,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     const int d = block_depth[blockIdx.x];
     const CgDepth& dp = deps[d];
     if (threadIdx.x < 27) sst[threadIdx.x] = dp.st[threadIdx.x];
+    const float cls[4] = {dp.cls[0], dp.cls[1], dp.cls[2], dp.cls[3]};
     __syncthreads();
     PartState* ps = &a.state[d];
     const int rank = blockIdx.x - dp.first_block;
@@ -306,9 +318,16 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                     if (g < ng) {
                         const float* blk = wsp + tt * 256 + gl * 64;
                         float o = 0.f;
+                        if (dp.sym) {
 #pragma unroll
-                        for (int j = 0; j < 27; ++j)
-                            o = fmaf(sst[j], blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
+                            for (int j = 0; j < 27; ++j)
+                                o = fmaf(cls[stencil_class(j)],
+                                         blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 27; ++j)
+                                o = fmaf(sst[j], blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
+                        }
                         const float pi = blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
                         pnew[dp.lo + 8 * g + ch] = pi;
                         a.q[dp.lo + 8 * g + ch] = o;
@@ -430,6 +449,13 @@ void stage_solve(Ctx& c) {
         deps[d].first_block = (int)block_depth.size();
         deps[d].nblocks = nb[d];
         for (int j = 0; j < 27; ++j) deps[d].st[j] = c.stencil[27 * d + j];
+        deps[d].sym = 1;
+        for (int j = 0; j < 27; ++j) {
+            const int k = stencil_class(j);
+            const float rep = c.stencil[27 * d + (k == 0 ? 13 : k == 1 ? 4 : k == 2 ? 1 : 0)];
+            if (c.stencil[27 * d + j] != rep) deps[d].sym = 0;
+            deps[d].cls[k] = rep;
+        }
         for (int k = 0; k < nb[d]; ++k) block_depth.push_back(d);
     }
     CgDepth* ddeps = dalloc<CgDepth>(D + 1, s);
