@@ -1,7 +1,11 @@
 // C ABI (include/prgpu.h) and stage orchestration.
+#include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "context.h"
@@ -10,7 +14,7 @@
 namespace prgpu {
 
 static thread_local char g_err[512] = {0};
-unsigned long long g_kernel_launches = 0;
+std::atomic<unsigned long long> g_kernel_launches(0);
 void set_last_error(const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -161,6 +165,8 @@ int prgpu_destroy(void* h) {
     Ctx* c = as_ctx(h);
     if (!c) return PRGPU_ERR_ARG;
     API_BEGIN
+    for (Ctx* w : c->workers) prgpu_destroy(w);
+    c->workers.clear();
     CK(cudaSetDevice(c->device));
     c->free_all();
     CK(cudaStreamSynchronize(c->stream));
@@ -307,6 +313,33 @@ int prgpu_mesh_free(prgpu_mesh* m) {
     return PRGPU_OK;
 }
 
+// a reconstructed mesh copied into memory the caller releases with prgpu_mesh_free
+static int copy_mesh_out(const prgpu_mesh& m, prgpu_mesh* out) {
+    float* vv = (float*)malloc(sizeof(float) * 3 * (size_t)std::max<int64_t>(m.n_vertices, 1));
+    int32_t* ff = (int32_t*)malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(m.n_triangles, 1));
+    if (!vv || !ff) {
+        free(vv);
+        free(ff);
+        set_last_error("host allocation failed");
+        return PRGPU_ERR_NOMEM;
+    }
+    memcpy(vv, m.vertices, sizeof(float) * 3 * (size_t)m.n_vertices);
+    memcpy(ff, m.triangles, sizeof(int32_t) * 3 * (size_t)m.n_triangles);
+    out->vertices = vv;
+    out->triangles = ff;
+    out->n_vertices = m.n_vertices;
+    out->n_triangles = m.n_triangles;
+    return PRGPU_OK;
+}
+
+// Clouds of at most BATCH_SHARED_POINTS points are reconstructed BATCH_WORKERS at a
+// time, each on a context of its own (own stream and buffers, a host thread each), so
+// that the launches and host round trips of small clouds overlap on the GPU; larger
+// clouds follow one at a time on the calling context, which bounds the memory held.
+// Every cloud's result is that of a separate reconstruction.
+constexpr int BATCH_WORKERS = 4;
+constexpr int64_t BATCH_SHARED_POINTS = 4000000;
+
 int prgpu_reconstruct_batch(void* h, const float* xyz, const float* nrm, const int64_t* offsets,
                             const int32_t* depths, int32_t ncloud, prgpu_mesh* outs) {
     Ctx* c = as_ctx(h);
@@ -320,44 +353,73 @@ int prgpu_reconstruct_batch(void* h, const float* xyz, const float* nrm, const i
         outs[k].n_vertices = outs[k].n_triangles = 0;
     }
     const int D0 = c->D;
-    int rc = PRGPU_OK;
-    for (int k = 0; k < ncloud && rc == PRGPU_OK; ++k) {
+    std::vector<int> shared, alone;
+    for (int k = 0; k < ncloud; ++k) {
         const int64_t n = offsets[k + 1] - offsets[k];
         const int d = depths ? depths[k] : D0;
         if (n <= 0 || offsets[k] < 0 || d < 2 || d > 15) {
             set_last_error("prgpu_reconstruct_batch: cloud %d: %lld points at depth %d", k, (long long)n, d);
-            rc = PRGPU_ERR_ARG;
-            break;
+            return PRGPU_ERR_ARG;
         }
-        c->D = d;
-        prgpu_mesh m;
-        rc = prgpu_reconstruct(h, xyz + 3 * offsets[k], nrm + 3 * offsets[k], n, &m);
-        if (rc) {
-            char msg[512];
-            snprintf(msg, sizeof msg, "%s", last_error());
-            set_last_error("prgpu_reconstruct_batch: cloud %d: %s", k, msg);
-            break;
-        }
-        float* vv = (float*)malloc(sizeof(float) * 3 * (size_t)std::max<int64_t>(m.n_vertices, 1));
-        int32_t* ff = (int32_t*)malloc(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(m.n_triangles, 1));
-        if (!vv || !ff) {
-            free(vv);
-            free(ff);
-            set_last_error("prgpu_reconstruct_batch: cloud %d: host allocation failed", k);
-            rc = PRGPU_ERR_NOMEM;
-            break;
-        }
-        memcpy(vv, m.vertices, sizeof(float) * 3 * (size_t)m.n_vertices);
-        memcpy(ff, m.triangles, sizeof(int32_t) * 3 * (size_t)m.n_triangles);
-        outs[k].vertices = vv;
-        outs[k].triangles = ff;
-        outs[k].n_vertices = m.n_vertices;
-        outs[k].n_triangles = m.n_triangles;
+        (n <= BATCH_SHARED_POINTS ? shared : alone).push_back(k);
     }
+    // the first failure (lowest cloud index) is reported
+    std::mutex mu;
+    int err_cloud = -1, err_rc = PRGPU_OK;
+    std::string err_msg;
+    auto fail = [&](int k, int rc) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (err_cloud < 0 || k < err_cloud) {
+            err_cloud = k;
+            err_rc = rc;
+            err_msg = last_error();
+        }
+    };
+    auto run = [&](Ctx* w, int k) -> bool {
+        w->D = depths ? depths[k] : D0;
+        prgpu_mesh m;
+        int rc = prgpu_reconstruct(w, xyz + 3 * offsets[k], nrm + 3 * offsets[k], offsets[k + 1] - offsets[k], &m);
+        if (rc == PRGPU_OK) rc = copy_mesh_out(m, &outs[k]);
+        if (rc != PRGPU_OK) fail(k, rc);
+        return rc == PRGPU_OK;
+    };
+    if (!shared.empty()) {
+        const int nw = (int)std::min<size_t>(BATCH_WORKERS, shared.size());
+        while ((int)c->workers.size() < nw) {
+            void* w = nullptr;
+            const int rc = prgpu_create(&c->params, &w);
+            if (rc != PRGPU_OK) {
+                set_last_error("prgpu_reconstruct_batch: worker context: %s", std::string(last_error()).c_str());
+                return rc;
+            }
+            c->workers.push_back(as_ctx(w));
+        }
+        std::atomic<size_t> next(0);
+        std::atomic<bool> failed(false);
+        std::vector<std::thread> th;
+        for (int wi = 0; wi < nw; ++wi)
+            th.emplace_back([&, wi]() {
+                if (cudaSetDevice(c->device) != cudaSuccess) {
+                    set_last_error("cudaSetDevice failed");
+                    fail(shared[0], PRGPU_ERR_CUDA);
+                    failed = true;
+                    return;
+                }
+                for (size_t q = next++; q < shared.size() && !failed; q = next++)
+                    if (!run(c->workers[wi], shared[q])) failed = true;
+            });
+        for (auto& t : th) t.join();
+    }
+    if (err_cloud < 0)
+        for (int k : alone)
+            if (!run(c, k)) break;
     c->D = D0;
-    if (rc)
+    if (err_cloud >= 0) {
         for (int k = 0; k < ncloud; ++k) prgpu_mesh_free(&outs[k]);
-    return rc;
+        set_last_error("prgpu_reconstruct_batch: cloud %d: %s", err_cloud, err_msg.c_str());
+        return err_rc;
+    }
+    return PRGPU_OK;
 }
 
 // ----------------------------- array access ---------------------------------
@@ -516,7 +578,7 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
              (long long)c->virtual_cells, (long long)c->total_bricks, (long long)c->live_bricks,
              (long long)c->foreign_corners, (long long)c->foreign_slow, (long long)c->super_bricks,
              (long long)c->super_decided,
-             (unsigned long long)g_kernel_launches);
+             (unsigned long long)g_kernel_launches.load());
     js += tmp;
     js += ",\"cg_iters\":[";
     for (size_t d = 0; d < c->cg_iters.size(); ++d) {
@@ -561,7 +623,7 @@ int prgpu_get_stream(void* h, void** stream) {
     return PRGPU_OK;
 }
 
-int64_t prgpu_kernel_launches(void) { return (int64_t)prgpu::g_kernel_launches; }
+int64_t prgpu_kernel_launches(void) { return (int64_t)prgpu::g_kernel_launches.load(); }
 
 int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* rowptr, const int32_t* col, const float* val, const float* rhs,
                  float* x, float tol, int32_t max_iter, int32_t* iters, float* kernel_ms) {

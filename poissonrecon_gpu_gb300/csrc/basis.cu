@@ -12,6 +12,7 @@
 //   * the Laplacian reads same-depth entries with offset 0 or 1, which are
 //     translation invariant: 27 stencil coefficients per depth.
 // The full res x res tables are built only on request (parity tests).
+#include <mutex>
 #include <vector>
 
 #include "context.h"
@@ -77,10 +78,9 @@ PP<4> to_pp(const HP& h) {
 }  // namespace
 
 static PP<4> g_B, g_dB;
-static bool g_B_ready = false;
+static std::once_flag g_B_once;
 
-static void ensure_base_function() {
-    if (g_B_ready) return;
+static void build_base_function() {
     HP c;  // ConstantFunction(0.5)
     c.n = 2;
     c.deg = 0;
@@ -99,8 +99,10 @@ static void ensure_base_function() {
         for (int i = 0; i < g_B.deg; ++i) o[i] = g_B.p[k].c[i + 1] * (float)(i + 1);
         for (int i = 0; i < 5; ++i) g_dB.p[k].c[i] = o[i];
     }
-    g_B_ready = true;
 }
+
+// the base function and its derivative, built once (contexts may run on several host threads)
+static void ensure_base_function() { std::call_once(g_B_once, build_base_function); }
 
 static CPoly to_cpoly(const PP<4>& a) {
     CPoly r;

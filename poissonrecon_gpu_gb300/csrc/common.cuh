@@ -5,6 +5,7 @@
 // rounding of each stage a property of the source, so the stages that restate
 // the reference arithmetic reproduce it bit for bit.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -36,7 +37,7 @@ const char* last_error();
         }                                                                               \
     } while (0)
 // every kernel launch is followed by CK_LAUNCH(), which also counts it
-extern unsigned long long g_kernel_launches;
+extern std::atomic<unsigned long long> g_kernel_launches;
 #define CK_LAUNCH()                            \
     do {                                       \
         ++::prgpu::g_kernel_launches;          \

@@ -71,6 +71,7 @@ struct PinnedBuf {
 
 struct Ctx {
     prgpu_params params;
+    std::vector<Ctx*> workers;          // contexts of prgpu_reconstruct_batch's host threads
     int device = 0;
     cudaStream_t stream = nullptr;
     int sms = 152;                      // multiprocessors of the device

@@ -16,6 +16,7 @@
 // arithmetic and owner rules.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "context.h"
@@ -31,7 +32,9 @@ __constant__ signed char c_pfk[8][6];        // parentFaceKind, reference layout
 __constant__ signed char c_vid[8];           // cube-vertex id of corner kind j
 __constant__ signed char c_face_edges[6][4];
 
-static bool g_mc_uploaded = false;
+// the tables go to each device's constant memory once (contexts may run on several host threads)
+static std::mutex g_mc_mu;
+static bool g_mc_uploaded[64] = {false};
 static void upload_mc_tables() {
     prgpu_mc::Tables T;
     prgpu_mc::build(T);
@@ -61,7 +64,16 @@ static void upload_mc_tables() {
     CK(cudaMemcpyToSymbol(c_pfk, pfk, sizeof pfk));
     CK(cudaMemcpyToSymbol(c_vid, vid, sizeof vid));
     CK(cudaMemcpyToSymbol(c_face_edges, fe, sizeof fe));
-    g_mc_uploaded = true;
+}
+static void ensure_mc_tables() {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_mc_mu);
+    if (dev < 0 || dev >= 64) throw Error{PRGPU_ERR_LIMIT, {0}};
+    if (!g_mc_uploaded[dev]) {
+        upload_mc_tables();
+        g_mc_uploaded[dev] = true;
+    }
 }
 
 // ----------------------------- evaluation ----------------------------------
@@ -1806,7 +1818,7 @@ __global__ void k_gather_ntri32(const int* __restrict__ ntri, const int* __restr
 }
 
 void stage_mesh(Ctx& c) {
-    if (!g_mc_uploaded) upload_mc_tables();
+    ensure_mc_tables();
     cudaStream_t s = c.stream;
     const int D = c.D;
     const NodeArrays& nd = c.nodes;
