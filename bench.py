@@ -185,6 +185,54 @@ def measured_traffic(args):
     return out
 
 
+def file_io_pass(r, xyz, nrm, steps):
+    """The same reconstruction from a binary PLY file to a PLY file through the C ABI
+    (prgpu_read_points, prgpu_reconstruct, prgpu_write_mesh_ply): host wall time per step,
+    file I/O included; the mesh is written binary (timed) and ascii (timed apart)."""
+    import shutil
+    import tempfile
+    import poissonrecon_gpu_gb300 as pg
+    L = pg._lib()
+    d = tempfile.mkdtemp(prefix="prgpu_bench_")
+    try:
+        src = os.path.join(d, "points.ply")
+        with open(src, "wb") as fh:
+            fh.write(b"ply\nformat binary_little_endian 1.0\nelement vertex %d\n" % len(xyz))
+            for k in ("x", "y", "z", "nx", "ny", "nz"):
+                fh.write(b"property float %s\n" % k.encode())
+            fh.write(b"end_header\n")
+            fh.write(np.concatenate([xyz, nrm], 1).astype("<f4").tobytes())
+        out_b, out_a = os.path.join(d, "mesh_bin.ply"), os.path.join(d, "mesh_ascii.ply")
+        rd, rc_, wb, wa = [], [], [], []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            n = ctypes.c_int64(0)
+            px, pn = ctypes.c_void_p(), ctypes.c_void_p()
+            if L.prgpu_read_points(src.encode(), ctypes.byref(n), ctypes.byref(px), ctypes.byref(pn)):
+                raise pg.PrgpuError(1, "prgpu_read_points")
+            t1 = time.perf_counter()
+            m = pg.Mesh()
+            rc = L.prgpu_reconstruct(r._h, px, pn, n.value, ctypes.byref(m))
+            if rc not in (0, 5):
+                raise pg.PrgpuError(rc, "prgpu_reconstruct")
+            t2 = time.perf_counter()
+            if L.prgpu_write_mesh_ply(out_b.encode(), ctypes.byref(m), 1):
+                raise pg.PrgpuError(1, "prgpu_write_mesh_ply")
+            t3 = time.perf_counter()
+            if L.prgpu_write_mesh_ply(out_a.encode(), ctypes.byref(m), 0):
+                raise pg.PrgpuError(1, "prgpu_write_mesh_ply")
+            t4 = time.perf_counter()
+            rd.append(t1 - t0); rc_.append(t2 - t1); wb.append(t3 - t2); wa.append(t4 - t3)
+        med = lambda v: float(np.median(v)) * 1e3
+        total = med(np.array(rd) + np.array(rc_) + np.array(wb))
+        return {"value": len(xyz) / (total * 1e-3), "unit": "points/s", "ms_per_step": total,
+                "read_ms": med(rd), "reconstruct_ms": med(rc_), "write_binary_ms": med(wb),
+                "write_ascii_ms": med(wa), "host_threads": os.cpu_count(),
+                "path": "binary PLY in, binary PLY out (ascii output timed apart), host wall time"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def max_over_ranks(values, device):
     """Replicas: every rank times its own reconstruction; the job's time is the slowest rank's."""
     import torch
@@ -318,6 +366,8 @@ def main():
         "nodes": stats.get("nodes"),
         "mesh": {"vertices": nv, "triangles": nt},
     }
+    if world == 1:
+        out["file_e2e"] = file_io_pass(r, xyz, nrm, max(args.steps, 3))
     if os.environ.get("PRGPU_BENCH_NO_CPU") != "1":
         cpu, _ = cpu_reference(args, 1, 0)
         out["cpu_baseline"] = cpu
