@@ -155,7 +155,6 @@ int prgpu_create(const prgpu_params* p, void** out) {
     CK(cudaDeviceGetDefaultMemPool(&pool, c->device));
     uint64_t thr = ~0ull;
     CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    upload_luts();
     *out = c;
     return PRGPU_OK;
     API_END

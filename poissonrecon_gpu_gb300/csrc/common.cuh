@@ -52,11 +52,10 @@ inline unsigned grid_for(i64 n, int block, i64 cap = (i64)152 * 64) {
 }
 
 // ---------------------------------------------------------------------------
-// neighbour lookup tables (main.cu:80-99): neighbour j = 9(dx+1)+3(dy+1)+(dz+1);
-// child code = x<<2 | y<<1 | z.  The tables live in octree.cu's constant bank
-// and are filled from their definition at context creation.
+// neighbour numbering (main.cu:80-99): neighbour j = 9(dx+1)+3(dy+1)+(dz+1);
+// child code = x<<2 | y<<1 | z.  k_neighbours computes the reference's lookup
+// tables' values from this definition.
 // ---------------------------------------------------------------------------
-void upload_luts();
 
 // ---------------------------------------------------------------------------
 // keys: 3 bits per level, level 1 most significant; x bit 2, y bit 1, z bit 0.

@@ -18,24 +18,6 @@
 
 namespace prgpu {
 
-__constant__ int c_lut_parent[8][27];
-__constant__ int c_lut_child[8][27];
-
-void upload_luts() {
-    int lp[8][27], lc[8][27];
-    for (int s = 0; s < 8; ++s) {
-        int cx = (s >> 2) & 1, cy = (s >> 1) & 1, cz = s & 1;
-        for (int j = 0; j < 27; ++j) {
-            int tx = cx + j / 9 - 1, ty = cy + (j / 3) % 3 - 1, tz = cz + j % 3 - 1;
-            int px = (tx + 2) / 2 - 1, py = (ty + 2) / 2 - 1, pz = (tz + 2) / 2 - 1;
-            lp[s][j] = 9 * (px + 1) + 3 * (py + 1) + (pz + 1);
-            lc[s][j] = ((tx & 1) << 2) | ((ty & 1) << 1) | (tz & 1);
-        }
-    }
-    CK(cudaMemcpyToSymbol(c_lut_parent, lp, sizeof lp));
-    CK(cudaMemcpyToSymbol(c_lut_child, lc, sizeof lc));
-}
-
 // --------------------------- bounding box -----------------------------------
 __device__ __forceinline__ unsigned f2ord(float f) {
     unsigned u = __float_as_uint(f);
@@ -227,21 +209,42 @@ __global__ void k_root(NodeArrays nd, i64 N, i64 countD, i64 M) {
 
 // computeNeighbor (main.cu:492-509): neighbour j of a node is a child of one of
 // its parent's neighbours
-__global__ void k_neighbours(NodeArrays nd, i64 lo, i64 hi, int shift) {
+// Neighbours of depth d from those of depth d-1 (main.cu:492-509): neighbour j of
+// child s of P is child (s + off_j) & 1 of P's neighbour (s + off_j) >> 1 per axis,
+// the values the reference's LUTs tabulate (main.cu:80-99).  The 8 children of a
+// node are contiguous, so a warp takes 4 sibling groups: the first children of
+// each parent's 27 neighbours are loaded once per group into shared memory, then
+// every lane writes its node's 27 neighbours (coalesced along the nodes).
+__global__ void __launch_bounds__(256) k_neighbours(NodeArrays nd, i64 lo, i64 ng) {
+    __shared__ int cn[8][4][27];
     const i64 M = nd.M;
-    for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
-        const int son = (int)((nd.key[i] >> shift) & 7);
-        const int p = nd.parent[i];
-#pragma unroll 3
-        for (int j = 0; j < 27; ++j) {
-            int np = nd.neigh[(i64)c_lut_parent[son][j] * M + p];
-            int r = -1;
-            if (np != -1) {
-                int c0 = nd.child0[np];
-                if (c0 != -1) r = c0 + c_lut_child[son][j];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    for (i64 tile = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile * 4 < ng; tile += nwarps) {
+        for (int e = lane; e < 4 * 27; e += 32) {
+            const i64 g = tile * 4 + e / 27;
+            int v = -1;
+            if (g < ng) {
+                const int p = nd.parent[lo + 8 * g];
+                const int np = nd.neigh[(i64)(e % 27) * M + p];
+                if (np != -1) v = nd.child0[np];
             }
-            nd.neigh[(i64)j * M + i] = r;
+            cn[w][e / 27][e % 27] = v;
         }
+        __syncwarp();
+        const i64 g = tile * 4 + (lane >> 3);
+        if (g < ng) {
+            const int s = lane & 7, sx = s >> 2, sy = (s >> 1) & 1, sz = s & 1;
+            const i64 i = lo + 8 * g + s;
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                const int ax = sx + j / 9 - 1, ay = sy + (j / 3) % 3 - 1, az = sz + j % 3 - 1;
+                const int jp = 9 * ((ax >> 1) + 1) + 3 * ((ay >> 1) + 1) + ((az >> 1) + 1);
+                const int c0 = cn[w][lane >> 3][jp];
+                nd.neigh[(i64)j * M + i] = c0 == -1 ? -1 : c0 + (((ax & 1) << 2) | ((ay & 1) << 1) | (az & 1));
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -405,7 +408,7 @@ void stage_octree(Ctx& c) {
     // ---- neighbours, top-down
     const int kn = c.kbegin("neighbours", (double)M * (108 + 8 + 4 + 4));
     for (int d = 1; d <= D; ++d) {
-        k_neighbours<<<grid_for(c.count[d], 256), 256, 0, s>>>(nd, c.base[d], c.base[d + 1], 3 * (D - d));
+        k_neighbours<<<grid_for(c.count[d] / 8 * 8, 256), 256, 0, s>>>(nd, c.base[d], c.count[d] / 8);
         CK_LAUNCH();
     }
     c.kend(kn);
