@@ -13,49 +13,74 @@ __device__ __forceinline__ float finest_center(int off, int D) {
     return (float)((0.5 + (double)off) * (double)w);
 }
 
-// One thread per finest slot, neighbours and their points in the reference's
-// order; the splat weight is (F/F(0)) scaled to the finest width, shifted to
-// the sample and evaluated at the node centre (main.cu:913-964).
-__global__ void k_splat(NodeArrays nd, i64 lo, i64 hi, int D, CPoly f, const float* __restrict__ pts,
-                        const float* __restrict__ nrm, float* __restrict__ vfield) {
-    const i64 M = nd.M;
-    for (i64 i = lo + (i64)blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += (i64)gridDim.x * blockDim.x) {
+// One lane per finest slot, neighbours and their points in the reference's order;
+// the splat weight is (F/F(0)) scaled to the finest width, shifted to the sample
+// and evaluated at the node centre (main.cu:913-964).  A warp takes 4 sibling
+// groups: the 27-neighbourhoods of a group's 8 nodes are the 4x4x4 block of the
+// children of the parent's 27 neighbours (the group table), whose point ranges
+// are staged once per group; each lane then runs its node's (neighbour, point)
+// pairs in neighbour order in one flat loop, so that the lanes stay together.
+constexpr int SPLAT_BLOCK = 128;
+__global__ void __launch_bounds__(SPLAT_BLOCK) k_splat(NodeArrays nd, const int* __restrict__ gn, i64 ngroups_all,
+                                                       i64 gfirst, i64 ng, i64 lo, int D, CPoly f,
+                                                       const float* __restrict__ pts, const float* __restrict__ nrm,
+                                                       float* __restrict__ vfield) {
+    __shared__ int2 rng[SPLAT_BLOCK / 32][4][64];   // (first point, count) of each block cell
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    for (i64 tile = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile * 4 < ng; tile += nwarps) {
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const int e = lane + 32 * m;
+            const i64 g = tile * 4 + (e >> 6);
+            const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
+            int2 r = make_int2(0, 0);
+            if (g < ng) {
+                const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
+                const int cn = gn[(i64)jp * ngroups_all + gfirst + g];
+                if (cn != -1) {
+                    const int node = cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1));
+                    r = make_int2(nd.pidx[node], nd.pnum[node]);
+                }
+            }
+            rng[w][e >> 6][cell] = r;
+        }
+        __syncwarp();
+        const i64 g = tile * 4 + (lane >> 3);
+        if (g >= ng) continue;
+        const int s = lane & 7, sx = s >> 2, sy = (s >> 1) & 1, sz = s & 1;
+        const i64 i = lo + 8 * g + s;
         int xyz[3];
         key_coords(nd.key[i], D, D, xyz);
         const float oc0 = finest_center(xyz[0], D), oc1 = finest_center(xyz[1], D), oc2 = finest_center(xyz[2], D);
+        const int2* br = rng[w][lane >> 3];
+        int T = 0;
+#pragma unroll
+        for (int j = 0; j < 27; ++j) T += br[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)].y;
         float v0 = 0.f, v1 = 0.f, v2 = 0.f;
-        // the 27 neighbours' indices, then their point ranges, loaded together; then the
-        // node's (neighbour, point) pairs in neighbour order by one flat loop, so that a
-        // warp's lanes run the same iteration whatever their neighbours' point counts
-        int p0s[27], pns[27], T = 0;
-        {
-            int nbs[27];
-#pragma unroll
-            for (int j = 0; j < 27; ++j) nbs[j] = nd.neigh[(i64)j * M + i];
-#pragma unroll
-            for (int j = 0; j < 27; ++j) {
-                p0s[j] = nbs[j] == -1 ? 0 : nd.pidx[nbs[j]];
-                pns[j] = nbs[j] == -1 ? 0 : nd.pnum[nbs[j]];
-                T += pns[j];
-            }
-        }
         int j = 0, k = 0;
+        int2 cur = br[sx * 16 + sy * 4 + sz];
         for (int t = 0; t < T; ++t) {
-            while (k >= pns[j]) { ++j; k = 0; }
-            const i64 pt = (i64)p0s[j] + k;
+            while (k >= cur.y) {
+                ++j;
+                k = 0;
+                cur = br[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)];
+            }
+            const i64 pt = (i64)cur.x + k;
             ++k;
             const float px = pts[3 * pt], py = pts[3 * pt + 1], pz = pts[3 * pt + 2];
-            CPoly sx, sy, sz;
-            cpoly_shift<2>(f, px, sx);
-            cpoly_shift<2>(f, py, sy);
-            cpoly_shift<2>(f, pz, sz);
-            const float wx = cpoly_value<2>(sx, oc0);
-            const float wy = cpoly_value<2>(sy, oc1);
-            const float wz = cpoly_value<2>(sz, oc2);
-            const float w = wx * wy * wz;
-            v0 = fmaf(w, nrm[3 * pt], v0);
-            v1 = fmaf(w, nrm[3 * pt + 1], v1);
-            v2 = fmaf(w, nrm[3 * pt + 2], v2);
+            CPoly cx, cy, cz;
+            cpoly_shift<2>(f, px, cx);
+            cpoly_shift<2>(f, py, cy);
+            cpoly_shift<2>(f, pz, cz);
+            const float wx = cpoly_value<2>(cx, oc0);
+            const float wy = cpoly_value<2>(cy, oc1);
+            const float wz = cpoly_value<2>(cz, oc2);
+            const float wgt = wx * wy * wz;
+            v0 = fmaf(wgt, nrm[3 * pt], v0);
+            v1 = fmaf(wgt, nrm[3 * pt + 1], v1);
+            v2 = fmaf(wgt, nrm[3 * pt + 2], v2);
         }
         const i64 o = i - lo;
         vfield[3 * o] = v0;
@@ -568,8 +593,12 @@ void stage_splat(Ctx& c) {
     }
     // compulsory: points+normals once, finest keys and neighbour tables, V written
     const int kt = c.kbegin("splat", (double)c.N * 24 + (double)(hi - lo) * (8 + 108 + 12));
-    k_splat<<<grid_for(hi - lo, 128, 1ll << 30), 128, 0, s>>>(c.nodes, lo, hi, D, c.basis_maxdepth, c.pts, nrm,
-                                                               c.vfield);
+    ensure_group_table(c);
+    {
+        const i64 ngroups_all = (c.nodes.M - 1) / 8, gfirst = (lo - 1) / 8, ng = (hi - lo) / 8;
+        k_splat<<<grid_for(ng * 8, SPLAT_BLOCK, 1ll << 30), SPLAT_BLOCK, 0, s>>>(
+            c.nodes, c.gn, ngroups_all, gfirst, ng, lo, D, c.basis_maxdepth, c.pts, nrm, c.vfield);
+    }
     CK_LAUNCH();
     c.kend(kt);
 }
