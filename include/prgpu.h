@@ -108,11 +108,11 @@ int prgpu_reconstruct(void* ctx, const float* xyz, const float* nrm, int64_t n, 
  * reconstructed at maxDepth depths[k] (the context's depth when depths is NULL).
  * Clouds of at most 4M points run four at a time on worker contexts the context
  * keeps (own stream, buffers and host thread each, released by prgpu_destroy),
- * larger ones one at a time; every mesh is that of a separate reconstruction.  outs[k] receives a copy
- * of the mesh in memory the caller releases with prgpu_mesh_free.  The reference
- * has no counterpart (one cloud per process run, main.cu:3247-4573); it is the
- * batched form of prgpu_reconstruct.  On error, the meshes already produced are
- * released and the error names the cloud. */
+ * larger ones one at a time; every mesh is that of a separate reconstruction.
+ * outs[k] receives a copy of the mesh in memory the caller releases with
+ * prgpu_mesh_free.  The reference has no counterpart (one cloud per process run,
+ * main.cu:3247-4573); it is the batched form of prgpu_reconstruct.  On error, the
+ * meshes already produced are released and the error names the cloud. */
 int prgpu_reconstruct_batch(void* ctx, const float* xyz, const float* nrm, const int64_t* offsets,
                             const int32_t* depths, int32_t ncloud, prgpu_mesh* outs);
 
