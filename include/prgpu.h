@@ -89,6 +89,11 @@ int prgpu_compute_rhs(void* ctx);
  * Replaces LaplacianIteration (main.cu:1223-1332) and solverCG_DeviceToDevice. */
 int prgpu_solve(void* ctx);
 
+/* One depth's system L_d x_d = b_d (0 <= depth <= maxDepth) with the given
+ * prgpu_solve_mode; the other depths' rows of x keep their values (0 before any
+ * solve).  The body of LaplacianIteration's per-depth loop (main.cu:1237-1329). */
+int prgpu_solve_depth(void* ctx, int32_t depth, int32_t mode);
+
 /* Implicit function at the input points and the iso-value.
  * Replaces calculatePointsImplicitFunctionValue + reduce (main.cu:1334-1381,3480-3499). */
 int prgpu_eval_points(void* ctx, float* iso_out);
@@ -118,6 +123,27 @@ int prgpu_reconstruct_batch(void* ctx, const float* xyz, const float* nrm, const
 
 /* Releases a mesh returned by prgpu_reconstruct_batch and zeroes it. */
 int prgpu_mesh_free(prgpu_mesh* mesh);
+
+/* The octree as the reference's OctNode fields (OctNode.cuh:8-41), structure of
+ * arrays in caller-allocated host memory: n_nodes and max_depth are filled in,
+ * and every non-NULL array is copied (base: max_depth + 2 entries, the first node
+ * of each depth and the total; children: 8 and neighs: 27 per node; the others
+ * one per node).  Call once with NULL arrays to learn n_nodes.  Replaces the
+ * NodeArray output of pipelineBuildNodeArray (main.cu:511-513). */
+typedef struct {
+    int64_t n_nodes;
+    int32_t max_depth;
+    int64_t* base;
+    uint64_t* key;
+    int32_t* pidx;
+    int32_t* pnum;
+    int32_t* parent;
+    int32_t* children;
+    int32_t* neighs;
+    int32_t* didx;
+    int32_t* dnum;
+} prgpu_node_arrays;
+int prgpu_get_node_arrays(void* ctx, prgpu_node_arrays* out);
 
 /* Copy an internal array to host memory.  Names: "key","pidx","pnum","parent",
  * "children","neighs","didx","dnum","base","count","points","normals",

@@ -61,6 +61,13 @@ class Mesh(ctypes.Structure):
                 ("vertices", ctypes.POINTER(ctypes.c_float)), ("triangles", ctypes.POINTER(ctypes.c_int32))]
 
 
+class NodeArrays(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int64), ("max_depth", ctypes.c_int32),
+                ("base", ctypes.c_void_p), ("key", ctypes.c_void_p), ("pidx", ctypes.c_void_p),
+                ("pnum", ctypes.c_void_p), ("parent", ctypes.c_void_p), ("children", ctypes.c_void_p),
+                ("neighs", ctypes.c_void_p), ("didx", ctypes.c_void_p), ("dnum", ctypes.c_void_p)]
+
+
 # every entry point of include/prgpu.h with its ctypes signature
 _VP, _I64, _I32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
 SIGNATURES = {
@@ -72,6 +79,8 @@ SIGNATURES = {
     "prgpu_build_octree": (ctypes.c_int, [_VP]),
     "prgpu_compute_rhs": (ctypes.c_int, [_VP]),
     "prgpu_solve": (ctypes.c_int, [_VP]),
+    "prgpu_solve_depth": (ctypes.c_int, [_VP, _I32, _I32]),
+    "prgpu_get_node_arrays": (ctypes.c_int, [_VP, ctypes.POINTER(NodeArrays)]),
     "prgpu_eval_points": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float)]),
     "prgpu_extract_mesh": (ctypes.c_int, [_VP]),
     "prgpu_get_mesh": (ctypes.c_int, [_VP, ctypes.POINTER(Mesh)]),
@@ -169,6 +178,29 @@ class Reconstructor:
             return False
         _check(rc, "prgpu_solve")
         return True
+
+    def solve_depth(self, depth: int, mode: int = SOLVE_REFERENCE, allow_not_converged: bool = True):
+        """One depth's system (prgpu_solve_depth); the other depths' x are kept."""
+        rc = _lib().prgpu_solve_depth(self._h, depth, mode)
+        if rc == 5 and allow_not_converged:
+            return False
+        _check(rc, "prgpu_solve_depth")
+        return True
+
+    def node_arrays(self) -> dict:
+        """The octree as the reference's OctNode fields (prgpu_get_node_arrays)."""
+        L = _lib()
+        na = NodeArrays()
+        _check(L.prgpu_get_node_arrays(self._h, ctypes.byref(na)), "prgpu_get_node_arrays")
+        M, D = na.n_nodes, na.max_depth
+        out = {"base": np.zeros(D + 2, np.int64), "key": np.zeros(M, np.uint64), "pidx": np.zeros(M, np.int32),
+               "pnum": np.zeros(M, np.int32), "parent": np.zeros(M, np.int32),
+               "children": np.zeros(8 * M, np.int32), "neighs": np.zeros(27 * M, np.int32),
+               "didx": np.zeros(M, np.int32), "dnum": np.zeros(M, np.int32)}
+        for k, a in out.items():
+            setattr(na, k, a.ctypes.data)
+        _check(L.prgpu_get_node_arrays(self._h, ctypes.byref(na)), "prgpu_get_node_arrays")
+        return out
 
     def eval_points(self) -> float:
         iso = ctypes.c_float(0)

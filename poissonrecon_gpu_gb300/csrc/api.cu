@@ -255,6 +255,21 @@ int prgpu_solve(void* h) {
     API_END
 }
 
+int prgpu_solve_depth(void* h, int32_t depth, int32_t mode) {
+    Ctx* c = as_ctx(h);
+    REQUIRE_STAGE(c, 3);
+    if (depth < 0 || depth > c->D || (mode != PRGPU_SOLVE_REFERENCE && mode != PRGPU_SOLVE_RELATIVE)) {
+        set_last_error("prgpu_solve_depth: depth %d (maxDepth %d), mode %d", depth, c->D, mode);
+        return PRGPU_ERR_ARG;
+    }
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    timed(*c, c->t.solve_ms, [&] { stage_solve_depths(*c, depth, depth, mode); });
+    c->stage = std::max(c->stage, 4);
+    return c->cg_iters[depth] >= c->params.cg_max_iter ? PRGPU_ERR_NOT_CONVERGED : PRGPU_OK;
+    API_END
+}
+
 int prgpu_eval_points(void* h, float* iso_out) {
     Ctx* c = as_ctx(h);
     REQUIRE_STAGE(c, 4);
@@ -445,6 +460,28 @@ static int copy_out(Ctx* c, const void* dsrc, int64_t bytes, void* dst, int64_t 
     if (host_src) { memcpy(dst, dsrc, (size_t)bytes); return PRGPU_OK; }
     CK(cudaMemcpyAsync(dst, dsrc, (size_t)bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return PRGPU_OK;
+}
+
+int prgpu_get_node_arrays(void* h, prgpu_node_arrays* out) {
+    Ctx* c = as_ctx(h);
+    if (!c || !out) return PRGPU_ERR_ARG;
+    REQUIRE_STAGE(c, 2);
+    const int64_t M = c->nodes.M;
+    out->n_nodes = M;
+    out->max_depth = c->D;
+    struct Field { const char* name; void* dst; int64_t bytes; };
+    const Field fields[] = {{"base", out->base, (int64_t)(c->D + 2) * 8}, {"key", out->key, M * 8},
+                            {"pidx", out->pidx, M * 4},     {"pnum", out->pnum, M * 4},
+                            {"parent", out->parent, M * 4}, {"children", out->children, M * 32},
+                            {"neighs", out->neighs, M * 108}, {"didx", out->didx, M * 4},
+                            {"dnum", out->dnum, M * 4}};
+    for (const Field& f : fields) {
+        if (!f.dst) continue;
+        int64_t got = 0;
+        const int rc = prgpu_get_array(h, f.name, f.dst, f.bytes, &got);
+        if (rc != PRGPU_OK) return rc;
+    }
     return PRGPU_OK;
 }
 

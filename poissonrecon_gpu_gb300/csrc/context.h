@@ -108,6 +108,7 @@ struct Ctx {
     float* wnrm = nullptr;           // 3N: the normals times the density weights
     float* divergence = nullptr;     // M
     float* x = nullptr;              // M
+    i64 x_rows = 0;                  // rows x was allocated for
     std::vector<int> cg_iters;
     std::vector<float> cg_rr;
     int* d_cg_iters = nullptr;
@@ -156,6 +157,7 @@ void stage_full_tables(Ctx& c);
 void stage_splat(Ctx& c);
 void stage_divergence(Ctx& c);
 void stage_solve(Ctx& c);
+void stage_solve_depths(Ctx& c, int d0, int d1, int mode);
 void ensure_group_table(Ctx& c);
 void stage_points(Ctx& c);
 void stage_mesh(Ctx& c);

@@ -392,12 +392,24 @@ void ensure_group_table(Ctx& c) {
     }
 }
 
-void stage_solve(Ctx& c) {
+void stage_solve_depths(Ctx& c, int d0, int d1, int mode);
+void stage_solve(Ctx& c) { stage_solve_depths(c, 0, c.D, c.params.solve_mode); }
+
+// depths d0..d1 with the given mode; the other depths' rows of x are left as they are
+void stage_solve_depths(Ctx& c, int d0, int d1, int mode) {
     cudaStream_t s = c.stream;
     const int D = c.D;
     const i64 M = c.nodes.M;
-    dfree(c.x, s);
-    c.x = dalloc<float>(M, s);
+    if (d0 == 0 && d1 == D) {   // every row is written
+        dfree(c.x, s);
+        c.x = dalloc<float>(M, s);
+        c.x_rows = M;
+    } else if (!c.x || c.x_rows != M) {   // the other depths start at 0
+        dfree(c.x, s);
+        c.x = dalloc<float>(M, s);
+        c.x_rows = M;
+        CK(cudaMemsetAsync(c.x, 0, M * sizeof(float), s));
+    }
     float* r = dalloc<float>(M, s);
     float* p = dalloc<float>(M, s);
     float* q = dalloc<float>(M, s);
@@ -414,16 +426,17 @@ void stage_solve(Ctx& c) {
     const int G = sms * per_sm;
     // partition: one block per small depth, the rest in proportion to rows
     std::vector<CgDepth> deps(D + 1);
-    std::vector<int> nb(D + 1, 1);
+    std::vector<int> nb(D + 1, 0);
     i64 big_rows = 0;
     const i64 small_rows = 4 * CG_BLOCK;
     int fixed = 0;
-    for (int d = 0; d <= D; ++d) {
+    for (int d = d0; d <= d1; ++d) {
+        nb[d] = 1;
         if (c.count[d] <= small_rows) ++fixed;
         else big_rows += c.count[d];
     }
     int avail = std::max(0, G - fixed);
-    for (int d = 0; d <= D; ++d) {
+    for (int d = d0; d <= d1; ++d) {
         if (c.count[d] > small_rows) {
             i64 want = (i64)((double)avail * (double)c.count[d] / (double)std::max<i64>(big_rows, 1));
             i64 cap = (c.count[d] + CG_BLOCK - 1) / CG_BLOCK;
@@ -471,7 +484,7 @@ void stage_solve(Ctx& c) {
     CK(cudaMemsetAsync(err, 0, sizeof(int), s));
     CgArgs a;
     a.ndepth = D + 1;
-    a.mode = c.params.solve_mode;
+    a.mode = mode;
     const float tolf = (float)c.params.cg_tol;
     a.tol2 = tolf * tolf;
     a.rel2 = c.params.cg_tol * c.params.cg_tol;
@@ -500,15 +513,17 @@ void stage_solve(Ctx& c) {
     CK(cudaMemcpyAsync(hs.data(), st, (D + 1) * sizeof(PartState), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    c.cg_iters.assign(D + 1, 0);
-    c.cg_rr.assign(D + 1, 0.f);
-    for (int d = 0; d <= D; ++d) { c.cg_iters[d] = hs[d].iters; c.cg_rr[d] = hs[d].rr; }
+    if ((int)c.cg_iters.size() != D + 1 || (d0 == 0 && d1 == D)) {
+        c.cg_iters.assign(D + 1, 0);
+        c.cg_rr.assign(D + 1, 0.f);
+    }
+    for (int d = d0; d <= d1; ++d) { c.cg_iters[d] = hs[d].iters; c.cg_rr[d] = hs[d].rr; }
     if (kt >= 0) {
         // compulsory per row and iteration: the group table (27 indices per 8 rows), the
         // previous direction and r read once, p and q written, then p/q/x/r read and x/r
         // written (8 words)
         double bytes = 0;
-        for (int d = 0; d <= D; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 8 * 4);
+        for (int d = d0; d <= d1; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 8 * 4);
         c.kpending[kt].bytes = bytes;
     }
     dfree(r, s); dfree(p, s); dfree(p2, s); dfree(q, s);

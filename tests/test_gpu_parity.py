@@ -304,3 +304,41 @@ def test_density_weights_remove_sparse_side_sheets(lib_built):
     r.close()
     x = xyz[order, 0]
     assert w[x < 0.3].mean() > 3 * w[x > 0.7].mean()
+
+
+def test_solve_depth_and_node_arrays(lib_built, oracle_mod):
+    """prgpu_solve_depth: solving the depths one call each gives the all-depth solve (the depths are
+    independent systems; the reduction partitions differ, so within the CG tolerance), and a depth
+    solved alone leaves the others' x untouched.  prgpu_get_node_arrays: the reference's OctNode
+    fields, equal to the named arrays and to the oracle's."""
+    import poissonrecon_gpu_gb300 as pg
+    xyz, nrm = sphere(5000, seed=2)
+    depth = 6
+    a = pg.Reconstructor(depth=depth)
+    a.set_points(xyz, nrm); a.build_octree(); a.compute_rhs(); a.solve()
+    xa = a.get("x")
+    b = pg.Reconstructor(depth=depth)
+    b.set_points(xyz, nrm); b.build_octree(); b.compute_rhs()
+    base = b.get("base")
+    b.solve_depth(depth, pg.SOLVE_REFERENCE)
+    xb = b.get("x")
+    assert np.all(xb[: base[depth]] == 0.0)          # the other depths are untouched
+    for d in range(depth):
+        b.solve_depth(d, pg.SOLVE_REFERENCE)
+    xb = b.get("x")
+    for d in range(depth + 1):
+        sl = slice(base[d], base[d + 1])
+        assert np.abs(xb[sl] - xa[sl]).max() <= 1e-4 * max(np.abs(xa[sl]).max(), 1e-30), d
+    assert np.all(np.abs(b.get("cg_iters") - a.get("cg_iters")) <= 2)
+    with pytest.raises(pg.PrgpuError):
+        b.solve_depth(depth + 1, pg.SOLVE_REFERENCE)
+    na = b.node_arrays()
+    for f in ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum", "base"):
+        assert np.array_equal(na[f], b.get(f)), f
+    o = oracle_mod.Oracle(depth)
+    o.set_points(xyz, nrm)
+    o.build_octree()
+    for f in ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum"):
+        assert np.array_equal(na[f].astype(np.int64), o.get(f).astype(np.int64)), f
+    a.close()
+    b.close()
