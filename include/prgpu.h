@@ -7,6 +7,9 @@
  * point below replaces one of those stages; the comment on each names the
  * reference code it stands in for.  Conventions:
  *   - every function returns a prgpu_status (0 = success) and never throws;
+ *     when a stage fails (CUDA error, allocation, limit, timeout), the context
+ *     releases its device buffers and needs its points again; nothing the
+ *     failed call allocated stays behind;
  *   - a context owns one CUDA stream and all device buffers of one
  *     reconstruction; it is not thread safe, distinct contexts are independent;
  *   - host pointers are caller owned; arrays returned through prgpu_mesh are

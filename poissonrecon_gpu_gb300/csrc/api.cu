@@ -106,13 +106,42 @@ static void timed(Ctx& c, float& acc, F&& f) {
 
 using namespace prgpu;
 
-#define API_BEGIN try {
+namespace prgpu {
+thread_local LiveAllocs* g_live = nullptr;
+}
+
+// One API call: collects the call's device allocations.  When the call fails, the
+// context (if given) releases its buffers and must be given its points again (stage
+// 0), then the call's remaining allocations -- temporaries of the stage that failed --
+// are freed, so repeated failures do not accumulate device memory.
+struct CallScope {
+    LiveAllocs live;
+    LiveAllocs* prev;
+    Ctx* c;
+    explicit CallScope(Ctx* ctx) : prev(g_live), c(ctx) { g_live = &live; }
+    ~CallScope() { g_live = prev; }
+    void fail() {
+        if (c) {
+            c->free_all();
+            c->stage = 0;
+        }
+        for (auto& a : live.v) cudaFreeAsync(a.first, a.second);
+        live.v.clear();
+    }
+};
+
+#define API_BEGIN_CTX(ctx) \
+    CallScope scope_(ctx); \
+    try {
+#define API_BEGIN API_BEGIN_CTX(nullptr)
 #define API_END                                                   \
     }                                                             \
     catch (const prgpu::Error& e) {                               \
+        scope_.fail();                                            \
         return e.status;                                          \
     }                                                             \
     catch (...) {                                                 \
+        scope_.fail();                                            \
         prgpu::set_last_error("unexpected host exception");       \
         return PRGPU_ERR_CUDA;                                    \
     }
@@ -187,7 +216,7 @@ static int set_points_common(Ctx* c, const float* xyz, const float* nrm, int64_t
         set_last_error("%lld points exceed the supported count", (long long)n);
         return PRGPU_ERR_LIMIT;
     }
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     dfree(c->in_xyz, s);
@@ -220,7 +249,7 @@ int prgpu_set_points_device(void* h, const float* xyz, const float* nrm, int64_t
 int prgpu_build_octree(void* h) {
     Ctx* c = as_ctx(h);
     REQUIRE_STAGE(c, 1);
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     timed(*c, c->t.octree_ms, [&] { stage_octree(*c); });
     c->stage = 2;
@@ -231,7 +260,7 @@ int prgpu_build_octree(void* h) {
 int prgpu_compute_rhs(void* h) {
     Ctx* c = as_ctx(h);
     REQUIRE_STAGE(c, 2);
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     timed(*c, c->t.basis_ms, [&] { stage_basis(*c); });
     timed(*c, c->t.splat_ms, [&] { stage_splat(*c); });
@@ -244,7 +273,7 @@ int prgpu_compute_rhs(void* h) {
 int prgpu_solve(void* h) {
     Ctx* c = as_ctx(h);
     REQUIRE_STAGE(c, 3);
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     timed(*c, c->t.solve_ms, [&] { stage_solve(*c); });
     c->stage = 4;
@@ -262,7 +291,7 @@ int prgpu_solve_depth(void* h, int32_t depth, int32_t mode) {
         set_last_error("prgpu_solve_depth: depth %d (maxDepth %d), mode %d", depth, c->D, mode);
         return PRGPU_ERR_ARG;
     }
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     timed(*c, c->t.solve_ms, [&] { stage_solve_depths(*c, depth, depth, mode); });
     c->stage = std::max(c->stage, 4);
@@ -273,7 +302,7 @@ int prgpu_solve_depth(void* h, int32_t depth, int32_t mode) {
 int prgpu_eval_points(void* h, float* iso_out) {
     Ctx* c = as_ctx(h);
     REQUIRE_STAGE(c, 4);
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     timed(*c, c->t.iso_ms, [&] { stage_points(*c); });
     if (iso_out) *iso_out = c->iso;
@@ -285,7 +314,7 @@ int prgpu_eval_points(void* h, float* iso_out) {
 int prgpu_extract_mesh(void* h) {
     Ctx* c = as_ctx(h);
     REQUIRE_STAGE(c, 5);
-    API_BEGIN
+    API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
     timed(*c, c->t.mesh_ms, [&] { stage_mesh(*c); });
     c->stage = 6;

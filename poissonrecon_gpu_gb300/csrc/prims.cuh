@@ -3,11 +3,22 @@
 // All work on the caller's stream; temporary memory comes from the stream's
 // memory pool (cudaMallocAsync).
 #pragma once
+#include <utility>
+#include <vector>
+
 #include "common.cuh"
 
 namespace prgpu {
 
 // ------------------------------- memory ------------------------------------
+// The device allocations an API call has made on this host thread and not yet
+// freed (null outside a call); when the call fails, it frees the ones its stages
+// left behind.
+struct LiveAllocs {
+    std::vector<std::pair<void*, cudaStream_t>> v;
+};
+extern thread_local LiveAllocs* g_live;
+
 template <class T>
 inline T* dalloc(i64 n, cudaStream_t s) {
     void* p = nullptr;
@@ -18,11 +29,20 @@ inline T* dalloc(i64 n, cudaStream_t s) {
                        cudaGetErrorString(e));
         throw Error{PRGPU_ERR_NOMEM, {0}};
     }
+    if (g_live) g_live->v.emplace_back(p, s);
     return (T*)p;
 }
 template <class T>
 inline void dfree(T*& p, cudaStream_t s) {
-    if (p) cudaFreeAsync((void*)p, s);
+    if (p) {
+        if (g_live)
+            for (size_t k = g_live->v.size(); k-- > 0;)
+                if (g_live->v[k].first == (void*)p) {
+                    g_live->v.erase(g_live->v.begin() + (long)k);
+                    break;
+                }
+        cudaFreeAsync((void*)p, s);
+    }
     p = nullptr;
 }
 
