@@ -124,6 +124,8 @@ struct CallScope {
         if (c) {
             c->free_all();
             c->stage = 0;
+            c->kpending.clear();   // timers of the failed stage may lack their end event
+            c->kev_next = 0;
         }
         for (auto& a : live.v) cudaFreeAsync(a.first, a.second);
         live.v.clear();
@@ -169,8 +171,8 @@ int prgpu_create(const prgpu_params* p, void** out) {
         set_last_error("depth %d outside the supported range 2..15", p->depth);
         return PRGPU_ERR_LIMIT;
     }
-    API_BEGIN
     Ctx* c = new Ctx();
+    API_BEGIN
     c->params = *p;
     c->D = p->depth;
     c->device = p->device;
@@ -186,7 +188,21 @@ int prgpu_create(const prgpu_params* p, void** out) {
     CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     *out = c;
     return PRGPU_OK;
-    API_END
+    }
+    catch (...) {   // nothing is handed out: release what was created
+        if (c->ev1) cudaEventDestroy(c->ev1);
+        if (c->ev0) cudaEventDestroy(c->ev0);
+        if (c->stream) cudaStreamDestroy(c->stream);
+        delete c;
+        try {
+            throw;
+        } catch (const prgpu::Error& e) {
+            return e.status;
+        } catch (...) {
+            set_last_error("unexpected host exception");
+            return PRGPU_ERR_CUDA;
+        }
+    }
 }
 
 int prgpu_destroy(void* h) {
