@@ -56,7 +56,13 @@ typedef struct {
                                 and its share of the iso-value are weighted by the inverse of the
                                 sampling density around it, estimated at depth maxDepth-2 (Kazhdan's
                                 adaptive weighting of non-uniform samples; not in the reference) */
-    int32_t reserved[6];
+    int32_t cascadic;     /* 0: every depth solves L_d x_d = b_d on its own, as the reference
+                             (main.cu:1237-1329); 1: the depths are solved coarse to fine and depth
+                             d's right-hand side first loses the coarser depths' solution,
+                             b_d - sum_{d'<d} L_{d,d'} x_{d'}, with the exact cross-depth
+                             inner products over the 27 neighbours of each ancestor (Kazhdan's
+                             coarse-to-fine formulation; not in the reference) */
+    int32_t reserved[5];
 } prgpu_params;
 
 typedef struct {
@@ -94,7 +100,9 @@ int prgpu_solve(void* ctx);
 
 /* One depth's system L_d x_d = b_d (0 <= depth <= maxDepth) with the given
  * prgpu_solve_mode; the other depths' rows of x keep their values (0 before any
- * solve).  The body of LaplacianIteration's per-depth loop (main.cu:1237-1329). */
+ * solve).  The body of LaplacianIteration's per-depth loop (main.cu:1237-1329).
+ * With params.cascadic the right-hand side is b_d less the coarser depths'
+ * current rows of x (as prgpu_solve uses it). */
 int prgpu_solve_depth(void* ctx, int32_t depth, int32_t mode);
 
 /* Implicit function at the input points and the iso-value.

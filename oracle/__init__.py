@@ -54,6 +54,7 @@ def lib():
             getattr(L, name).argtypes = [vp]
         L.orc_build_basis.argtypes = [vp, c_int]
         L.orc_set_root_stride.argtypes = [vp, c_int]
+        L.orc_set_cascadic.argtypes = [vp, c_int]
         L.orc_solve.argtypes = [vp, c_int, dbl, c_int]
         L.orc_reconstruct.argtypes = [vp, c_int, dbl, c_int]
         L.orc_get.restype = vp
@@ -105,6 +106,10 @@ class Oracle:
 
     def marching_cubes(self):
         lib().orc_marching_cubes(self._h)
+
+    def set_cascadic(self, on: bool = True):
+        """Coarse-to-fine solve: each depth's right-hand side less the coarser solution."""
+        lib().orc_set_cascadic(self._h, int(on))
 
     def set_root_stride(self, stride: int):
         """Timing samples only: subdivide every stride-th root (0: none)."""

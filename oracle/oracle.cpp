@@ -330,6 +330,7 @@ struct Ctx {
     std::vector<int> cg_iters;              // D+1
     std::vector<float> cg_rr;               // D+1 final r.r
     std::vector<float> stencil;             // 27*(D+1)
+    int cascadic = 0;                       // coarse-to-fine solve (not the reference's)
     // iso
     std::vector<float> point_value;
     float iso = 0;
@@ -696,12 +697,50 @@ static void divergence(Ctx& c) {
 }
 
 // ---------------------------------------------------------------------------
+// Cascadic option (not the reference's, whose depths are independent systems):
+// depth d's right-hand side loses the coarser depths' solution,
+//   b'_i = b_i - sum_{d' < d} sum_{j in N27(ancestor_d'(i))} <grad B_i, grad B_j> x_j,
+// over the 27 neighbours of i's ancestor at each coarser depth (the truncation
+// the reference's divergence uses).  <grad B_i, grad B_j> is the product of the
+// 1-D tables, dd_x t_y t_z + t_x dd_y t_z + t_x t_y dd_z with t = dot and
+// dd = d2dot (the form of the same-depth stencil), in double, summed in double
+// in the order d' = 0.., j = 0..26.
+// ---------------------------------------------------------------------------
+static float cascade_rhs(const Ctx& c, i64 i, int d) {
+    const size_t res = (size_t)c.res;
+    int fi[3];
+    function_index(c, i, fi);
+    i64 anc[32];
+    i64 a = i;
+    for (int e = d; e > 0; --e) { a = c.parent[a]; anc[e - 1] = a; }
+    double acc = 0;
+    for (int e = 0; e < d; ++e) {
+        for (int j = 0; j < 27; ++j) {
+            const int q = c.neighs[27 * anc[e] + j];
+            if (q == -1) continue;
+            int fq[3];
+            function_index(c, q, fq);
+            double t[3], dd[3];
+            for (int k = 0; k < 3; ++k) {
+                const size_t idx = (size_t)fi[k] + res * (size_t)fq[k];
+                t[k] = c.dot[idx];
+                dd[k] = c.d2dot[idx];
+            }
+            const double l = dd[0] * t[1] * t[2] + t[0] * dd[1] * t[2] + t[0] * t[1] * dd[2];
+            acc += l * (double)c.x[q];
+        }
+    }
+    return (float)((double)c.divergence[i] - acc);
+}
+
+// ---------------------------------------------------------------------------
 // a12-a13: per-depth Laplacian and CG  (main.cu:1143-1332, CG_CUDA.cuh:186-509)
 // mode 0: reference schedule (x0=0, stop when float(r.r) <= 1e-5f*1e-5f or after
 //         max_iter iterations).  mode 1: relative residual ||r|| <= tol*||b||.
 // ---------------------------------------------------------------------------
-static void solve(Ctx& c, int mode, double tol, int max_iter) {
+static int solve(Ctx& c, int mode, double tol, int max_iter) {
     const int D = c.D;
+    if (c.cascadic && c.dot.empty()) return -1;   // the cross-depth products need the full tables
     c.x.assign(c.M, 0.f);
     c.cg_iters.assign(D + 1, 0);
     c.cg_rr.assign(D + 1, 0.f);
@@ -710,6 +749,13 @@ static void solve(Ctx& c, int mode, double tol, int max_iter) {
         const float* st = &c.stencil[27 * d];
         std::vector<float> r(n), p(n), Ax(n), xx(n, 0.f);
         const float* b = &c.divergence[lo];
+        std::vector<float> rhs;
+        if (c.cascadic) {
+            rhs.resize(n);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(static)
+            for (i64 i = 0; i < n; ++i) rhs[i] = cascade_rhs(c, lo + i, d);
+            b = rhs.data();
+        }
         auto spmv = [&](const std::vector<float>& in, std::vector<float>& out) {
 #pragma omp parallel for num_threads(omp_threads(c)) schedule(static)
             for (i64 i = 0; i < n; ++i) {
@@ -759,6 +805,7 @@ static void solve(Ctx& c, int mode, double tol, int max_iter) {
         c.cg_rr[d] = r1;
         for (i64 i = 0; i < n; ++i) c.x[lo + i] = xx[i];
     }
+    return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1399,7 +1446,8 @@ int orc_build_octree(void* h) { build_octree(*(Ctx*)h); return 0; }
 int orc_build_basis(void* h, int full_tables) { build_basis(*(Ctx*)h, full_tables != 0); return 0; }
 int orc_vector_field(void* h) { vector_field(*(Ctx*)h); return 0; }
 int orc_divergence(void* h) { divergence(*(Ctx*)h); return 0; }
-int orc_solve(void* h, int mode, double tol, int max_iter) { solve(*(Ctx*)h, mode, tol, max_iter); return 0; }
+int orc_solve(void* h, int mode, double tol, int max_iter) { return solve(*(Ctx*)h, mode, tol, max_iter); }
+int orc_set_cascadic(void* h, int on) { ((Ctx*)h)->cascadic = on != 0; return 0; }
 int orc_point_values(void* h) { point_values(*(Ctx*)h); return 0; }
 int orc_marching_cubes(void* h) { marching_cubes(*(Ctx*)h); return 0; }
 // timing samples: subdivide every stride-th root only (0: none); the default 1 is the full path
@@ -1412,7 +1460,7 @@ int orc_reconstruct(void* h, int mode, double tol, int max_iter) {
     build_basis(*c, true);
     vector_field(*c);
     divergence(*c);
-    solve(*c, mode, tol, max_iter);
+    if (solve(*c, mode, tol, max_iter)) return -1;
     point_values(*c);
     marching_cubes(*c);
     return 0;

@@ -53,7 +53,8 @@ class PrgpuError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("depth", ctypes.c_int32), ("solve_mode", ctypes.c_int32), ("cg_tol", ctypes.c_double),
                 ("cg_max_iter", ctypes.c_int32), ("device", ctypes.c_int32), ("weld", ctypes.c_int32),
-                ("density_weights", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("density_weights", ctypes.c_int32), ("cascadic", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 class Mesh(ctypes.Structure):
@@ -134,13 +135,15 @@ class Reconstructor:
     """One reconstruction context on one GPU (its own CUDA stream)."""
 
     def __init__(self, depth: int = 8, solve_mode: int = SOLVE_REFERENCE, cg_tol: float = 1e-5,
-                 cg_max_iter: int = 10000, device: int = 0, weld: bool = False, density_weights: bool = False):
+                 cg_max_iter: int = 10000, device: int = 0, weld: bool = False, density_weights: bool = False,
+                 cascadic: bool = False):
         L = _lib()
         p = Params()
         L.prgpu_params_default(ctypes.byref(p))
         p.depth, p.solve_mode, p.cg_tol, p.cg_max_iter, p.device = depth, solve_mode, cg_tol, cg_max_iter, device
         p.weld = 1 if weld else 0
         p.density_weights = 1 if density_weights else 0
+        p.cascadic = 1 if cascadic else 0
         self.params = p
         self._h = _VP()
         _check(L.prgpu_create(ctypes.byref(p), ctypes.byref(self._h)), "prgpu_create")

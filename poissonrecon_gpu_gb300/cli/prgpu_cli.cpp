@@ -1,6 +1,6 @@
 // prgpu: command-line front end of the library.
 //   prgpu --in points.ply --out mesh.ply [--depth 8] [--binary] [--relative TOL]
-//         [--maxIter N] [--device K] [--weld] [--density] [--stats]
+//         [--maxIter N] [--device K] [--weld] [--density] [--cascadic] [--stats]
 // The reference takes its input/output paths and maxDepth at compile time
 // (main.cu:69,3251-3252); the flag names follow the Kazhdan-style "--name value"
 // convention of its CmdLineParser (CmdLineParser.cu:205-240).
@@ -15,7 +15,7 @@
 static void usage() {
     fprintf(stderr,
             "usage: prgpu --in <points.ply|.bnpts|ascii> --out <mesh.ply> [--depth D] [--binary]\n"
-            "             [--relative TOL] [--maxIter N] [--device K] [--weld] [--density] [--stats]\n");
+            "             [--relative TOL] [--maxIter N] [--device K] [--weld] [--density] [--cascadic] [--stats]\n");
 }
 
 int main(int argc, char** argv) {
@@ -36,6 +36,7 @@ int main(int argc, char** argv) {
         else if (a == "--binary") binary = 1;
         else if (a == "--weld") p.weld = 1;
         else if (a == "--density") p.density_weights = 1;
+        else if (a == "--cascadic") p.cascadic = 1;
         else if (a == "--relative") { p.solve_mode = PRGPU_SOLVE_RELATIVE; p.cg_tol = atof(next()); }
         else if (a == "--maxIter") p.cg_max_iter = atoi(next());
         else if (a == "--device") p.device = atoi(next());

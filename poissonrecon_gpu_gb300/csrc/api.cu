@@ -36,6 +36,8 @@ void Ctx::free_all() {
     free_nodes();
     dfree(in_xyz, s); dfree(in_nrm, s); dfree(pts, s); dfree(nrm, s); dfree(sort_idx, s);
     dfree(point_node, s); dfree(basis, s); dfree(ddot_div, s); dfree(full_tables, s);
+    dfree(cascade_tab, s);
+    cascade_off.clear();
     dfree(vfield, s); dfree(divergence, s); dfree(x, s); dfree(point_value, s);
     dfree(point_weight, s); dfree(wnrm, s);
     dfree(d_cg_iters, s); dfree(d_cg_rr, s);
@@ -309,7 +311,22 @@ int prgpu_solve_depth(void* h, int32_t depth, int32_t mode) {
     }
     API_BEGIN_CTX(c)
     CK(cudaSetDevice(c->device));
-    timed(*c, c->t.solve_ms, [&] { stage_solve_depths(*c, depth, depth, mode); });
+    timed(*c, c->t.solve_ms, [&] {
+        if (!c->params.cascadic) {
+            stage_solve_depths(*c, depth, depth, mode);
+            return;
+        }
+        if (!c->x || c->x_rows != c->nodes.M) {   // no solve yet: the coarser rows are 0
+            dfree(c->x, c->stream);
+            c->x = dalloc<float>(c->nodes.M, c->stream);
+            c->x_rows = c->nodes.M;
+            CK(cudaMemsetAsync(c->x, 0, c->nodes.M * sizeof(float), c->stream));
+        }
+        float* rhs = dalloc<float>(c->nodes.M, c->stream);
+        cascade_rhs(*c, depth, rhs);
+        stage_solve_depths(*c, depth, depth, mode, rhs);
+        dfree(rhs, c->stream);
+    });
     c->stage = std::max(c->stage, 4);
     return c->cg_iters[depth] >= c->params.cg_max_iter ? PRGPU_ERR_NOT_CONVERGED : PRGPU_OK;
     API_END

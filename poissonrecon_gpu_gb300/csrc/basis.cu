@@ -222,11 +222,78 @@ __global__ void k_full_tables(BasePack bp, int res, double t1, double t2, double
     }
 }
 
+// Cross-depth 1-D inner products for the cascadic solve.  For a node at depth d
+// and a neighbour of its ancestor at depth e < d (k = d - e levels up), the 1-D
+// pair (dot, d2dot) depends only on the node's position a in [0, 2^k) within the
+// ancestor along the axis and the neighbour's offset o - 1, o in {0, 1, 2}: the
+// centres enter inner_products only through (c2 - c1) / w1 and w2 / w1, which are
+// exact in double.  The entry is the full table's value for (finer, coarser)
+// (the same overlap test and |dot| < 1e-15 drop as k_full_tables), at
+// off[d * (D + 1) + e] + o * 2^k + a.
+__global__ void k_cascade_tables(BasePack bp, int D, double t1, double t2, const i64* __restrict__ off, i64 n,
+                                 double2* __restrict__ tab) {
+    for (i64 g = (i64)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (i64)gridDim.x * blockDim.x) {
+        // locate the (d, e) table holding g
+        int d = 1, e = 0;
+        for (int dd = 1; dd <= D; ++dd)
+            for (int ee = 0; ee < dd; ++ee)
+                if (off[dd * (D + 1) + ee] <= g) { d = dd; e = ee; }
+        const int k = d - e;
+        const i64 r = g - off[d * (D + 1) + e];
+        const int o = (int)(r >> k);
+        const i64 a = r - ((i64)o << k);
+        const double w1 = 1.0 / (double)(1ll << d), w2 = 1.0 / (double)(1ll << e);
+        // ancestor at position 1, node at 2^k + a below it, neighbour at 1 + o - 1
+        const double c1 = ((double)((1ll << k) + a) + 0.5) * w1;
+        const double c2 = ((double)o + 0.5) * w2;
+        double2 v = make_double2(0.0, 0.0);
+        if (supports_overlap(t1, t2, c1, w1, c2, w2)) {
+            InnerProducts ip = inner_products(bp.B, bp.dB, c1, w1, c2, w2, true);
+            if (!(fabs(ip.dot) < 1e-15)) v = make_double2(ip.dot, ip.d2dot);
+        }
+        tab[g] = v;
+    }
+}
+
+void ensure_cascade_tables(Ctx& c) {
+    const int D = c.D;
+    if (c.cascade_tab && (int)c.cascade_off.size() == (D + 1) * (D + 1) + 1) return;
+    ensure_base_function();
+    cudaStream_t s = c.stream;
+    c.cascade_off.assign((size_t)(D + 1) * (D + 1) + 1, 0);
+    i64 n = 0;
+    for (int d = 0; d <= D; ++d)
+        for (int e = 0; e <= D; ++e) {
+            c.cascade_off[(size_t)d * (D + 1) + e] = n;
+            if (e < d) n += 3ll << (d - e);
+        }
+    c.cascade_off[(size_t)(D + 1) * (D + 1)] = n;
+    dfree(c.cascade_tab, s);
+    c.cascade_tab = dalloc<double2>(std::max<i64>(n, 1), s);
+    i64* doff = dalloc<i64>((i64)c.cascade_off.size(), s);
+    CK(cudaMemcpyAsync(doff, c.cascade_off.data(), c.cascade_off.size() * sizeof(i64), cudaMemcpyHostToDevice, s));
+    BasePack bp;
+    bp.B = g_B;
+    bp.dB = g_dB;
+    const double t1 = g_B.p[0].start, t2 = g_B.p[g_B.n - 1].start;
+    if (n > 0) {
+        k_cascade_tables<<<grid_for(n, 128, 152 * 16), 128, 0, s>>>(bp, D, t1, t2, doff, n, c.cascade_tab);
+        CK_LAUNCH();
+    }
+    dfree(doff, s);
+}
+
 void stage_basis(Ctx& c) {
     ensure_base_function();
     cudaStream_t s = c.stream;
     const int D = c.D;
     c.res = (1 << (D + 1)) - 1;
+    // tables of another maxDepth (a batch may change it) are rebuilt on demand
+    dfree(c.full_tables, s);
+    if ((int)c.cascade_off.size() != (D + 1) * (D + 1) + 1) {
+        dfree(c.cascade_tab, s);
+        c.cascade_off.clear();
+    }
     BasePack bp;
     bp.B = g_B;
     bp.dB = g_dB;

@@ -101,6 +101,8 @@ struct Ctx {
     std::vector<i64> ddot_row_start; // per depth
     std::vector<float> stencil;      // 27 per depth
     double* full_tables = nullptr;   // dot, ddot, d2dot (res*res each), on demand
+    double2* cascade_tab = nullptr;  // cross-depth 1-D (dot, d2dot) for params.cascadic
+    std::vector<i64> cascade_off;    // (D+1)^2: start of the (depth, coarser depth) table
 
     // rhs / solve
     float* vfield = nullptr;         // 3 x count[D]
@@ -154,10 +156,12 @@ struct Ctx {
 void stage_octree(Ctx& c);
 void stage_basis(Ctx& c);
 void stage_full_tables(Ctx& c);
+void ensure_cascade_tables(Ctx& c);
 void stage_splat(Ctx& c);
 void stage_divergence(Ctx& c);
 void stage_solve(Ctx& c);
-void stage_solve_depths(Ctx& c, int d0, int d1, int mode);
+void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs = nullptr);
+void cascade_rhs(Ctx& c, int d, float* rhs);   // depth d's rows of an M-row device buffer
 void ensure_group_table(Ctx& c);
 void stage_points(Ctx& c);
 void stage_mesh(Ctx& c);

@@ -392,11 +392,139 @@ void ensure_group_table(Ctx& c) {
     }
 }
 
-void stage_solve_depths(Ctx& c, int d0, int d1, int mode);
-void stage_solve(Ctx& c) { stage_solve_depths(c, 0, c.D, c.params.solve_mode); }
+// ---------------------------------------------------------------------------
+// Cascadic solve (params.cascadic; not the reference's): the depths are solved
+// coarse to fine and depth d's right-hand side first loses the coarser depths'
+// solution,
+//   b'_i = b_i - sum_{e < d} sum_{j in N27(ancestor_e(i))} <grad B_i, grad B_j> x_j,
+// the coarser nodes being the 27 neighbours of i's ancestor at each depth e (the
+// truncation the reference's divergence uses).  The 3-D inner product is the
+// same-depth stencil's form, dd_x t_y t_z + t_x dd_y t_z + t_x t_y dd_z, over
+// the cross-depth 1-D tables (k_cascade_tables); products and sums in double,
+// in the order e = 0.., j = 0..26.  One thread per node of depth d.
+// ---------------------------------------------------------------------------
+constexpr int CASCADE_MAX_DEPTH = 16;
 
-// depths d0..d1 with the given mode; the other depths' rows of x are left as they are
-void stage_solve_depths(Ctx& c, int d0, int d1, int mode) {
+struct CascadeArgs {
+    int d, D;
+    i64 lo, n, M;
+    const u64* key;
+    const int* parent;
+    const int* neigh;       // 27 x M
+    const double2* tab;
+    i64 off[CASCADE_MAX_DEPTH];   // start of the (d, e) table, e < d
+    const float* x;
+    const float* b;
+    float* rhs;
+};
+
+__global__ void __launch_bounds__(128) k_cascade_rhs(CascadeArgs a) {
+    const int d = a.d, sh0 = 3 * (a.D - d);
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < a.n; t += (i64)gridDim.x * blockDim.x) {
+        const i64 i = a.lo + t;
+        const u64 key = a.key[i] >> sh0;
+        int p[3] = {0, 0, 0};
+        for (int l = d - 1; l >= 0; --l) {
+            p[0] = (p[0] << 1) | (int)((key >> (3 * l + 2)) & 1);
+            p[1] = (p[1] << 1) | (int)((key >> (3 * l + 1)) & 1);
+            p[2] = (p[2] << 1) | (int)((key >> (3 * l)) & 1);
+        }
+        int anc[CASCADE_MAX_DEPTH];
+        int q = (int)i;
+        for (int e = d - 1; e >= 0; --e) {
+            q = a.parent[q];
+            anc[e] = q;
+        }
+        double acc = 0.0;
+        for (int e = 0; e < d; ++e) {
+            const int k = d - e;
+            const int mask = (1 << k) - 1;
+            const double2* T = a.tab + a.off[e];
+            double tv[3][3], dv[3][3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+                for (int o = 0; o < 3; ++o) {
+                    const double2 v = T[((i64)o << k) + (p[ax] & mask)];
+                    tv[ax][o] = v.x;
+                    dv[ax][o] = v.y;
+                }
+            const int A = anc[e];
+#pragma unroll
+            for (int j = 0; j < 27; ++j) {
+                const int nb = a.neigh[(i64)j * a.M + A];
+                if (nb < 0) continue;
+                const int ox = j / 9, oy = (j / 3) % 3, oz = j % 3;
+                const double l = dv[0][ox] * tv[1][oy] * tv[2][oz] + tv[0][ox] * dv[1][oy] * tv[2][oz] +
+                                 tv[0][ox] * tv[1][oy] * dv[2][oz];
+                acc += l * (double)a.x[nb];
+            }
+        }
+        a.rhs[i] = (float)((double)a.b[i] - acc);
+    }
+}
+
+// depth d's rows of rhs: the divergence less the coarser depths' current solution
+void cascade_rhs(Ctx& c, int d, float* rhs) {
+    cudaStream_t s = c.stream;
+    const i64 lo = c.base[d], n = c.count[d];
+    if (n == 0) return;
+    if (d == 0) {
+        CK(cudaMemcpyAsync(rhs + lo, c.divergence + lo, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        return;
+    }
+    if (c.D >= CASCADE_MAX_DEPTH) {
+        set_last_error("cascadic solve supports maxDepth < %d", CASCADE_MAX_DEPTH);
+        throw Error{PRGPU_ERR_LIMIT, {0}};
+    }
+    ensure_cascade_tables(c);
+    CascadeArgs a;
+    a.d = d;
+    a.D = c.D;
+    a.lo = lo;
+    a.n = n;
+    a.M = c.nodes.M;
+    a.key = c.nodes.key;
+    a.parent = c.nodes.parent;
+    a.neigh = c.nodes.neigh;
+    a.tab = c.cascade_tab;
+    for (int e = 0; e < CASCADE_MAX_DEPTH; ++e) a.off[e] = e < d ? c.cascade_off[(size_t)d * (c.D + 1) + e] : 0;
+    a.x = c.x;
+    a.b = c.divergence;
+    a.rhs = rhs;
+    // compulsory: key, parent, b and rhs of each node; the coarser depths' neighbour rows and x
+    double bytes = (double)n * 20;
+    for (int e = 0; e < d; ++e) bytes += (double)c.count[e] * (27 * 4 + 4);
+    const int kt = c.kbegin("cascade_rhs", bytes);
+    k_cascade_rhs<<<grid_for(n, 128), 128, 0, s>>>(a);
+    CK_LAUNCH();
+    c.kend(kt);
+}
+
+void stage_solve(Ctx& c) {
+    if (!c.params.cascadic) {
+        stage_solve_depths(c, 0, c.D, c.params.solve_mode);
+        return;
+    }
+    cudaStream_t s = c.stream;
+    const i64 M = c.nodes.M;
+    if (!c.x || c.x_rows != M) {
+        dfree(c.x, s);
+        c.x = dalloc<float>(M, s);
+        c.x_rows = M;
+        CK(cudaMemsetAsync(c.x, 0, M * sizeof(float), s));
+    }
+    float* rhs = dalloc<float>(M, s);
+    for (int d = 0; d <= c.D; ++d) {
+        cascade_rhs(c, d, rhs);
+        stage_solve_depths(c, d, d, c.params.solve_mode, rhs);
+    }
+    dfree(rhs, s);
+}
+
+// depths d0..d1 with the given mode (right-hand side: rhs, or the divergence);
+// the other depths' rows of x are left as they are
+void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     cudaStream_t s = c.stream;
     const int D = c.D;
     const i64 M = c.nodes.M;
@@ -493,7 +621,7 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode) {
     a.neigh = c.nodes.neigh;
     a.gn = gn;
     a.ngroups = ngroups;
-    a.b = c.divergence;
+    a.b = rhs ? rhs : c.divergence;
     a.x = c.x;
     a.r = r;
     a.p = p;
