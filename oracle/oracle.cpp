@@ -703,9 +703,19 @@ static void divergence(Ctx& c) {
 // over the 27 neighbours of i's ancestor at each coarser depth (the truncation
 // the reference's divergence uses).  <grad B_i, grad B_j> is the product of the
 // 1-D tables, dd_x t_y t_z + t_x dd_y t_z + t_x t_y dd_z with t = dot and
-// dd = d2dot (the form of the same-depth stencil), in double, summed in double
-// in the order d' = 0.., j = 0..26.
+// dd = d2dot (the form of the same-depth stencil), so the 3x3x3 sum factors axis
+// by axis.  In double with explicit fma, in the library's order (solve.cu,
+// k_cascade_rhs): per ancestor d' = 0.., for ox: for oy:
+//   zt[oy] = fma(t_z0, X0, fma(t_z1, X1, t_z2 * X2)), zd[oy] likewise with dd_z,
+// then ytt, ydt, ytd (the same nesting over oy) and
+//   acc = fma(dd_x[ox], ytt, fma(t_x[ox], ydt + ytd, acc)).
+// The table entries for one axis depend on the node's and the neighbour's
+// function indices only; a missing neighbour contributes X = 0.
 // ---------------------------------------------------------------------------
+static inline double dot3(double a0, double a1, double a2, double x0, double x1, double x2) {
+    return std::fma(a0, x0, std::fma(a1, x1, a2 * x2));
+}
+
 static float cascade_rhs(const Ctx& c, i64 i, int d) {
     const size_t res = (size_t)c.res;
     int fi[3];
@@ -715,19 +725,36 @@ static float cascade_rhs(const Ctx& c, i64 i, int d) {
     for (int e = d; e > 0; --e) { a = c.parent[a]; anc[e - 1] = a; }
     double acc = 0;
     for (int e = 0; e < d; ++e) {
-        for (int j = 0; j < 27; ++j) {
-            const int q = c.neighs[27 * anc[e] + j];
-            if (q == -1) continue;
-            int fq[3];
-            function_index(c, q, fq);
-            double t[3], dd[3];
-            for (int k = 0; k < 3; ++k) {
-                const size_t idx = (size_t)fi[k] + res * (size_t)fq[k];
-                t[k] = c.dot[idx];
-                dd[k] = c.d2dot[idx];
+        // the ancestor's function index per axis; its neighbour at offset o - 1 has index + o - 1
+        int fa[3];
+        function_index(c, anc[e], fa);
+        double t[3][3], dd[3][3];
+        for (int k = 0; k < 3; ++k)
+            for (int o = 0; o < 3; ++o) {
+                const long fq = (long)fa[k] + o - 1;
+                const long lo = (1l << e) - 1, hi = (2l << e) - 1;   // depth e's function indices
+                t[k][o] = dd[k][o] = 0.0;
+                if (fq >= lo && fq < hi) {
+                    const size_t idx = (size_t)fi[k] + res * (size_t)fq;
+                    t[k][o] = c.dot[idx];
+                    dd[k][o] = c.d2dot[idx];
+                }
             }
-            const double l = dd[0] * t[1] * t[2] + t[0] * dd[1] * t[2] + t[0] * t[1] * dd[2];
-            acc += l * (double)c.x[q];
+        for (int ox = 0; ox < 3; ++ox) {
+            double zt[3], zd[3];
+            for (int oy = 0; oy < 3; ++oy) {
+                double X[3];
+                for (int oz = 0; oz < 3; ++oz) {
+                    const int q = c.neighs[27 * anc[e] + 9 * ox + 3 * oy + oz];
+                    X[oz] = q != -1 ? (double)c.x[q] : 0.0;
+                }
+                zt[oy] = dot3(t[2][0], t[2][1], t[2][2], X[0], X[1], X[2]);
+                zd[oy] = dot3(dd[2][0], dd[2][1], dd[2][2], X[0], X[1], X[2]);
+            }
+            const double ytt = dot3(t[1][0], t[1][1], t[1][2], zt[0], zt[1], zt[2]);
+            const double ydt = dot3(dd[1][0], dd[1][1], dd[1][2], zt[0], zt[1], zt[2]);
+            const double ytd = dot3(t[1][0], t[1][1], t[1][2], zd[0], zd[1], zd[2]);
+            acc = std::fma(dd[0][ox], ytt, std::fma(t[0][ox], ydt + ytd, acc));
         }
     }
     return (float)((double)c.divergence[i] - acc);
