@@ -24,6 +24,24 @@ def test_header_compiles_as_c(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_python_params_layout_matches_header(tmp_path):
+    """The ctypes mirror of prgpu_params has the C struct's size and field offsets."""
+    import ctypes
+    from poissonrecon_gpu_gb300 import Params
+    fields = [f[0] for f in Params._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "prgpu.h"\n'
+                   'int main(void) {\n    printf("%zu\\n", sizeof(prgpu_params));\n' +
+                   "".join('    printf("%%zu\\n", offsetof(prgpu_params, %s));\n' % f for f in fields) +
+                   '    return 0;\n}\n')
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", INC, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(Params)
+    assert got[1:] == [getattr(Params, f).offset for f in fields]
+
+
 def _build_client(lib_built, out):
     r = subprocess.run(["g++", "-O1", "-std=c++17", "-Wall", "-I", INC, CLIENT, "-o", str(out), "-L", PKG, "-lprgpu",
                         "-Wl,-rpath," + PKG], capture_output=True, text=True)

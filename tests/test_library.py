@@ -100,6 +100,10 @@ def test_cli_usage(lib_built):
     exe = os.path.join(REPO, "poissonrecon_gpu_gb300", "prgpu")
     r = subprocess.run([exe], capture_output=True)
     assert r.returncode == 2 and b"usage" in r.stderr
+    for flag in (b"--weld", b"--density", b"--cascadic", b"--relative", b"--binary"):
+        assert flag in r.stderr
+    r = subprocess.run([exe, "--no-such-flag"], capture_output=True)
+    assert r.returncode == 2 and b"usage" in r.stderr
 
 
 def _ply_header(fmt, n, props, pre=b""):
