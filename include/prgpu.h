@@ -186,6 +186,27 @@ int64_t prgpu_kernel_launches(void);
 /* Human-readable text of the last error on this thread. */
 const char* prgpu_last_error(void);
 
+/* Failure-path hooks for tests.  The reference has no counterpart: its failures
+ * end the process (exit() in PointStream.inl:33, CG_CUDA.cuh:359-373).  The
+ * hooks are process-wide and off by default.  'what':
+ *   PRGPU_HOOK_CLEAR          all hooks off;
+ *   PRGPU_HOOK_FAIL_ALLOC     the arg-th device allocation from now on fails (once) as if
+ *                             the device were out of memory (arg >= 1);
+ *   PRGPU_HOOK_BARRIER_WAIT   the solvers' grid barriers expect one block more than the
+ *                             launch has -- an arrival that never comes -- and give up
+ *                             after arg polls of about 32 ns, so a solve returns
+ *                             PRGPU_ERR_TIMEOUT without hanging (arg >= 1);
+ *   PRGPU_HOOK_POOL_USED      *out = bytes the current device's memory pool has handed out
+ *                             and not taken back (after a device synchronisation).
+ * out may be NULL except for PRGPU_HOOK_POOL_USED. */
+enum {
+    PRGPU_HOOK_CLEAR = 0,
+    PRGPU_HOOK_FAIL_ALLOC = 1,
+    PRGPU_HOOK_BARRIER_WAIT = 2,
+    PRGPU_HOOK_POOL_USED = 3
+};
+int prgpu_test_hook(int32_t what, int64_t arg, int64_t* out);
+
 /* Conjugate gradients on a CSR matrix in device memory, x0 = 0, stopping when
  * float(r.r) <= tol^2 or after max_iter iterations; FP32 vectors, FP64 dots.
  * Replaces solverCG_DeviceToDevice(N, nz, I, J, val, rhs, x) (CG_CUDA.cuh:344-509).

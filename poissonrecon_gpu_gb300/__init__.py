@@ -95,6 +95,7 @@ SIGNATURES = {
     "prgpu_get_stream": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "prgpu_set_profiling": (ctypes.c_int, [_VP, _I32]),
     "prgpu_kernel_launches": (ctypes.c_int64, []),
+    "prgpu_test_hook": (ctypes.c_int, [_I32, _I64, ctypes.POINTER(_I64)]),
     "prgpu_cg_csr": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32,
                                     ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_float)]),
     "prgpu_cg_csr_noalloc": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32, _VP,
@@ -308,6 +309,17 @@ def solverCG_DeviceToDevice(N: int, nz: int, I: int, J: int, val: int, rhs: int,
 
 def kernel_launches() -> int:
     return int(_lib().prgpu_kernel_launches())
+
+
+HOOK_CLEAR, HOOK_FAIL_ALLOC, HOOK_BARRIER_WAIT, HOOK_POOL_USED = 0, 1, 2, 3
+
+
+def test_hook(what: int, arg: int = 0) -> int:
+    """Failure-path hooks (prgpu_test_hook): returns the hook's output value (pool bytes
+    for HOOK_POOL_USED, else 0)."""
+    out = _I64(0)
+    _check(_lib().prgpu_test_hook(what, arg, ctypes.byref(out)), "prgpu_test_hook")
+    return out.value
 
 
 def read_points(path: str):

@@ -15,6 +15,15 @@ namespace prgpu {
 
 static thread_local char g_err[512] = {0};
 std::atomic<unsigned long long> g_kernel_launches(0);
+std::atomic<long long> g_fail_alloc_countdown(0);
+static std::atomic<long long> g_spin_limit(DEFAULT_SPIN_LIMIT);
+static std::atomic<int> g_wait_extra(0);
+WaitLimits wait_limits() {
+    WaitLimits w;
+    w.spin_limit = g_spin_limit.load();
+    w.extra = g_wait_extra.load();
+    return w;
+}
 void set_last_error(const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -722,6 +731,42 @@ int prgpu_get_stream(void* h, void** stream) {
 }
 
 int64_t prgpu_kernel_launches(void) { return (int64_t)prgpu::g_kernel_launches.load(); }
+
+int prgpu_test_hook(int32_t what, int64_t arg, int64_t* out) {
+    switch (what) {
+    case PRGPU_HOOK_CLEAR:
+        g_fail_alloc_countdown = 0;
+        g_spin_limit = DEFAULT_SPIN_LIMIT;
+        g_wait_extra = 0;
+        return PRGPU_OK;
+    case PRGPU_HOOK_FAIL_ALLOC:
+        if (arg < 1) return PRGPU_ERR_ARG;
+        g_fail_alloc_countdown = arg;
+        return PRGPU_OK;
+    case PRGPU_HOOK_BARRIER_WAIT:
+        if (arg < 1) return PRGPU_ERR_ARG;
+        g_spin_limit = arg;
+        g_wait_extra = 1;
+        return PRGPU_OK;
+    case PRGPU_HOOK_POOL_USED: {
+        if (!out) return PRGPU_ERR_ARG;
+        API_BEGIN
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceSynchronize());
+        cudaMemPool_t pool;
+        CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+        uint64_t used = 0;
+        CK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+        *out = (int64_t)used;
+        return PRGPU_OK;
+        API_END
+    }
+    default:
+        set_last_error("prgpu_test_hook: unknown hook %d", what);
+        return PRGPU_ERR_ARG;
+    }
+}
 
 int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* rowptr, const int32_t* col, const float* val, const float* rhs,
                  float* x, float tol, int32_t max_iter, int32_t* iters, float* kernel_ms) {

@@ -38,6 +38,17 @@ const char* last_error();
     } while (0)
 // every kernel launch is followed by CK_LAUNCH(), which also counts it
 extern std::atomic<unsigned long long> g_kernel_launches;
+
+// Bounded waits of the persistent solver kernels: a barrier polls at most
+// spin_limit times (about 32-64 ns apart) and then records PRGPU_ERR_TIMEOUT.
+// PRGPU_HOOK_BARRIER_WAIT sets extra = 1 (an arrival that never comes) and a
+// small limit, so tests reach the timeout path without a real hang.
+constexpr long long DEFAULT_SPIN_LIMIT = 1ll << 24;   // about half a second
+struct WaitLimits {
+    long long spin_limit = DEFAULT_SPIN_LIMIT;
+    int extra = 0;
+};
+WaitLimits wait_limits();   // current settings (host)
 #define CK_LAUNCH()                            \
     do {                                       \
         ++::prgpu::g_kernel_launches;          \

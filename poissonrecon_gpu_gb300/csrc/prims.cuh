@@ -18,11 +18,18 @@ struct LiveAllocs {
     std::vector<std::pair<void*, cudaStream_t>> v;
 };
 extern thread_local LiveAllocs* g_live;
+// PRGPU_HOOK_FAIL_ALLOC: allocations left before the one that fails (0: off)
+extern std::atomic<long long> g_fail_alloc_countdown;
 
 template <class T>
 inline T* dalloc(i64 n, cudaStream_t s) {
     void* p = nullptr;
     if (n <= 0) n = 1;
+    if (g_fail_alloc_countdown.load(std::memory_order_relaxed) > 0 && --g_fail_alloc_countdown == 0) {
+        set_last_error("cudaMallocAsync(%lld bytes): failure injected by PRGPU_HOOK_FAIL_ALLOC",
+                       (long long)((size_t)n * sizeof(T)));
+        throw Error{PRGPU_ERR_NOMEM, {0}};
+    }
     cudaError_t e = cudaMallocAsync(&p, (size_t)n * sizeof(T), s);
     if (e != cudaSuccess) {
         set_last_error("cudaMallocAsync(%lld bytes): %s", (long long)((size_t)n * sizeof(T)),

@@ -31,7 +31,6 @@
 namespace prgpu {
 
 constexpr int CG_BLOCK = 256;
-constexpr long long SPIN_LIMIT = 1ll << 24;   // polls of ~32 ns: about half a second
 
 struct PartState {          // one per depth, in global memory, zero-initialised
     double acc[3];
@@ -92,6 +91,8 @@ struct CgArgs {
     PartSync* sync;         // one per depth
     double* partial;        // one per block
     int* err;
+    long long spin_limit;   // bounded waits (WaitLimits)
+    int extra;
 };
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -106,23 +107,23 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 }
 
 // barrier over the blocks of one partition; returns false after a timeout
-__device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok) {
+__device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok, long long spin_limit, int extra) {
     __syncthreads();
-    if (nblocks > 1) {
+    if (nblocks + extra > 1) {
         if (threadIdx.x == 0) {
             volatile unsigned* vgen = &ps->gen;
             unsigned g = *vgen;
             __threadfence();
             unsigned arrived = atomicAdd(&ps->count, 1u);
             int ok = 1;
-            if (arrived == (unsigned)nblocks - 1) {
+            if (arrived == (unsigned)(nblocks + extra) - 1) {
                 atomicExch(&ps->count, 0u);
                 __threadfence();
                 atomicAdd(&ps->gen, 1u);
             } else {
                 long long spins = 0;
                 while (*vgen == g) {
-                    if (++spins > SPIN_LIMIT || *(volatile int*)err) { ok = 0; break; }
+                    if (++spins > spin_limit || *(volatile int*)err) { ok = 0; break; }
                     __nanosleep(32);
                 }
             }
@@ -143,14 +144,15 @@ __device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok) {
 // result does not depend on arrival order) and releases the others.  Waits spin
 // with a limit; on expiry the error flag is set and false returned.
 __device__ double part_reduce(PartSync* ps, double* partial, int first_block, int nblocks, int slot, double v,
-                              int* err, double* sh, int* sh_flag, double* sh_val, bool& ok) {
+                              int* err, double* sh, int* sh_flag, double* sh_val, bool& ok, long long spin_limit,
+                              int extra) {
     const double s = block_sum(v, sh);
     if (threadIdx.x == 0) {
         partial[blockIdx.x] = s;
         __threadfence();
         const unsigned g = *(volatile unsigned*)&ps->gen;
         const unsigned arrived = atomicAdd(&ps->count, 1u);
-        sh_flag[0] = (arrived == (unsigned)nblocks - 1) ? 1 : 0;
+        sh_flag[0] = (arrived == (unsigned)(nblocks + extra) - 1) ? 1 : 0;
         sh_flag[1] = (int)g;
     }
     __syncthreads();
@@ -173,7 +175,7 @@ __device__ double part_reduce(PartSync* ps, double* partial, int first_block, in
         long long spins = 0;
         int good = 1;
         while (*vgen == g) {
-            if (++spins > SPIN_LIMIT || *(volatile int*)err) { good = 0; break; }
+            if (++spins > spin_limit || *(volatile int*)err) { good = 0; break; }
             __nanosleep(64);
         }
         __threadfence();
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     __shared__ int sh_flag[3];
     auto preduce = [&](double v, bool& ok) -> double {
         const double res = part_reduce(&a.sync[d], a.partial, dp.first_block, dp.nblocks, red & 1, v, a.err, sh,
-                                       sh_flag, &sh_val, ok);
+                                       sh_flag, &sh_val, ok, a.spin_limit, a.extra);
         ++red;
         return res;
     };
@@ -663,6 +665,9 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     a.sync = psync;
     a.partial = partial;
     a.err = err;
+    const WaitLimits wl = wait_limits();
+    a.spin_limit = wl.spin_limit;
+    a.extra = wl.extra;
     void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
     const int kt = c.kbegin("cg", 0.0);
     CK(cudaLaunchCooperativeKernel((void*)k_cg_all, dim3((unsigned)block_depth.size()), dim3(CG_BLOCK), kargs, 0, s));
@@ -711,6 +716,8 @@ struct CsrArgs {
     int max_iter;
     PartState* state;
     int* err;
+    long long spin_limit;
+    int extra;
 };
 
 __global__ void __launch_bounds__(CG_BLOCK) k_cg_csr(CsrArgs a) {
@@ -725,7 +732,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_csr(CsrArgs a) {
     auto preduce = [&](double v, bool& ok) -> double {
         double s = block_sum(v, sh);
         if (threadIdx.x == 0) atomicAdd(&ps->acc[red % 3], s);
-        ok = part_barrier(ps, nblocks, a.err, &sh_ok);
+        ok = part_barrier(ps, nblocks, a.err, &sh_ok, a.spin_limit, a.extra);
         if (threadIdx.x == 0) sh_val = *(volatile double*)&ps->acc[red % 3];
         __syncthreads();
         double res = sh_val;
@@ -749,7 +756,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_csr(CsrArgs a) {
         } else {
             for (i64 i = start; i < a.n; i += stride) a.p[i] = a.r[i];
         }
-        if (!part_barrier(ps, nblocks, a.err, &sh_ok)) break;
+        if (!part_barrier(ps, nblocks, a.err, &sh_ok, a.spin_limit, a.extra)) break;
         loc = 0;
         for (i64 i = start; i < a.n; i += stride) {
             float o = 0.f;
@@ -802,6 +809,9 @@ int cg_csr_impl(int n, const int* rowptr, const int* col, const float* val, cons
     a.max_iter = max_iter;
     a.state = st;
     a.err = err;
+    const WaitLimits wl = wait_limits();
+    a.spin_limit = wl.spin_limit;
+    a.extra = wl.extra;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
