@@ -62,7 +62,19 @@ typedef struct {
                              b_d - sum_{d'<d} L_{d,d'} x_{d'}, with the exact cross-depth
                              inner products over the 27 neighbours of each ancestor (Kazhdan's
                              coarse-to-fine formulation; not in the reference) */
-    int32_t reserved[5];
+    int32_t learned;      /* 0: plain CG, as the reference (CG_CUDA.cuh:256-324); 1: flexible CG
+                             preconditioned by the per-node network loaded with
+                             prgpu_load_preconditioner, with the same stopping rule, and plain CG
+                             taking over a depth whenever a learned step fails to reduce its
+                             residual (not in the reference) */
+    int32_t refine;       /* PRGPU_SOLVE_RELATIVE only.  0: stop on the CG recurrence's residual,
+                             as the reference does (CG_CUDA.cuh:284); 1: then recompute the true
+                             residual b - Ax with FP64 accumulation on the GPU and, while it is
+                             above tol*||b||, restart CG from the current x on it (at most two
+                             refinements); the true relative residual per depth is reported
+                             (the reference checks max|Ax-b| on the host afterwards,
+                             CG_CUDA.cuh:476-490) */
+    int32_t reserved[3];
 } prgpu_params;
 
 typedef struct {
@@ -229,6 +241,48 @@ int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* 
 int prgpu_cg_csr_noalloc(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* d_col,
                          const float* d_val, const float* d_rhs, float* d_x, float tol, int32_t max_iter,
                          void* stream, int32_t* iters);
+
+/* ---- learned preconditioner --------------------------------------------------
+ * None of these has a counterpart in the reference, which solves every depth with
+ * plain CG (CG_CUDA.cuh:256-324).  The network: per node, 64 features (the 27
+ * neighbours' residuals scaled by their largest magnitude, the 27 normalised
+ * stencil coefficients of the neighbours present, depth/16, zero padding) ->
+ * 64 -> 64 -> 1 with ReLU, BF16 weights and FP32 accumulation on the tensor cores;
+ * parameters as 8385 floats: W1[64][64] (out, in), b1[64], W2[64][64], b2[64],
+ * w3[64], b3.  Features are passed as BF16 bit patterns, 64 per row.
+ * Checkpoint file: "PRGPULPC", u32 version 1, u32 64, u32 64, u32 8385, i64 step,
+ * u64 seed, i64 epoch, then the parameters and Adam's two moment vectors (f32,
+ * little endian). */
+
+/* Loads a checkpoint's weights into the context (used when params.learned = 1). */
+int prgpu_load_preconditioner(void* ctx, const char* checkpoint_path);
+
+/* A trainer: parameters (initialised from the seed), Adam state and training
+ * samples on one device. */
+int prgpu_trainer_create(int32_t device, uint64_t seed, void** trainer);
+int prgpu_trainer_destroy(void* trainer);
+/* Residual/error pairs of plain CG on ctx's system (after prgpu_compute_rhs):
+ * the solution to relative 1e-7, then the iterates after 1, 2, 3, 5, 8, 12 and 20
+ * iterations; rows_per_depth random rows of every depth >= 1 per iterate.  The
+ * context's x is left at the solution.  *added may be NULL. */
+int prgpu_trainer_record(void* trainer, void* ctx, int32_t rows_per_depth, int64_t* added);
+/* Adam steps on shuffled minibatches of the recorded samples (mean squared
+ * error); *loss (may be NULL) receives the last minibatch's loss. */
+int prgpu_trainer_train(void* trainer, int32_t steps, int32_t batch, float lr, double* loss);
+int prgpu_trainer_save(void* trainer, const char* path);
+/* Resumes from a checkpoint: parameters, Adam state, step count and seed. */
+int prgpu_trainer_load(void* trainer, const char* path);
+int prgpu_trainer_info(void* trainer, int64_t* samples, int64_t* step);
+int prgpu_trainer_get_params(void* trainer, float* params);
+int prgpu_trainer_set_params(void* trainer, const float* params);
+/* Copies recorded samples [first, first+n) to host memory (features: 64 BF16 bit
+ * patterns per row; targets: one float per row). */
+int prgpu_trainer_samples(void* trainer, int64_t first, int64_t n, uint16_t* features, float* targets);
+/* The network on host feature rows: forward outputs y[n]; or the gradient of the
+ * mean squared error against targets (grad: 8385 floats) and the loss. */
+int prgpu_mlp_forward(void* trainer, const uint16_t* features, int64_t n, float* y);
+int prgpu_mlp_gradients(void* trainer, const uint16_t* features, const float* targets, int64_t n, float* grad,
+                        double* loss);
 
 /* PLY I/O (PointStream.inl:160-239 input; PlyWriteTriangles plyfile.cu:2769-2836 output).
  * prgpu_read_points returns library-owned arrays valid until the next call. */

@@ -28,6 +28,8 @@ _DTYPES = {
     "batch_tri": np.int64, "center": np.float32, "scale": np.float32, "iso": np.float32,
     "subdivide_roots": np.int64,
     "vcells": np.int64,
+    "vfield64": np.float64, "divergence64": np.float64, "x64": np.float64, "point_value64": np.float64,
+    "cg_iters64": np.int32, "stencil64": np.float64, "iso64": np.float64,
 }
 
 
@@ -56,6 +58,7 @@ def lib():
         L.orc_set_root_stride.argtypes = [vp, c_int]
         L.orc_set_cascadic.argtypes = [vp, c_int]
         L.orc_solve.argtypes = [vp, c_int, dbl, c_int]
+        L.orc_fp64_run.argtypes = [vp, dbl]
         L.orc_reconstruct.argtypes = [vp, c_int, dbl, c_int]
         L.orc_get.restype = vp
         L.orc_get.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(i64)]
@@ -110,6 +113,13 @@ class Oracle:
     def set_cascadic(self, on: bool = True):
         """Coarse-to-fine solve: each depth's right-hand side less the coarser solution."""
         lib().orc_set_cascadic(self._h, int(on))
+
+    def fp64_run(self, tol: float = 1e-6):
+        """Precision study: the pipeline after the octree and tables in FP64 (needs
+        build_basis(True)); results under vfield64, divergence64, x64,
+        point_value64, cg_iters64, iso64."""
+        if lib().orc_fp64_run(self._h, tol):
+            raise RuntimeError("fp64_run needs the full tables (build_basis(True))")
 
     def set_root_stride(self, stride: int):
         """Timing samples only: subdivide every stride-th root (0: none)."""

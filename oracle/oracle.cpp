@@ -330,7 +330,12 @@ struct Ctx {
     std::vector<int> cg_iters;              // D+1
     std::vector<float> cg_rr;               // D+1 final r.r
     std::vector<float> stencil;             // 27*(D+1)
+    std::vector<double> stencil64;          // the same entries before the cast to float
     int cascadic = 0;                       // coarse-to-fine solve (not the reference's)
+    // FP64 run (precision study)
+    std::vector<double> vfield64, divergence64, x64, point_value64;
+    std::vector<int> cg_iters64;
+    double iso64 = 0;
     // iso
     std::vector<float> point_value;
     float iso = 0;
@@ -578,6 +583,7 @@ static void build_basis(Ctx& c, bool full_tables) {
     const PPoly& dB = c.dbase_f;
     // same-depth stencil factors are translation invariant; record them per depth
     c.stencil.assign(27 * (D + 1), 0.f);
+    c.stencil64.assign(27 * (D + 1), 0.0);
     std::vector<double> sdot(2 * (D + 1)), sd2(2 * (D + 1));
     for (int d = 0; d <= D; ++d) {
         double w = 1.0 / (1 << d);
@@ -596,6 +602,7 @@ static void build_basis(Ctx& c, bool full_tables) {
             for (int a = 0; a < 3; ++a) { dt[a] = sdot[2 * d + dd[a]]; d2[a] = sd2[2 * d + dd[a]]; }
             double e = d2[0] * dt[1] * dt[2] + d2[1] * dt[0] * dt[2] + d2[2] * dt[0] * dt[1];
             c.stencil[27 * d + j] = (std::fabs(e) > (double)float(1e-6)) ? (float)e : 0.f;
+            c.stencil64[27 * d + j] = (std::fabs(e) > (double)float(1e-6)) ? e : 0.0;
         }
     }
     if (!full_tables) return;
@@ -868,6 +875,147 @@ static void point_values(Ctx& c) {
     double s = 0;
     for (i64 k = 0; k < c.N; ++k) s += c.point_value[k];
     c.iso = (float)s / (float)c.N;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 run (precision study; not a stage of the reference, which computes in
+// FP32 apart from its inner-product tables).  The same octree, normalised points
+// and FP64 inner-product tables; everything after them in double: the splat
+// with the closed-form B-spline F/F(0) (F the quadratic B-spline of support
+// [-1.5, 1.5], F(0) = 3/4: the function GaussianApproximation builds,
+// PPolynomial.inl:384-423), the divergence (main.cu:1007-1141 semantics), the
+// stencil with the same drop rule (main.cu:1143-1213), CG per depth from x0 = 0
+// to ||r|| <= tol ||b||, the implicit function at the points and the iso-value.
+// ---------------------------------------------------------------------------
+static inline double bspline_norm(double t) {
+    t = std::fabs(t);
+    if (t < 0.5) return (0.75 - t * t) / 0.75;
+    if (t < 1.5) {
+        const double u = 1.5 - t;
+        return 0.5 * u * u / 0.75;
+    }
+    return 0.0;
+}
+
+static void fp64_run(Ctx& c, double tol) {
+    const int D = c.D, res = c.res;
+    const i64 M = c.M, lo = c.base[D], nD = c.count[D];
+    const double sD = (double)(1 << D);
+    // splat
+    c.vfield64.assign(3 * nD, 0.0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 256)
+    for (i64 i = lo; i < lo + nD; ++i) {
+        int fi[3];
+        function_index(c, i, fi);
+        double oc[3], w;
+        for (int a = 0; a < 3; ++a) center_width_d(fi[a], oc[a], w);
+        double v[3] = {0, 0, 0};
+        for (int j = 0; j < 27; ++j) {
+            const int nb = c.neighs[27 * i + j];
+            if (nb == -1) continue;
+            for (int k = 0; k < c.pnum[nb]; ++k) {
+                const i64 pt = c.pidx[nb] + k;
+                const double wgt = bspline_norm((oc[0] - c.P[3 * pt]) * sD) * bspline_norm((oc[1] - c.P[3 * pt + 1]) * sD) *
+                                   bspline_norm((oc[2] - c.P[3 * pt + 2]) * sD);
+                for (int a = 0; a < 3; ++a) v[a] += wgt * (double)c.Nn[3 * pt + a];
+            }
+        }
+        for (int a = 0; a < 3; ++a) c.vfield64[3 * (i - lo) + a] = v[a];
+    }
+    // divergence
+    std::vector<int> fiD(3 * nD);
+    for (i64 s = 0; s < nD; ++s) function_index(c, lo + s, &fiD[3 * s]);
+    c.divergence64.assign(M, 0.0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(dynamic, 64)
+    for (i64 i = 0; i < M; ++i) {
+        int fi[3];
+        function_index(c, i, fi);
+        double val = 0;
+        for (int j = 0; j < 27; ++j) {
+            const int nb = c.neighs[27 * i + j];
+            if (nb == -1) continue;
+            for (int k = 0; k < c.dnum[nb]; ++k) {
+                const i64 o = c.didx[nb] + k;
+                const int* fo = &fiD[3 * o];
+                val += c.vfield64[3 * o] * c.ddot[(size_t)fi[0] + (size_t)fo[0] * res] +
+                       c.vfield64[3 * o + 1] * c.ddot[(size_t)fi[1] + (size_t)fo[1] * res] +
+                       c.vfield64[3 * o + 2] * c.ddot[(size_t)fi[2] + (size_t)fo[2] * res];
+            }
+        }
+        c.divergence64[i] = val;
+    }
+    // CG per depth in double
+    c.x64.assign(M, 0.0);
+    c.cg_iters64.assign(D + 1, 0);
+    for (int d = 0; d <= D; ++d) {
+        const i64 dlo = c.base[d], n = c.count[d];
+        const double* st = &c.stencil64[27 * d];
+        std::vector<double> r(n), p(n), q(n), xx(n, 0.0);
+        for (i64 i = 0; i < n; ++i) r[i] = c.divergence64[dlo + i];
+        auto dot = [&](const std::vector<double>& a, const std::vector<double>& b) {
+            double s = 0;
+#pragma omp parallel for num_threads(omp_threads(c)) reduction(+ : s) schedule(static)
+            for (i64 i = 0; i < n; ++i) s += a[i] * b[i];
+            return s;
+        };
+        const double bb = dot(r, r);
+        double rr = bb, rr0 = 0;
+        int k = 1;
+        while (rr > tol * tol * bb && k <= 100000) {
+            if (k == 1) p = r;
+            else {
+                const double beta = rr / rr0;
+                for (i64 i = 0; i < n; ++i) p[i] = r[i] + beta * p[i];
+            }
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(static)
+            for (i64 i = 0; i < n; ++i) {
+                double o = 0;
+                for (int j = 0; j < 27; ++j) {
+                    const int nb = c.neighs[27 * (dlo + i) + j];
+                    if (nb != -1 && st[j] != 0.0) o += st[j] * p[nb - dlo];
+                }
+                q[i] = o;
+            }
+            const double al = rr / dot(p, q);
+            for (i64 i = 0; i < n; ++i) {
+                xx[i] += al * p[i];
+                r[i] -= al * q[i];
+            }
+            rr0 = rr;
+            rr = dot(r, r);
+            ++k;
+        }
+        c.cg_iters64[d] = k - 1;
+        for (i64 i = 0; i < n; ++i) c.x64[dlo + i] = xx[i];
+    }
+    // implicit function at the points, iso-value
+    c.point_value64.assign(c.N, 0.0);
+#pragma omp parallel for num_threads(omp_threads(c)) schedule(static)
+    for (i64 k = 0; k < c.N; ++k) {
+        i64 node = c.point_node[k];
+        double val = 0.0;
+        const float* q = &c.P[3 * k];
+        while (node != -1) {
+            for (int j = 0; j < 27; ++j) {
+                const int nb = c.neighs[27 * node + j];
+                if (nb == -1) continue;
+                int fi[3];
+                function_index(c, nb, fi);
+                double v = c.x64[nb];
+                for (int a = 0; a < 3; ++a) {
+                    double cc, w;
+                    center_width_d(fi[a], cc, w);
+                    v *= bspline_norm(((double)q[a] - cc) / w);
+                }
+                val += v;
+            }
+            node = c.parent[node];
+        }
+        c.point_value64[k] = val;
+    }
+    double s = 0;
+    for (i64 k = 0; k < c.N; ++k) s += c.point_value64[k];
+    c.iso64 = s / (double)c.N;
 }
 
 // ---------------------------------------------------------------------------
@@ -1476,6 +1624,13 @@ int orc_divergence(void* h) { divergence(*(Ctx*)h); return 0; }
 int orc_solve(void* h, int mode, double tol, int max_iter) { return solve(*(Ctx*)h, mode, tol, max_iter); }
 int orc_set_cascadic(void* h, int on) { ((Ctx*)h)->cascadic = on != 0; return 0; }
 int orc_point_values(void* h) { point_values(*(Ctx*)h); return 0; }
+// FP64 run after build_octree and build_basis(full tables): see fp64_run
+int orc_fp64_run(void* h, double tol) {
+    Ctx* c = (Ctx*)h;
+    if (c->ddot.empty()) return -1;
+    fp64_run(*c, tol);
+    return 0;
+}
 int orc_marching_cubes(void* h) { marching_cubes(*(Ctx*)h); return 0; }
 // timing samples: subdivide every stride-th root only (0: none); the default 1 is the full path
 int orc_set_root_stride(void* h, int stride) { ((Ctx*)h)->root_stride = stride; return 0; }
@@ -1527,10 +1682,17 @@ const void* orc_get(void* h, const char* name, int64_t* count) {
     if (n == "has_tri") RET(c->has_tri);
     if (n == "has_int") RET(c->has_int);
     if (n == "batch_tri") RET(c->batch_tri);
+    if (n == "vfield64") RET(c->vfield64);
+    if (n == "divergence64") RET(c->divergence64);
+    if (n == "x64") RET(c->x64);
+    if (n == "point_value64") RET(c->point_value64);
+    if (n == "cg_iters64") RET(c->cg_iters64);
+    if (n == "stencil64") RET(c->stencil64);
 #undef RET
     if (n == "center") { *count = 3; return c->center; }
     if (n == "scale") { *count = 1; return &c->scale; }
     if (n == "iso") { *count = 1; return &c->iso; }
+    if (n == "iso64") { *count = 1; return &c->iso64; }
     if (n == "subdivide_roots") { *count = 1; return &c->subdivide_roots; }
     if (n == "vcells") { *count = 2; return c->vcells; }
     *count = -1;

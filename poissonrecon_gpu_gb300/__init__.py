@@ -53,8 +53,8 @@ class PrgpuError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("depth", ctypes.c_int32), ("solve_mode", ctypes.c_int32), ("cg_tol", ctypes.c_double),
                 ("cg_max_iter", ctypes.c_int32), ("device", ctypes.c_int32), ("weld", ctypes.c_int32),
-                ("density_weights", ctypes.c_int32), ("cascadic", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("density_weights", ctypes.c_int32), ("cascadic", ctypes.c_int32), ("learned", ctypes.c_int32),
+                ("refine", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class Mesh(ctypes.Structure):
@@ -96,6 +96,19 @@ SIGNATURES = {
     "prgpu_set_profiling": (ctypes.c_int, [_VP, _I32]),
     "prgpu_kernel_launches": (ctypes.c_int64, []),
     "prgpu_test_hook": (ctypes.c_int, [_I32, _I64, ctypes.POINTER(_I64)]),
+    "prgpu_load_preconditioner": (ctypes.c_int, [_VP, ctypes.c_char_p]),
+    "prgpu_trainer_create": (ctypes.c_int, [_I32, ctypes.c_uint64, ctypes.POINTER(_VP)]),
+    "prgpu_trainer_destroy": (ctypes.c_int, [_VP]),
+    "prgpu_trainer_record": (ctypes.c_int, [_VP, _VP, _I32, ctypes.POINTER(_I64)]),
+    "prgpu_trainer_train": (ctypes.c_int, [_VP, _I32, _I32, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]),
+    "prgpu_trainer_save": (ctypes.c_int, [_VP, ctypes.c_char_p]),
+    "prgpu_trainer_load": (ctypes.c_int, [_VP, ctypes.c_char_p]),
+    "prgpu_trainer_info": (ctypes.c_int, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "prgpu_trainer_get_params": (ctypes.c_int, [_VP, _VP]),
+    "prgpu_trainer_set_params": (ctypes.c_int, [_VP, _VP]),
+    "prgpu_trainer_samples": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP]),
+    "prgpu_mlp_forward": (ctypes.c_int, [_VP, _VP, _I64, _VP]),
+    "prgpu_mlp_gradients": (ctypes.c_int, [_VP, _VP, _VP, _I64, _VP, ctypes.POINTER(ctypes.c_double)]),
     "prgpu_cg_csr": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32,
                                     ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_float)]),
     "prgpu_cg_csr_noalloc": (ctypes.c_int, [_I32, _I32, _VP, _VP, _VP, _VP, _VP, ctypes.c_float, _I32, _VP,
@@ -137,7 +150,7 @@ class Reconstructor:
 
     def __init__(self, depth: int = 8, solve_mode: int = SOLVE_REFERENCE, cg_tol: float = 1e-5,
                  cg_max_iter: int = 10000, device: int = 0, weld: bool = False, density_weights: bool = False,
-                 cascadic: bool = False):
+                 cascadic: bool = False, preconditioner: str | None = None, refine: bool = False):
         L = _lib()
         p = Params()
         L.prgpu_params_default(ctypes.byref(p))
@@ -145,10 +158,18 @@ class Reconstructor:
         p.weld = 1 if weld else 0
         p.density_weights = 1 if density_weights else 0
         p.cascadic = 1 if cascadic else 0
+        p.learned = 1 if preconditioner else 0
+        p.refine = 1 if refine else 0
         self.params = p
         self._h = _VP()
         _check(L.prgpu_create(ctypes.byref(p), ctypes.byref(self._h)), "prgpu_create")
         self.depth = depth
+        if preconditioner:
+            self.load_preconditioner(preconditioner)
+
+    def load_preconditioner(self, path: str):
+        """Weights of the learned preconditioner from a checkpoint (used when learned=1)."""
+        _check(_lib().prgpu_load_preconditioner(self._h, os.fspath(path).encode()), "prgpu_load_preconditioner")
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -305,6 +326,97 @@ def solverCG_DeviceToDevice(N: int, nz: int, I: int, J: int, val: int, rhs: int,
     if rc not in (0, 5):
         raise PrgpuError(rc, "prgpu_cg_csr")
     return ms.value, it.value
+
+
+N_PARAMS = 8385
+# offsets in the parameter vector: W1 [64 out][64 in], b1, W2 [64][64], b2, w3, b3
+P_W1, P_B1, P_W2, P_B2, P_W3, P_B3 = 0, 4096, 4160, 8256, 8320, 8384
+
+
+def to_bf16_bits(a) -> np.ndarray:
+    """float32 -> bfloat16 bit patterns (round to nearest even)."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return r.astype(np.uint16)
+
+
+def from_bf16_bits(b) -> np.ndarray:
+    return (np.asarray(b, dtype=np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+class Trainer:
+    """The learned preconditioner's trainer on one GPU (prgpu_trainer_*): parameters,
+    Adam state and the residual/error samples recorded from plain CG."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self._h = _VP()
+        _check(_lib().prgpu_trainer_create(device, seed, ctypes.byref(self._h)), "prgpu_trainer_create")
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib().prgpu_trainer_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def record(self, rec: "Reconstructor", rows_per_depth: int = 256) -> int:
+        n = _I64(0)
+        _check(_lib().prgpu_trainer_record(self._h, rec._h, rows_per_depth, ctypes.byref(n)), "prgpu_trainer_record")
+        return n.value
+
+    def train(self, steps: int, batch: int = 8192, lr: float = 1e-3) -> float:
+        loss = ctypes.c_double(0)
+        _check(_lib().prgpu_trainer_train(self._h, steps, batch, lr, ctypes.byref(loss)), "prgpu_trainer_train")
+        return loss.value
+
+    def save(self, path: str):
+        _check(_lib().prgpu_trainer_save(self._h, os.fspath(path).encode()), "prgpu_trainer_save")
+
+    def load(self, path: str):
+        _check(_lib().prgpu_trainer_load(self._h, os.fspath(path).encode()), "prgpu_trainer_load")
+
+    def info(self):
+        ns, st = _I64(0), _I64(0)
+        _check(_lib().prgpu_trainer_info(self._h, ctypes.byref(ns), ctypes.byref(st)), "prgpu_trainer_info")
+        return {"samples": ns.value, "step": st.value}
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(N_PARAMS, np.float32)
+        _check(_lib().prgpu_trainer_get_params(self._h, out.ctypes.data), "prgpu_trainer_get_params")
+        return out
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        assert a.size == N_PARAMS
+        _check(_lib().prgpu_trainer_set_params(self._h, a.ctypes.data), "prgpu_trainer_set_params")
+
+    def samples(self, first: int = 0, n: int | None = None):
+        """Recorded samples: (features as bf16 bit patterns [n, 64], targets [n])."""
+        if n is None:
+            n = self.info()["samples"] - first
+        f = np.zeros((n, 64), np.uint16)
+        t = np.zeros(n, np.float32)
+        _check(_lib().prgpu_trainer_samples(self._h, first, n, f.ctypes.data, t.ctypes.data), "prgpu_trainer_samples")
+        return f, t
+
+    def forward(self, feat_bits) -> np.ndarray:
+        f = np.ascontiguousarray(feat_bits, dtype=np.uint16).reshape(-1, 64)
+        y = np.zeros(len(f), np.float32)
+        _check(_lib().prgpu_mlp_forward(self._h, f.ctypes.data, len(f), y.ctypes.data), "prgpu_mlp_forward")
+        return y
+
+    def gradients(self, feat_bits, targets):
+        f = np.ascontiguousarray(feat_bits, dtype=np.uint16).reshape(-1, 64)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(N_PARAMS, np.float32)
+        loss = ctypes.c_double(0)
+        _check(_lib().prgpu_mlp_gradients(self._h, f.ctypes.data, t.ctypes.data, len(f), g.ctypes.data,
+                                          ctypes.byref(loss)), "prgpu_mlp_gradients")
+        return g, loss.value
 
 
 def kernel_launches() -> int:

@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                    "-Xptxas", "-O3"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
-SOURCES = ["api.cu", "octree.cu", "basis.cu", "rhs.cu", "solve.cu", "iso.cu", "noalloc.cu", "ply.cpp"]
+SOURCES = ["api.cu", "octree.cu", "basis.cu", "rhs.cu", "solve.cu", "iso.cu", "noalloc.cu", "learned.cu", "flexcg.cu",
+           "ply.cpp"]
 
 
 def _run(cmd):

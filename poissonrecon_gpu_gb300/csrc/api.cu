@@ -8,7 +8,10 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "context.h"
+#include "learned.h"
 #include "prims.cuh"
 
 namespace prgpu {
@@ -225,6 +228,9 @@ int prgpu_destroy(void* h) {
     CK(cudaSetDevice(c->device));
     c->free_all();
     CK(cudaStreamSynchronize(c->stream));
+    if (c->lp_params) cudaFree(c->lp_params);
+    if (c->lp_w1b) cudaFree(c->lp_w1b);
+    if (c->lp_w2b) cudaFree(c->lp_w2b);
     for (auto e : c->kevents) cudaEventDestroy(e);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
@@ -692,6 +698,26 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
         snprintf(tmp, sizeof tmp, "%s%d", d ? "," : "", c->cg_iters[d]);
         js += tmp;
     }
+    js += "],\"cg_fallback\":[";
+    for (size_t d = 0; d < c->cg_fallback.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%d", d ? "," : "", c->cg_fallback[d]);
+        js += tmp;
+    }
+    js += "],\"cg_rel_residual\":[";
+    for (size_t d = 0; d < c->cg_true_rel.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%.6g", d ? "," : "", c->cg_true_rel[d]);
+        js += tmp;
+    }
+    js += "],\"cg_fp64_residual\":[";
+    for (size_t d = 0; d < c->cg_fp64_rel.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%.6g", d ? "," : "", c->cg_fp64_rel[d]);
+        js += tmp;
+    }
+    js += "],\"cg_refinements\":[";
+    for (size_t d = 0; d < c->cg_refines.size(); ++d) {
+        snprintf(tmp, sizeof tmp, "%s%d", d ? "," : "", c->cg_refines[d]);
+        js += tmp;
+    }
     snprintf(tmp, sizeof tmp,
              "],\"ms\":{\"octree\":%.4f,\"basis\":%.4f,\"splat\":%.4f,\"divergence\":%.4f,\"solve\":%.4f,"
              "\"iso\":%.4f,\"mesh\":%.4f},",
@@ -766,6 +792,175 @@ int prgpu_test_hook(int32_t what, int64_t arg, int64_t* out) {
         set_last_error("prgpu_test_hook: unknown hook %d", what);
         return PRGPU_ERR_ARG;
     }
+}
+
+// ----------------------------- learned preconditioner ------------------------
+static Trainer* as_tr(void* p) { return (Trainer*)p; }
+
+int prgpu_load_preconditioner(void* h, const char* path) {
+    Ctx* c = as_ctx(h);
+    if (!c || !path) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(c->device));
+    std::vector<float> hp, hm, hv;
+    i64 step = 0, epoch = 0;
+    uint64_t seed = 0;
+    read_checkpoint(path, hp, hm, hv, step, seed, epoch);
+    if (!c->lp_params) {
+        CK(cudaMalloc(&c->lp_params, P_COUNT * sizeof(float)));
+        CK(cudaMalloc(&c->lp_w1b, 4096 * sizeof(__nv_bfloat16)));
+        CK(cudaMalloc(&c->lp_w2b, 4096 * sizeof(__nv_bfloat16)));
+    }
+    std::vector<__nv_bfloat16> b1(4096), b2(4096);
+    for (int k = 0; k < 4096; ++k) {
+        b1[k] = __float2bfloat16_rn(hp[P_W1 + k]);
+        b2[k] = __float2bfloat16_rn(hp[P_W2 + k]);
+    }
+    CK(cudaMemcpyAsync(c->lp_params, hp.data(), P_COUNT * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->lp_w1b, b1.data(), 4096 * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->lp_w2b, b2.data(), 4096 * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_create(int32_t device, uint64_t seed, void** out) {
+    if (!out) return PRGPU_ERR_ARG;
+    API_BEGIN
+    *out = new Trainer(device, seed);
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_destroy(void* t) {
+    if (!t) return PRGPU_ERR_ARG;
+    delete as_tr(t);
+    return PRGPU_OK;
+}
+
+int prgpu_trainer_record(void* t, void* h, int32_t rows_per_depth, int64_t* added) {
+    Trainer* T = as_tr(t);
+    Ctx* c = as_ctx(h);
+    if (!T || !c || rows_per_depth < 1) return PRGPU_ERR_ARG;
+    REQUIRE_STAGE(c, 3);
+    if (c->device != T->device) {
+        set_last_error("trainer on device %d, context on device %d", T->device, c->device);
+        return PRGPU_ERR_ARG;
+    }
+    API_BEGIN_CTX(c)
+    CK(cudaSetDevice(c->device));
+    const i64 n = T->record(*c, rows_per_depth);
+    if (added) *added = n;
+    c->stage = std::max(c->stage, 4);
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_train(void* t, int32_t steps, int32_t batch, float lr, double* loss) {
+    Trainer* T = as_tr(t);
+    if (!T || steps < 0 || batch < 1 || !(lr > 0.f)) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(T->device));
+    const double l = T->train(steps, batch, lr);
+    if (loss) *loss = l;
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_save(void* t, const char* path) {
+    if (!t || !path) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(as_tr(t)->device));
+    as_tr(t)->save(path);
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_load(void* t, const char* path) {
+    if (!t || !path) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(as_tr(t)->device));
+    as_tr(t)->load(path);
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_info(void* t, int64_t* samples, int64_t* step) {
+    if (!t) return PRGPU_ERR_ARG;
+    if (samples) *samples = as_tr(t)->nsamples;
+    if (step) *step = as_tr(t)->step;
+    return PRGPU_OK;
+}
+
+int prgpu_trainer_get_params(void* t, float* params) {
+    if (!t || !params) return PRGPU_ERR_ARG;
+    API_BEGIN
+    Trainer* T = as_tr(t);
+    CK(cudaSetDevice(T->device));
+    CK(cudaMemcpyAsync(params, T->p, P_COUNT * sizeof(float), cudaMemcpyDeviceToHost, T->stream));
+    CK(cudaStreamSynchronize(T->stream));
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_set_params(void* t, const float* params) {
+    if (!t || !params) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(as_tr(t)->device));
+    as_tr(t)->set_params(params, nullptr, nullptr);
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_trainer_samples(void* t, int64_t first, int64_t n, uint16_t* features, float* targets) {
+    Trainer* T = as_tr(t);
+    if (!T || first < 0 || n < 0 || first + n > T->nsamples) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(T->device));
+    if (features && n)
+        CK(cudaMemcpyAsync(features, T->feat + first * 64, (size_t)n * 128, cudaMemcpyDeviceToHost, T->stream));
+    if (targets && n)
+        CK(cudaMemcpyAsync(targets, T->target + first, (size_t)n * 4, cudaMemcpyDeviceToHost, T->stream));
+    CK(cudaStreamSynchronize(T->stream));
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_mlp_forward(void* t, const uint16_t* features, int64_t n, float* y) {
+    Trainer* T = as_tr(t);
+    if (!T || !features || !y || n < 1) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(T->device));
+    cudaStream_t s = T->stream;
+    __nv_bfloat16* df = dalloc<__nv_bfloat16>(n * 64, s);
+    float* dy = dalloc<float>(n, s);
+    CK(cudaMemcpyAsync(df, features, (size_t)n * 128, cudaMemcpyHostToDevice, s));
+    T->forward(df, n, dy);
+    CK(cudaMemcpyAsync(y, dy, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    dfree(df, s);
+    dfree(dy, s);
+    return PRGPU_OK;
+    API_END
+}
+
+int prgpu_mlp_gradients(void* t, const uint16_t* features, const float* targets, int64_t n, float* grad, double* loss) {
+    Trainer* T = as_tr(t);
+    if (!T || !features || !targets || !grad || n < 1) return PRGPU_ERR_ARG;
+    API_BEGIN
+    CK(cudaSetDevice(T->device));
+    cudaStream_t s = T->stream;
+    __nv_bfloat16* df = dalloc<__nv_bfloat16>(n * 64, s);
+    float* dt = dalloc<float>(n, s);
+    CK(cudaMemcpyAsync(df, features, (size_t)n * 128, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dt, targets, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    const double l = T->gradients(df, dt, n, grad);
+    if (loss) *loss = l;
+    dfree(df, s);
+    dfree(dt, s);
+    CK(cudaStreamSynchronize(s));
+    return PRGPU_OK;
+    API_END
 }
 
 int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* rowptr, const int32_t* col, const float* val, const float* rhs,

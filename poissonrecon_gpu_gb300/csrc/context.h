@@ -113,6 +113,15 @@ struct Ctx {
     i64 x_rows = 0;                  // rows x was allocated for
     std::vector<int> cg_iters;
     std::vector<float> cg_rr;
+    std::vector<int> cg_fallback;    // learned solve: iteration at which plain CG took a depth over (-1: never)
+    std::vector<double> cg_true_rel; // final relative residual of the CG recurrence per depth (FP64 reductions)
+    std::vector<double> cg_fp64_rel; // params.refine: |b - Ax| / |b| recomputed in FP64 (-1: not computed)
+    std::vector<int> cg_refines;     // params.refine: restarts on the recomputed residual
+
+    // learned preconditioner weights (prgpu_load_preconditioner), owned by the context
+    float* lp_params = nullptr;      // fp32 parameter vector
+    void* lp_w1b = nullptr;          // bf16 [64][64]
+    void* lp_w2b = nullptr;
     int* d_cg_iters = nullptr;
     float* d_cg_rr = nullptr;
 
@@ -161,6 +170,11 @@ void stage_splat(Ctx& c);
 void stage_divergence(Ctx& c);
 void stage_solve(Ctx& c);
 void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs = nullptr);
+void stage_solve_learned(Ctx& c);   // flexcg.cu
+// co-resident blocks of the persistent solvers split between depths d0..d1 in proportion
+// to their rows (one block for a depth of at most 4*256 rows); fills deps and block_depth
+struct CgDepth;
+void partition_depths(const Ctx& c, int d0, int d1, int G, std::vector<CgDepth>& deps, std::vector<int>& block_depth);
 void cascade_rhs(Ctx& c, int d, float* rhs);   // depth d's rows of an M-row device buffer
 void ensure_group_table(Ctx& c);
 void stage_points(Ctx& c);

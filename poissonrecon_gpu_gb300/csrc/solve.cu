@@ -25,51 +25,12 @@
 #include <cmath>
 #include <vector>
 
+#include "cg_common.cuh"
 #include "context.h"
 #include "prims.cuh"
 
 namespace prgpu {
 
-constexpr int CG_BLOCK = 256;
-
-struct PartState {          // one per depth, in global memory, zero-initialised
-    double acc[3];
-    unsigned count;
-    unsigned gen;
-    int iters;
-    float rr;
-    int status;
-    int pad;
-};
-
-// reduction barrier of one depth's partition in k_cg_all: arrival counter, release
-// generation and result on separate cache lines (the blocks poll 'gen' while the
-// last one sums)
-struct alignas(128) PartSync {
-    unsigned count;
-    unsigned pad0[31];
-    unsigned gen;
-    unsigned pad1[31];
-    double res[2];
-    double pad2[14];
-};
-
-struct CgDepth {
-    i64 lo, n;              // global row range
-    int first_block, nblocks;
-    float st[27];
-    // The Laplacian stencil is symmetric under the reflections and permutations of the
-    // axes (a product of symmetric 1-D tables), so entry j depends only on how many of
-    // its offsets are nonzero: cls[0] centre, [1] faces, [2] edges, [3] corners.  sym = 1
-    // when the float entries are exactly so; the matrix-vector product then keeps the
-    // four values in registers (the same values in the same FMA order).
-    float cls[4];
-    int sym;
-};
-
-__host__ __device__ constexpr int stencil_class(int j) {
-    return (j / 9 != 1) + ((j / 3) % 3 != 1) + (j % 3 != 1);
-}
 
 struct CgArgs {
     int ndepth;
@@ -93,18 +54,8 @@ struct CgArgs {
     int* err;
     long long spin_limit;   // bounded waits (WaitLimits)
     int extra;
+    int refine;             // relative mode: FP64 true-residual check and refinement
 };
-
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double s = 0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
-    __syncthreads();
-    return s;   // valid in thread 0
-}
 
 // barrier over the blocks of one partition; returns false after a timeout
 __device__ bool part_barrier(PartState* ps, int nblocks, int* err, int* sh_ok, long long spin_limit, int extra) {
@@ -188,19 +139,6 @@ __device__ double part_reduce(PartSync* ps, double* partial, int first_block, in
     return *sh_val;
 }
 
-// per-thread partial dot product: a compensated float pair (Neumaier), exact to
-// about 2u|sum| + n u^2 sum|term| -- FP64 accuracy for a thread's few dozen rows
-// without FP64 arithmetic per row
-struct FSum {
-    float h = 0.f, l = 0.f;
-    __device__ __forceinline__ void add(float v) {
-        const float t = h + v;
-        l += (fabsf(h) >= fabsf(v)) ? (h - t) + v : (v - t) + h;
-        h = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)h + (double)l; }
-};
-
 // per sibling group: first child of each of the parent's 27 neighbours (-1: none or a leaf)
 __global__ void k_group_table(NodeArrays nd, i64 ngroups, int* __restrict__ gn) {
     const i64 M = nd.M;
@@ -256,14 +194,40 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     float r1 = (float)bb;
     float r0 = 0.f;
     int k = 1;
+    int refines = 0;
+    double rr_true = -1.0;
+    bool restart = true;
     // p = r + beta p is formed where p is read: from the previous direction in
     // 'pold' (never written during the pass) into 'pnew' (each row by its own thread)
     const float* pold = a.p2;
     float* pnew = a.p;
     while (ok) {
         const bool go = (a.mode == PRGPU_SOLVE_REFERENCE) ? (r1 > a.tol2) : ((double)r1 > a.rel2 * bb);
-        if (!go || k > a.max_iter) break;
-        const bool first = (k == 1);
+        if (!go || k > a.max_iter) {
+            if (!a.refine || a.mode != PRGPU_SOLVE_RELATIVE || k > a.max_iter) break;
+            // the recurrence says converged: recompute r = b - A x with FP64 accumulation
+            double tsum = 0.0;
+            for (i64 t = start; t < dp.n; t += stride) {
+                const i64 i = dp.lo + t;
+                double acc = (double)a.b[i];
+#pragma unroll
+                for (int j = 0; j < 27; ++j) {
+                    const int nb = a.neigh[(i64)j * a.M + i];
+                    if (nb != -1) acc = fma(-(double)sst[j], (double)a.x[nb], acc);
+                }
+                a.r[i] = (float)acc;
+                tsum = fma(acc, acc, tsum);
+            }
+            rr_true = preduce(tsum, ok);
+            if (!ok || rr_true <= a.rel2 * bb || refines >= 2) break;
+            // restart CG from the current x on the true residual
+            ++refines;
+            r1 = (float)rr_true;
+            restart = true;
+            continue;
+        }
+        const bool first = restart;
+        restart = false;
         const float beta = first ? 0.f : r1 / r0;
         auto pdir = [&](i64 i) -> float { return first ? a.r[i] : fmaf(beta, pold[i], a.r[i]); };
         // q = A p, partial p.q
@@ -379,6 +343,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     if (rank == 0 && threadIdx.x == 0) {
         ps->iters = k - 1;
         ps->rr = r1;
+        ps->bb = bb;
+        ps->rr_true = rr_true;
+        ps->refines = refines;
         ps->status = ok ? 0 : PRGPU_ERR_TIMEOUT;
     }
 }
@@ -536,6 +503,10 @@ void cascade_rhs(Ctx& c, int d, float* rhs) {
 }
 
 void stage_solve(Ctx& c) {
+    if (c.params.learned) {
+        stage_solve_learned(c);
+        return;
+    }
     if (!c.params.cascadic) {
         stage_solve_depths(c, 0, c.D, c.params.solve_mode);
         return;
@@ -554,6 +525,58 @@ void stage_solve(Ctx& c) {
         stage_solve_depths(c, d, d, c.params.solve_mode, rhs);
     }
     dfree(rhs, s);
+}
+
+// co-resident blocks split between the depths d0..d1: one block for a depth of at most
+// 4*256 rows, the rest in proportion to the rows; the depths outside d0..d1 get none
+void partition_depths(const Ctx& c, int d0, int d1, int G, std::vector<CgDepth>& deps, std::vector<int>& block_depth) {
+    const int D = c.D;
+    deps.assign(D + 1, CgDepth());
+    std::vector<int> nb(D + 1, 0);
+    i64 big_rows = 0;
+    const i64 small_rows = 4 * CG_BLOCK;
+    int fixed = 0;
+    for (int d = d0; d <= d1; ++d) {
+        nb[d] = 1;
+        if (c.count[d] <= small_rows) ++fixed;
+        else big_rows += c.count[d];
+    }
+    int avail = std::max(0, G - fixed);
+    for (int d = d0; d <= d1; ++d) {
+        if (c.count[d] > small_rows) {
+            i64 want = (i64)((double)avail * (double)c.count[d] / (double)std::max<i64>(big_rows, 1));
+            i64 cap = (c.count[d] + CG_BLOCK - 1) / CG_BLOCK;
+            nb[d] = (int)std::max<i64>(1, std::min(want, cap));
+        }
+    }
+    int total = 0;
+    for (int d = 0; d <= D; ++d) total += nb[d];
+    while (total > G) {   // trim the largest partitions
+        int dm = (int)(std::max_element(nb.begin(), nb.end()) - nb.begin());
+        if (nb[dm] <= 1) break;
+        --nb[dm];
+        --total;
+    }
+    if (total > G) {
+        set_last_error("solver needs %d co-resident blocks, device offers %d", total, G);
+        throw Error{PRGPU_ERR_LIMIT, {0}};
+    }
+    block_depth.clear();
+    for (int d = 0; d <= D; ++d) {
+        deps[d].lo = c.base[d];
+        deps[d].n = c.count[d];
+        deps[d].first_block = (int)block_depth.size();
+        deps[d].nblocks = nb[d];
+        for (int j = 0; j < 27; ++j) deps[d].st[j] = c.stencil[27 * d + j];
+        deps[d].sym = 1;
+        for (int j = 0; j < 27; ++j) {
+            const int k = stencil_class(j);
+            const float rep = c.stencil[27 * d + (k == 0 ? 13 : k == 1 ? 4 : k == 2 ? 1 : 0)];
+            if (c.stencil[27 * d + j] != rep) deps[d].sym = 0;
+            deps[d].cls[k] = rep;
+        }
+        for (int k = 0; k < nb[d]; ++k) block_depth.push_back(d);
+    }
 }
 
 // depths d0..d1 with the given mode (right-hand side: rhs, or the divergence);
@@ -586,53 +609,9 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_all, CG_BLOCK, 0));
     if (per_sm < 1) per_sm = 1;
     const int G = sms * per_sm;
-    // partition: one block per small depth, the rest in proportion to rows
-    std::vector<CgDepth> deps(D + 1);
-    std::vector<int> nb(D + 1, 0);
-    i64 big_rows = 0;
-    const i64 small_rows = 4 * CG_BLOCK;
-    int fixed = 0;
-    for (int d = d0; d <= d1; ++d) {
-        nb[d] = 1;
-        if (c.count[d] <= small_rows) ++fixed;
-        else big_rows += c.count[d];
-    }
-    int avail = std::max(0, G - fixed);
-    for (int d = d0; d <= d1; ++d) {
-        if (c.count[d] > small_rows) {
-            i64 want = (i64)((double)avail * (double)c.count[d] / (double)std::max<i64>(big_rows, 1));
-            i64 cap = (c.count[d] + CG_BLOCK - 1) / CG_BLOCK;
-            nb[d] = (int)std::max<i64>(1, std::min(want, cap));
-        }
-    }
-    int total = 0;
-    for (int d = 0; d <= D; ++d) total += nb[d];
-    while (total > G) {   // trim the largest partitions
-        int dm = (int)(std::max_element(nb.begin(), nb.end()) - nb.begin());
-        if (nb[dm] <= 1) break;
-        --nb[dm];
-        --total;
-    }
-    if (total > G) {
-        set_last_error("solver needs %d co-resident blocks, device offers %d", total, G);
-        throw Error{PRGPU_ERR_LIMIT, {0}};
-    }
+    std::vector<CgDepth> deps;
     std::vector<int> block_depth;
-    for (int d = 0; d <= D; ++d) {
-        deps[d].lo = c.base[d];
-        deps[d].n = c.count[d];
-        deps[d].first_block = (int)block_depth.size();
-        deps[d].nblocks = nb[d];
-        for (int j = 0; j < 27; ++j) deps[d].st[j] = c.stencil[27 * d + j];
-        deps[d].sym = 1;
-        for (int j = 0; j < 27; ++j) {
-            const int k = stencil_class(j);
-            const float rep = c.stencil[27 * d + (k == 0 ? 13 : k == 1 ? 4 : k == 2 ? 1 : 0)];
-            if (c.stencil[27 * d + j] != rep) deps[d].sym = 0;
-            deps[d].cls[k] = rep;
-        }
-        for (int k = 0; k < nb[d]; ++k) block_depth.push_back(d);
-    }
+    partition_depths(c, d0, d1, G, deps, block_depth);
     CgDepth* ddeps = dalloc<CgDepth>(D + 1, s);
     int* dbd = dalloc<int>((i64)block_depth.size(), s);
     PartState* st = dalloc<PartState>(D + 1, s);
@@ -668,6 +647,7 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     const WaitLimits wl = wait_limits();
     a.spin_limit = wl.spin_limit;
     a.extra = wl.extra;
+    a.refine = c.params.refine;
     void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
     const int kt = c.kbegin("cg", 0.0);
     CK(cudaLaunchCooperativeKernel((void*)k_cg_all, dim3((unsigned)block_depth.size()), dim3(CG_BLOCK), kargs, 0, s));
@@ -682,7 +662,17 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
         c.cg_iters.assign(D + 1, 0);
         c.cg_rr.assign(D + 1, 0.f);
     }
-    for (int d = d0; d <= d1; ++d) { c.cg_iters[d] = hs[d].iters; c.cg_rr[d] = hs[d].rr; }
+    c.cg_fallback.assign(D + 1, -1);
+    c.cg_true_rel.resize(D + 1, 0.0);
+    c.cg_fp64_rel.resize(D + 1, -1.0);
+    c.cg_refines.resize(D + 1, 0);
+    for (int d = d0; d <= d1; ++d) {
+        c.cg_iters[d] = hs[d].iters;
+        c.cg_rr[d] = hs[d].rr;
+        c.cg_true_rel[d] = hs[d].bb > 0 ? std::sqrt((double)hs[d].rr / hs[d].bb) : 0.0;
+        c.cg_fp64_rel[d] = (hs[d].rr_true >= 0 && hs[d].bb > 0) ? std::sqrt(hs[d].rr_true / hs[d].bb) : -1.0;
+        c.cg_refines[d] = hs[d].refines;
+    }
     if (kt >= 0) {
         // compulsory per row and iteration: the group table (27 indices per 8 rows), the
         // previous direction and r read once, p and q written, then p/q/x/r read and x/r

@@ -1,0 +1,204 @@
+"""Pins the library and the CPU oracle to the reference's own CUDA build.
+
+Runs on a machine with a GPU and the reference build (oracle/ref_cuda.sh builds
+oracle/_ref/ref_cuda from the reference sources, unchanged; maxDepth is 8 there,
+main.cu:69), on the 50,000-point sphere (shapes.sphere(50000, seed=0), radius
+0.35, centre (0.5,0.5,0.5), exact normals) written as a binary PLY file:
+
+  1. the reference's pipelineBuildNodeArray (main.cu:511-841), three runs, node
+     arrays dumped (ref_cuda octree) and compared run to run (the racy parent map);
+  2. the reference's stock main() (main.cu:3247-4573), three runs: its printed
+     stage times, iso-value and CG time, its ASCII mesh, and the process's wall time;
+  3. this library on the same points with the same solver schedule (absolute
+     tolerance 1e-5, at most 10000 iterations per depth): node arrays, iso-value,
+     mesh, device time, and file-to-file wall time (binary PLY in, ASCII PLY out,
+     as the reference writes).
+
+Writes <out>/ref_cuda_sphere50k_d8.npz (per-field SHA-256 digests of the
+reference's arrays, the positions where they differ from this library's and both
+values there, the level sizes, centre and scale) and
+<out>/ref_cuda_sphere50k_d8.json (counts, times, iso-values, mesh sizes, the
+symmetric Hausdorff distance between the meshes).  Copy both into tests/golden/.
+
+Usage:  python tests/golden/gen_reference_cuda.py <out_dir>
+"""
+import hashlib
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+REF = os.path.join(REPO, "oracle", "_ref", "ref_cuda")
+D = 8
+FIELDS = ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum", "points", "normals", "point_node")
+
+
+def write_points_ply(path, xyz, nrm):
+    with open(path, "wb") as fh:
+        fh.write(b"ply\nformat binary_little_endian 1.0\nelement vertex %d\n" % len(xyz))
+        for k in ("x", "y", "z", "nx", "ny", "nz"):
+            fh.write(b"property float %s\n" % k.encode())
+        fh.write(b"end_header\n")
+        fh.write(np.concatenate([xyz, nrm], 1).astype("<f4").tobytes())
+
+
+def read_octree_dump(path):
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"PRREFOCT"
+    hdr = np.frombuffer(raw, np.int32, 4, 8)
+    version, depth, npts, nodes = (int(v) for v in hdr)
+    assert version == 1 and depth == D
+    off = 24
+    counts = np.frombuffer(raw, np.int32, D + 1, off); off += 4 * (D + 1)
+    base = np.frombuffer(raw, np.int32, D + 1, off); off += 4 * (D + 1)
+    cs = np.frombuffer(raw, np.float32, 4, off); off += 16
+    pts = np.frombuffer(raw, np.float32, 3 * npts, off); off += 12 * npts
+    nrm = np.frombuffer(raw, np.float32, 3 * npts, off); off += 12 * npts
+    p2n = np.frombuffer(raw, np.int32, npts, off); off += 4 * npts
+    rec = np.frombuffer(raw, np.int32, 41 * nodes, off).reshape(nodes, 41)
+    return {"counts": counts.astype(np.int64), "base": base.astype(np.int64), "center": cs[:3].copy(),
+            "scale": cs[3:4].copy(), "points": pts.copy(), "normals": nrm.copy(), "point_node": p2n.copy(),
+            "key": rec[:, 0].astype(np.int64), "pidx": rec[:, 1].copy(), "pnum": rec[:, 2].copy(),
+            "parent": rec[:, 3].copy(), "children": rec[:, 4:12].ravel().copy(),
+            "neighs": rec[:, 12:39].ravel().copy(), "didx": rec[:, 39].copy(), "dnum": rec[:, 40].copy()}
+
+
+def read_ascii_mesh(path):
+    with open(path, "rb") as fh:
+        nv = nf = 0
+        while True:
+            line = fh.readline().decode().strip()
+            if line.startswith("element vertex"):
+                nv = int(line.split()[2])
+            elif line.startswith("element face"):
+                nf = int(line.split()[2])
+            elif line == "end_header":
+                break
+        rest = fh.read().decode().split("\n")
+    v = np.array([[float(t) for t in rest[i].split()[:3]] for i in range(nv)], np.float32).reshape(-1, 3)
+    f = np.array([[int(t) for t in rest[nv + i].split()[1:4]] for i in range(nf)], np.int32).reshape(-1, 3)
+    return v, f
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def hausdorff(a, b):
+    from scipy.spatial import cKDTree
+    return float(max(cKDTree(b).query(a)[0].max(), cKDTree(a).query(b)[0].max()))
+
+
+def main(out):
+    import poissonrecon_gpu_gb300 as pg
+    from poissonrecon_gpu_gb300 import shapes
+    os.makedirs(out, exist_ok=True)
+    if not os.path.exists(REF):
+        subprocess.check_call(["sh", os.path.join(REPO, "oracle", "ref_cuda.sh"), "build"])
+    xyz, nrm = shapes.sphere(50000, seed=0)
+    summary = {"workload": "sphere, 50,000 points (shapes.sphere seed 0), maxDepth 8, binary PLY"}
+    work = tempfile.mkdtemp(prefix="prgpu_refcuda_")
+    ply = os.path.join(work, "bunny.points.ply")   # the file name main() opens (main.cu:3251)
+    write_points_ply(ply, xyz, nrm)
+
+    # 1. node arrays, three runs
+    dumps = []
+    for k in range(3):
+        path = os.path.join(work, "octree%d.bin" % k)
+        subprocess.check_call([REF, "octree", ply, path], timeout=600, stdout=subprocess.DEVNULL)
+        dumps.append(read_octree_dump(path))
+    ref = dumps[0]
+    summary["run_to_run_differences"] = {f: [int(np.count_nonzero(dumps[j][f] != ref[f])) for j in (1, 2)]
+                                         for f in FIELDS}
+
+    # 2. the stock main(), three runs
+    runs = []
+    for k in range(3):
+        env = dict(os.environ, PRGPU_REF_IO_DIR=work)
+        t0 = time.perf_counter()
+        p = subprocess.run([REF, "pipeline"], env=env, timeout=900, capture_output=True, text=True)
+        wall = time.perf_counter() - t0
+        with open(os.path.join(out, "pipeline%d.log" % k), "w") as fh:
+            fh.write("returncode %d\n--- stdout\n%s\n--- stderr\n%s\n" % (p.returncode, p.stdout, p.stderr))
+        assert p.returncode == 0, p.stderr[-2000:]
+        runs.append((wall, p.stdout))
+    stdout = runs[-1][1]
+    iso_ref = float(re.search(r"isoValue:([-0-9.eE+]+)", stdout).group(1))
+    summary["reference"] = {
+        "main_wall_s": [float(re.search(r"prgpu_ref_wall_s ([0-9.]+)", r[1]).group(1)) for r in runs],
+        "process_wall_s": [r[0] for r in runs],
+        "whole_project_s": [float(re.search(r"The whole project takes ([0-9.]+)s", r[1]).group(1)) for r in runs],
+        "cg_ms": [float(re.search(r"Pure CG solving process takes:([0-9.]+)ms", r[1]).group(1)) for r in runs],
+        "iso_printed": iso_ref,
+        "stage_lines": [ln for ln in stdout.splitlines() if "takes" in ln],
+    }
+    rv, rf = read_ascii_mesh(os.path.join(work, "bunny.ply"))
+    summary["reference"]["mesh"] = {"vertices": int(len(rv)), "triangles": int(len(rf))}
+
+    # 3. this library, same points and solver schedule
+    r = pg.Reconstructor(depth=D)
+    gv, gf = r.reconstruct(xyz, nrm)
+    ours = {f: r.get(f) for f in ("key", "pidx", "pnum", "parent", "children", "neighs", "didx", "dnum", "points",
+                                  "normals", "point_node", "base", "count", "center", "scale")}
+    iso_ours = float(r.get("iso")[0])
+    st = r.stats()
+    ms = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        r.reconstruct(xyz, nrm)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    out_ply = os.path.join(work, "ours.ply")
+    f2f = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        px, pn = pg.read_points(ply)
+        v, f = r.reconstruct(px, pn)
+        pg.write_mesh(out_ply, v, f, binary=False)
+        f2f.append(time.perf_counter() - t0)
+    r.close()
+    summary["ours"] = {"iso": iso_ours, "mesh": {"vertices": int(len(gv)), "triangles": int(len(gf))},
+                       "reconstruct_ms_host_wall": ms, "stage_ms": st.get("ms"), "cg_iters": st.get("cg_iters"),
+                       "file_to_file_s": f2f}
+    # B2: subdivision batches of fewer than 32768 iso-vertices are never interpolated by the
+    # reference (main.cu:4152, 4509: a grid of n/32768 blocks); their vertices keep the
+    # buffer's initial contents and land at the centre offset after the output transform
+    center = ref["center"]
+    at_origin = np.all(np.abs(rv - center[None, :]) < 1e-6, axis=1)
+    summary["reference"]["mesh"]["vertices_at_output_origin"] = int(at_origin.sum())
+    tri_ok = ~np.any(at_origin[rf], axis=1)
+    summary["reference"]["mesh"]["triangles_without_such_vertices"] = int(tri_ok.sum())
+    used_r = np.unique(rf[tri_ok])
+    summary["hausdorff"] = hausdorff(gv[np.unique(gf)], rv[used_r])
+    summary["diagonal"] = float(np.linalg.norm(xyz.max(0) - xyz.min(0)))
+
+    # node arrays: digests of the reference's, and where they differ from ours
+    arrays = {"counts": ref["counts"], "base": ref["base"], "center": ref["center"], "scale": ref["scale"]}
+    summary["fields"] = {}
+    for fld in FIELDS:
+        a = ref[fld]
+        b = ours[fld].astype(a.dtype) if fld != "key" else ours[fld].astype(np.int64)
+        assert a.shape == b.shape, (fld, a.shape, b.shape)
+        arrays["sha256_" + fld] = np.array(digest(a))
+        idx = np.nonzero(a != b)[0]
+        arrays["diff_%s_idx" % fld] = idx.astype(np.int64)
+        arrays["diff_%s_ref" % fld] = a[idx]
+        arrays["diff_%s_ours" % fld] = b[idx]
+        summary["fields"][fld] = {"entries": int(a.size), "differ": int(len(idx))}
+    np.savez_compressed(os.path.join(out, "ref_cuda_sphere50k_d8.npz"), **arrays)
+    with open(os.path.join(out, "ref_cuda_sphere50k_d8.json"), "w") as fh:
+        json.dump(summary, fh, indent=1)
+    print(json.dumps({k: summary[k] for k in ("fields", "run_to_run_differences", "hausdorff")}, indent=1))
+
+
+if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    main(sys.argv[1])
