@@ -74,7 +74,13 @@ typedef struct {
                              refinements); the true relative residual per depth is reported
                              (the reference checks max|Ax-b| on the host afterwards,
                              CG_CUDA.cuh:476-490) */
-    int32_t reserved[3];
+    int32_t stable_basis; /* 0: basis values as the reference computes them in single precision:
+                             the B-spline shifted to the point, then evaluated
+                             (ConfirmedPPolynomial.cuh:37-91), whose coefficients grow as 4^depth,
+                             so their rounding error does too (about 1e-3 of the vector field at
+                             maxDepth 8, 2e-2 at 10); 1: the closed form of the same B-spline at an
+                             offset formed with one rounding (not in the reference) */
+    int32_t reserved[2];
 } prgpu_params;
 
 typedef struct {

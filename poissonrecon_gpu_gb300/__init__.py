@@ -54,7 +54,7 @@ class Params(ctypes.Structure):
     _fields_ = [("depth", ctypes.c_int32), ("solve_mode", ctypes.c_int32), ("cg_tol", ctypes.c_double),
                 ("cg_max_iter", ctypes.c_int32), ("device", ctypes.c_int32), ("weld", ctypes.c_int32),
                 ("density_weights", ctypes.c_int32), ("cascadic", ctypes.c_int32), ("learned", ctypes.c_int32),
-                ("refine", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("refine", ctypes.c_int32), ("stable_basis", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class Mesh(ctypes.Structure):
@@ -150,7 +150,8 @@ class Reconstructor:
 
     def __init__(self, depth: int = 8, solve_mode: int = SOLVE_REFERENCE, cg_tol: float = 1e-5,
                  cg_max_iter: int = 10000, device: int = 0, weld: bool = False, density_weights: bool = False,
-                 cascadic: bool = False, preconditioner: str | None = None, refine: bool = False):
+                 cascadic: bool = False, preconditioner: str | None = None, refine: bool = False,
+                 stable_basis: bool = False):
         L = _lib()
         p = Params()
         L.prgpu_params_default(ctypes.byref(p))
@@ -160,6 +161,7 @@ class Reconstructor:
         p.cascadic = 1 if cascadic else 0
         p.learned = 1 if preconditioner else 0
         p.refine = 1 if refine else 0
+        p.stable_basis = 1 if stable_basis else 0
         self.params = p
         self._h = _VP()
         _check(L.prgpu_create(ctypes.byref(p), ctypes.byref(self._h)), "prgpu_create")

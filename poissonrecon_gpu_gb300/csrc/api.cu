@@ -693,6 +693,8 @@ int prgpu_stats_json(void* h, char* buf, int64_t len) {
              (long long)c->super_decided,
              (unsigned long long)g_kernel_launches.load());
     js += tmp;
+    snprintf(tmp, sizeof tmp, ",\"solver_blocks\":%d", c->solver_blocks);
+    js += tmp;
     js += ",\"cg_iters\":[";
     for (size_t d = 0; d < c->cg_iters.size(); ++d) {
         snprintf(tmp, sizeof tmp, "%s%d", d ? "," : "", c->cg_iters[d]);

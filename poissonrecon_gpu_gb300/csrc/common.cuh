@@ -120,6 +120,26 @@ __device__ __forceinline__ float cpoly_value(const CPoly& p, float x) {
     return res;
 }
 
+// Closed form of the normalised basis F/F(0), F the quadratic B-spline of
+// support [-1.5, 1.5] with F(0) = 3/4 (what GaussianApproximation builds,
+// PPolynomial.inl:384-423), for params.stable_basis.  Callers form the offset t
+// with one fmaf (q * 2^d - (n + 1/2), or (x + 1/2) - p * 2^D): the product is
+// exact, so t carries a single rounding, and the evaluation needs no shifted
+// polynomial whose single-precision coefficients grow as 4^d.
+__host__ __device__ __forceinline__ float bspline_unit(float t) {
+    t = fabsf(t);
+    if (t < 0.5f) return (0.75f - t * t) * (4.0f / 3.0f);
+    if (t < 1.5f) {
+        const float u = 1.5f - t;
+        return u * u * (2.0f / 3.0f);
+    }
+    return 0.f;
+}
+// basis function n of depth d at coordinate q in [0, 1]
+__device__ __forceinline__ float basis_stable(int d, int n, float q) {
+    return bspline_unit(fmaf(q, (float)(1 << d), -((float)n + 0.5f)));
+}
+
 // ConfirmedPPolynomial::shift (ConfirmedPPolynomial.cuh:37-50)
 template <int DEG>
 __device__ __forceinline__ void cpoly_shift(const CPoly& p, float t, CPoly& r) {

@@ -117,6 +117,7 @@ struct Ctx {
     std::vector<double> cg_true_rel; // final relative residual of the CG recurrence per depth (FP64 reductions)
     std::vector<double> cg_fp64_rel; // params.refine: |b - Ax| / |b| recomputed in FP64 (-1: not computed)
     std::vector<int> cg_refines;     // params.refine: restarts on the recomputed residual
+    int solver_blocks = 0;           // co-resident blocks of the last persistent solve
 
     // learned preconditioner weights (prgpu_load_preconditioner), owned by the context
     float* lp_params = nullptr;      // fp32 parameter vector

@@ -47,7 +47,8 @@ struct FcgState {           // one per depth
     double rr;              // final r.r
     double bb;              // b.b
     int status;
-    int pad;
+    int refines;            // restarts on the FP64 true residual (params.refine)
+    double rr_true;         // |b - Ax|^2 with FP64 accumulation (-1: not computed)
 };
 
 constexpr int FCG_NV = 3;
@@ -87,9 +88,11 @@ struct FcgArgs {
     MlpWeights wt;
     const float* cnorm;     // 27 per depth: L_d[j] / L_d[13]
     const float* centre;    // per depth: L_d[13]
+    int refine;             // relative mode: FP64 true-residual check and refinement
 };
 
 constexpr int FCG_TILE_GROUPS = CG_BLOCK / 8;
+constexpr i64 FCG_MIN_ROWS = 256;
 constexpr int FCG_WARP_TILES = 2;
 constexpr int FCG_DSMEM = 16384 + 8192 + 8192 + 1024;   // feature tile, W1, W2 (+ alignment)
 
@@ -232,7 +235,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
     const double bb = v[0];
     float* rcur = a.ra;
     float* rnext = a.rb;
-    bool plain = (d == 0);
+    // depths of fewer than FCG_MIN_ROWS rows (tiny systems plain CG solves in a few
+    // iterations) and depth 0 run plain CG
+    bool plain = (d == 0) || (n < FCG_MIN_ROWS);
     int fallback_at = -1;
     const i64 gfirst = (lo - 1) >> 3, ng = n >> 3;
 
@@ -260,6 +265,18 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
             uint8_t* spr = reinterpret_cast<uint8_t*>(sp + 16 * 64);        // their presence, one byte each
             const i64 ntile = (n + 127) / 128;
             for (i64 tile = rank; tile < ntile; tile += dp.nblocks) {
+                // the row's own vectors, loaded before the staging gathers so that both are in flight
+                const bool own = threadIdx.x < 128 && tile * 128 + threadIdx.x < n;
+                const i64 iown = lo + tile * 128 + threadIdx.x;
+                float own_r = 0.f, own_q = 0.f, own_x = 0.f, own_p = 0.f;
+                if (own) {
+                    own_r = rcur[iown];
+                    if (!init) {
+                        own_q = a.q[iown];
+                        own_x = a.x[iown];
+                        own_p = pnew[iown];
+                    }
+                }
                 for (int e = threadIdx.x; e < 16 * 64; e += blockDim.x) {
                     const int gl = e >> 6, cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
                     const i64 G = tile * 16 + gl;
@@ -319,13 +336,13 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
                     mma_ok = false;
                     break;
                 }
-                if (threadIdx.x < 128 && tile * 128 + threadIdx.x < n) {
-                    const i64 i = lo + tile * 128 + threadIdx.x;
-                    const float rc = rcur[i];
+                if (own) {
+                    const i64 i = iown;
+                    const float rc = own_r;
                     float rn = rc;
                     if (!init) {
-                        a.x[i] = fmaf(al, pnew[i], a.x[i]);
-                        rn = fmaf(nal, a.q[i], rc);
+                        a.x[i] = fmaf(al, own_p, own_x);
+                        rn = fmaf(nal, own_q, rc);
                         rnext[i] = rn;
                     }
                     const float s = ss[threadIdx.x];
@@ -360,9 +377,37 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
     float beta = 0.f;
     const float* pold = a.p2;
     float* pnew = a.p;
+    int refines = 0;
+    double rr_true = -1.0;
     while (ok) {
         const bool go = (a.mode == PRGPU_SOLVE_REFERENCE) ? ((float)rr_prev > a.tol2) : (rr_prev > a.rel2 * bb);
-        if (!go || k > a.max_iter) break;
+        if (!go || k > a.max_iter) {
+            if (!a.refine || a.mode != PRGPU_SOLVE_RELATIVE || k > a.max_iter) break;
+            // the recurrence says converged: r = b - A x with FP64 accumulation
+            double tsum = 0.0;
+            for (i64 t = start; t < n; t += stride) {
+                const i64 i = lo + t;
+                double acc = (double)a.b[i];
+#pragma unroll
+                for (int j = 0; j < 27; ++j) {
+                    const int nb = a.neigh[(i64)j * a.M + i];
+                    if (nb != -1) acc = fma(-(double)sst[j], (double)a.x[nb], acc);
+                }
+                rcur[i] = (float)acc;
+                tsum = fma(acc, acc, tsum);
+            }
+            v[0] = tsum;
+            v[1] = v[2] = 0.0;
+            if (!(ok = reduce(v))) break;
+            rr_true = v[0];
+            if (rr_true <= a.rel2 * bb || refines >= 2) break;
+            // restart from the current x on the true residual, as plain CG
+            ++refines;
+            plain = true;
+            restart = true;
+            rz_prev = rr_prev = rr_true;
+            continue;
+        }
         const float* zsrc = plain ? rcur : a.z;
         auto pdir = [&](i64 i) -> float { return restart ? zsrc[i] : fmaf(beta, pold[i], zsrc[i]); };
         // phase A: p = z + beta p_old where it is read, q = A p, partial p.q
@@ -477,6 +522,8 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
         a.state[d].fallback_at = fallback_at;
         a.state[d].rr = rr_prev;
         a.state[d].bb = bb;
+        a.state[d].rr_true = rr_true;
+        a.state[d].refines = refines;
         a.state[d].status = ok ? 0 : PRGPU_ERR_TIMEOUT;
     }
     // every MMA was waited for, except after a wait that gave up: wait (bounded) for it
@@ -514,16 +561,17 @@ void stage_solve_learned(Ctx& c) {
     float* dcentre = dalloc<float>(D + 1, s);
     CK(cudaMemcpyAsync(dcn, cn.data(), cn.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(dcentre, centre.data(), centre.size() * 4, cudaMemcpyHostToDevice, s));
-    static bool attr = false;
-    if (!attr) {
-        CK(cudaFuncSetAttribute(k_fcg_all, cudaFuncAttributeMaxDynamicSharedMemorySize, FCG_DSMEM));
-        attr = true;
-    }
+    // the largest shared-memory carveout, so that the three blocks per SM that the
+    // registers allow also fit the shared memory (and the occupancy query says so)
+    CK(cudaFuncSetAttribute(k_fcg_all, cudaFuncAttributeMaxDynamicSharedMemorySize, FCG_DSMEM));
+    CK(cudaFuncSetAttribute(k_fcg_all, cudaFuncAttributePreferredSharedMemoryCarveout,
+                            (int)cudaSharedmemCarveoutMaxShared));
     int sms = 0, per_sm = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fcg_all, CG_BLOCK, FCG_DSMEM));
     // each block holds 128 TMEM columns: at most 4 blocks per SM fit the SM's 512
     per_sm = std::max(1, std::min(per_sm, 4));
+    c.solver_blocks = sms * per_sm;
     std::vector<CgDepth> deps;
     std::vector<int> block_depth;
     partition_depths(c, 0, D, sms * per_sm, deps, block_depth);
@@ -569,6 +617,7 @@ void stage_solve_learned(Ctx& c) {
     a.wt.p = c.lp_params;
     a.cnorm = dcn;
     a.centre = dcentre;
+    a.refine = c.params.refine;
     void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
     const int kt = c.kbegin("fcg", 0.0);
     CK(cudaLaunchCooperativeKernel((void*)k_fcg_all, dim3((unsigned)nblk), dim3(CG_BLOCK), kargs, FCG_DSMEM, s));
@@ -583,12 +632,16 @@ void stage_solve_learned(Ctx& c) {
     c.cg_rr.assign(D + 1, 0.f);
     c.cg_fallback.assign(D + 1, -1);
     c.cg_true_rel.assign(D + 1, 0.0);
+    c.cg_fp64_rel.assign(D + 1, -1.0);
+    c.cg_refines.assign(D + 1, 0);
     double bytes = 0;
     for (int d = 0; d <= D; ++d) {
         c.cg_iters[d] = hs[d].iters;
         c.cg_rr[d] = (float)hs[d].rr;
         c.cg_fallback[d] = hs[d].fallback_at;
         c.cg_true_rel[d] = hs[d].bb > 0 ? std::sqrt(hs[d].rr / hs[d].bb) : 0.0;
+        c.cg_fp64_rel[d] = (hs[d].rr_true >= 0 && hs[d].bb > 0) ? std::sqrt(hs[d].rr_true / hs[d].bb) : -1.0;
+        c.cg_refines[d] = hs[d].refines;
         // per row and iteration: the group table twice (product and preconditioner
         // staging), z or r, the previous p, p and q written; r and q staged, x read and
         // written, p read, r' and z written

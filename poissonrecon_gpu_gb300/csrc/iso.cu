@@ -85,6 +85,7 @@ struct EvalArgs {
     const float* x27;      // nodes [0, nx27): x of the 27 neighbours (0: none), 28 floats per node; or null
     i64 nx27;
     const float* lb;       // basis values at finest-lattice points (see lattice_basis), or null
+    int stable;            // params.stable_basis: closed-form basis values (basis_stable)
 };
 
 // start of depth d in the lattice basis table: sum_{l<d} 2^l (3 2^(D-l) + 1) = 3 d 2^D + 2^d - 1
@@ -99,10 +100,11 @@ __device__ __forceinline__ float lattice_basis(const EvalArgs& a, int d, int n, 
     const int w = 1 << (a.D - d);
     const int k = u - (n - 1) * w;
     if (a.lb && k >= 0 && k <= 3 * w) return a.lb[lattice_basis_offset(a.D, d) + (i64)n * (3 * w + 1) + k];
+    if (a.stable) return basis_stable(d, n, (float)u * (1.0f / (float)(1 << a.D)));
     return cpoly_value<3>(a.basis[(1 << d) - 1 + n], (float)u * (1.0f / (float)(1 << a.D)));
 }
 
-__global__ void k_lattice_basis(const CPoly* __restrict__ basis, int D, i64 total, float* __restrict__ lb) {
+__global__ void k_lattice_basis(const CPoly* __restrict__ basis, int D, i64 total, float* __restrict__ lb, int stable) {
     const float inv = 1.0f / (float)(1 << D);
     for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
         // depth d holds 2^d functions of 3w+1 points: offset sum_{l<d} 2^l (3 2^(D-l) + 1)
@@ -117,7 +119,8 @@ __global__ void k_lattice_basis(const CPoly* __restrict__ basis, int D, i64 tota
         const int w = 1 << (D - d);
         const i64 r = e - off;
         const int n = (int)(r / (3 * w + 1)), k = (int)(r % (3 * w + 1));
-        lb[e] = cpoly_value<3>(basis[(1 << d) - 1 + n], (float)((n - 1) * w + k) * inv);
+        const float q = (float)((n - 1) * w + k) * inv;
+        lb[e] = stable ? basis_stable(d, n, q) : cpoly_value<3>(basis[(1 << d) - 1 + n], q);
     }
 }
 
@@ -149,7 +152,9 @@ __device__ __forceinline__ float level_sum(const EvalArgs& a, i64 node, int d, c
 #pragma unroll
         for (int t = 0; t < 3; ++t) {
             int c = xyz[ax] + t - 1;
-            bv[ax][t] = (c >= 0 && c < lim) ? cpoly_value<3>(a.basis[fb + c], q[ax]) : 0.f;
+            bv[ax][t] = (c >= 0 && c < lim)
+                            ? (a.stable ? basis_stable(d, c, q[ax]) : cpoly_value<3>(a.basis[fb + c], q[ax]))
+                            : 0.f;
         }
     if (node < a.nx27) {
         // absent neighbours read 0: adding a zero product leaves the sum unchanged
@@ -261,7 +266,7 @@ void stage_points(Ctx& c) {
     double* sum = dalloc<double>(1, s);
     CK(cudaMemsetAsync(sum, 0, sizeof(double), s));
     float* x27 = build_x27(c, c.base[c.D]);
-    EvalArgs a{c.nodes, c.D, c.basis, c.x, x27, x27 ? c.base[c.D] : 0, nullptr};
+    EvalArgs a{c.nodes, c.D, c.basis, c.x, x27, x27 ? c.base[c.D] : 0, nullptr, c.params.stable_basis};
     const int kt = c.kbegin("point_values", (double)c.N * (12 + 4 + 4) + (double)c.nodes.M * (4 + 4 + 8 + 108));
     k_point_values<<<grid_for(c.N, 128, 1ll << 30), 128, 0, s>>>(a, c.pts, c.point_node, c.N, c.point_weight,
                                                                  c.point_value, sum);
@@ -1825,12 +1830,12 @@ void stage_mesh(Ctx& c) {
     const i64 M = nd.M, lo = c.base[D], nD = c.count[D];
     const int kx = c.kbegin("mesh_tables", 0.0);
     float* x27 = build_x27(c, lo);
-    EvalArgs ea{c.nodes, D, c.basis, c.x, x27, x27 ? lo : 0, nullptr};
+    EvalArgs ea{c.nodes, D, c.basis, c.x, x27, x27 ? lo : 0, nullptr, c.params.stable_basis};
     float* lb = nullptr;
     {
         const i64 total = lattice_basis_offset(D, D + 1);
         lb = dalloc<float>(total, s);
-        k_lattice_basis<<<grid_for(total, 256), 256, 0, s>>>(c.basis, D, total, lb);
+        k_lattice_basis<<<grid_for(total, 256), 256, 0, s>>>(c.basis, D, total, lb, c.params.stable_basis);
         CK_LAUNCH();
         ea.lb = lb;
     }

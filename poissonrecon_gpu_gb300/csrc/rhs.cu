@@ -24,7 +24,7 @@ constexpr int SPLAT_BLOCK = 128;
 __global__ void __launch_bounds__(SPLAT_BLOCK) k_splat(NodeArrays nd, const int* __restrict__ gn, i64 ngroups_all,
                                                        i64 gfirst, i64 ng, i64 lo, int D, CPoly f,
                                                        const float* __restrict__ pts, const float* __restrict__ nrm,
-                                                       float* __restrict__ vfield) {
+                                                       float* __restrict__ vfield, int stable) {
     __shared__ int2 rng[SPLAT_BLOCK / 32][4][64];   // (first point, count) of each block cell
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
@@ -70,13 +70,21 @@ __global__ void __launch_bounds__(SPLAT_BLOCK) k_splat(NodeArrays nd, const int*
             const i64 pt = (i64)cur.x + k;
             ++k;
             const float px = pts[3 * pt], py = pts[3 * pt + 1], pz = pts[3 * pt + 2];
-            CPoly cx, cy, cz;
-            cpoly_shift<2>(f, px, cx);
-            cpoly_shift<2>(f, py, cy);
-            cpoly_shift<2>(f, pz, cz);
-            const float wx = cpoly_value<2>(cx, oc0);
-            const float wy = cpoly_value<2>(cy, oc1);
-            const float wz = cpoly_value<2>(cz, oc2);
+            float wx, wy, wz;
+            if (stable) {   // F/F(0) at (centre - p) 2^D = (xyz + 1/2) - p 2^D, one rounding
+                const float sD = (float)(1 << D);
+                wx = bspline_unit(fmaf(-px, sD, (float)xyz[0] + 0.5f));
+                wy = bspline_unit(fmaf(-py, sD, (float)xyz[1] + 0.5f));
+                wz = bspline_unit(fmaf(-pz, sD, (float)xyz[2] + 0.5f));
+            } else {
+                CPoly cx, cy, cz;
+                cpoly_shift<2>(f, px, cx);
+                cpoly_shift<2>(f, py, cy);
+                cpoly_shift<2>(f, pz, cz);
+                wx = cpoly_value<2>(cx, oc0);
+                wy = cpoly_value<2>(cy, oc1);
+                wz = cpoly_value<2>(cz, oc2);
+            }
             const float wgt = wx * wy * wz;
             v0 = fmaf(wgt, nrm[3 * pt], v0);
             v1 = fmaf(wgt, nrm[3 * pt + 1], v1);
@@ -597,7 +605,8 @@ void stage_splat(Ctx& c) {
     {
         const i64 ngroups_all = (c.nodes.M - 1) / 8, gfirst = (lo - 1) / 8, ng = (hi - lo) / 8;
         k_splat<<<grid_for(ng * 8, SPLAT_BLOCK, 1ll << 30), SPLAT_BLOCK, 0, s>>>(
-            c.nodes, c.gn, ngroups_all, gfirst, ng, lo, D, c.basis_maxdepth, c.pts, nrm, c.vfield);
+            c.nodes, c.gn, ngroups_all, gfirst, ng, lo, D, c.basis_maxdepth, c.pts, nrm, c.vfield,
+            c.params.stable_basis);
     }
     CK_LAUNCH();
     c.kend(kt);

@@ -609,6 +609,7 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_all, CG_BLOCK, 0));
     if (per_sm < 1) per_sm = 1;
     const int G = sms * per_sm;
+    c.solver_blocks = G;
     std::vector<CgDepth> deps;
     std::vector<int> block_depth;
     partition_depths(c, d0, d1, G, deps, block_depth);

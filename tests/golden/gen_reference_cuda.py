@@ -128,16 +128,21 @@ def main(out):
         wall = time.perf_counter() - t0
         with open(os.path.join(out, "pipeline%d.log" % k), "w") as fh:
             fh.write("returncode %d\n--- stdout\n%s\n--- stderr\n%s\n" % (p.returncode, p.stdout, p.stderr))
-        assert p.returncode == 0, p.stderr[-2000:]
-        runs.append((wall, p.stdout))
+        # the reference's main() writes the mesh and prints its total time as its last act;
+        # the process then dies in host-side teardown (SIGSEGV after main returns), which
+        # is recorded, not treated as a failed run
+        assert "The whole project takes" in p.stdout, p.stderr[-2000:]
+        runs.append((wall, p.stdout, p.returncode))
     stdout = runs[-1][1]
     iso_ref = float(re.search(r"isoValue:([-0-9.eE+]+)", stdout).group(1))
+    iso_runs = [float(re.search(r"isoValue:([-0-9.eE+]+)", r[1]).group(1)) for r in runs]
     summary["reference"] = {
-        "main_wall_s": [float(re.search(r"prgpu_ref_wall_s ([0-9.]+)", r[1]).group(1)) for r in runs],
         "process_wall_s": [r[0] for r in runs],
+        "process_returncode": [r[2] for r in runs],
         "whole_project_s": [float(re.search(r"The whole project takes ([0-9.]+)s", r[1]).group(1)) for r in runs],
         "cg_ms": [float(re.search(r"Pure CG solving process takes:([0-9.]+)ms", r[1]).group(1)) for r in runs],
         "iso_printed": iso_ref,
+        "iso_printed_runs": iso_runs,
         "stage_lines": [ln for ln in stdout.splitlines() if "takes" in ln],
     }
     rv, rf = read_ascii_mesh(os.path.join(work, "bunny.ply"))
@@ -185,13 +190,22 @@ def main(out):
     for fld in FIELDS:
         a = ref[fld]
         b = ours[fld].astype(a.dtype) if fld != "key" else ours[fld].astype(np.int64)
+        if fld == "point_node":   # the reference indexes leaves within the finest depth
+            b = (ours[fld].astype(np.int64) - int(ours["base"][D])).astype(a.dtype)
         assert a.shape == b.shape, (fld, a.shape, b.shape)
         arrays["sha256_" + fld] = np.array(digest(a))
         idx = np.nonzero(a != b)[0]
+        summary["fields"][fld] = {"entries": int(a.size), "differ": int(len(idx))}
+        if fld == "children":
+            # the reference leaves the children of finest-depth nodes uninitialised
+            # (main.cu:466-472): digest with those set to -1, and a sample of the raw values
+            canon = a.copy().reshape(-1, 8)
+            canon[int(ref["base"][D]):] = -1
+            arrays["sha256_children_canonical"] = np.array(digest(canon))
+            idx = idx[:256]
         arrays["diff_%s_idx" % fld] = idx.astype(np.int64)
         arrays["diff_%s_ref" % fld] = a[idx]
         arrays["diff_%s_ours" % fld] = b[idx]
-        summary["fields"][fld] = {"entries": int(a.size), "differ": int(len(idx))}
     np.savez_compressed(os.path.join(out, "ref_cuda_sphere50k_d8.npz"), **arrays)
     with open(os.path.join(out, "ref_cuda_sphere50k_d8.json"), "w") as fh:
         json.dump(summary, fh, indent=1)
