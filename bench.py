@@ -10,6 +10,10 @@ values + iso-value, marching cubes with subdivision, mesh to host.
   value : points/s with the input already resident in HBM (prgpu_set_points_device)
   e2e   : points/s through prgpu_reconstruct with pinned host buffers, host->device
           copy of the points and device->host copy of the mesh inside the timed region
+  solver_study : solve ms to relative residual 1e-6, learned-preconditioned
+          flexible CG against plain CG, on held-out unions of ellipsoids at maxDepth 9
+  reference_cuda_build : the reference's own CUDA program on the 50,000-point sphere at
+          maxDepth 8 (its compile-time depth), beside this library on the same file
 Timing: CUDA events on the library's stream, per step, L2 flushed (256 MiB
 write) between steps; clocks sampled with nvidia-smi during the timed steps.
 
@@ -50,6 +54,8 @@ def parse():
     ap.add_argument("--points", type=int, default=1_000_000)
     ap.add_argument("--depth", type=int, default=10)
     ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--solver-seeds", type=int, default=200, help="held-out shapes of the learned-vs-plain "
+                    "solver study (0: skip)")
     ap.add_argument("--clocks-csv", default=None, help="where to keep the nvidia-smi clock samples "
                     "(default: a temporary directory)")
     ap.add_argument("--shape", default="torus", choices=["torus", "sphere", "displaced_sphere"],
@@ -238,6 +244,111 @@ def file_io_pass(r, xyz, nrm, steps):
         shutil.rmtree(d, ignore_errors=True)
 
 
+CHECKPOINT = os.path.join(REPO, "poissonrecon_gpu_gb300", "weights", "lpc_ellipsoids_d9.bin")
+REF_CUDA = os.path.join(REPO, "oracle", "_ref", "ref_cuda")
+
+
+def solver_study(seeds, device):
+    """Learned-preconditioned flexible CG against plain CG on held-out shapes of the
+    solver-study configuration: unions of 3-8 ellipsoids (20k-200k points), maxDepth 9,
+    every depth solved to relative residual 1e-6 checked on the FP64 true residual
+    (params.refine).  Solve time: the library's CUDA-event timer around the solve stage,
+    median of 3 solves per shape."""
+    import poissonrecon_gpu_gb300 as pg
+    from poissonrecon_gpu_gb300 import shapes
+    if not os.path.exists(CHECKPOINT):
+        return {"unavailable": "no checkpoint at %s" % os.path.relpath(CHECKPOINT, REPO)}
+    kw = dict(depth=9, solve_mode=pg.SOLVE_RELATIVE, cg_tol=1e-6, refine=True, device=device)
+    plain = pg.Reconstructor(**kw)
+    lrn = pg.Reconstructor(preconditioner=CHECKPOINT, **kw)
+    rows = []
+    for k in range(seeds):
+        xyz, nrm = shapes.ellipsoid_union(100000 + k)
+        row = {"points": len(xyz)}
+        for name, r in (("plain", plain), ("learned", lrn)):
+            r.set_points(xyz, nrm)
+            r.build_octree()
+            r.compute_rhs()
+            ts = []
+            for _ in range(3):
+                r.solve()
+                ts.append(r.stats()["ms"]["solve"])
+            st = r.stats()
+            row[name] = {"ms": float(np.median(ts)), "iters": st["cg_iters"], "fallback": st["cg_fallback"],
+                         "fp64": max(st["cg_fp64_residual"])}
+        rows.append(row)
+    plain.close()
+    lrn.close()
+    pm = np.array([r["plain"]["ms"] for r in rows])
+    lm = np.array([r["learned"]["ms"] for r in rows])
+    it_p = np.array([sum(r["plain"]["iters"]) for r in rows])
+    it_l = np.array([sum(r["learned"]["iters"]) for r in rows])
+    return {"workload": "unions of 3-8 ellipsoids, held-out seeds 100000-%d, 20k-200k points, maxDepth 9, relative "
+                        "residual 1e-6 (FP64 true residual)" % (100000 + seeds - 1),
+            "shapes": seeds, "points_mean": float(np.mean([r["points"] for r in rows])),
+            "plain_solve_ms_mean": float(pm.mean()), "learned_solve_ms_mean": float(lm.mean()),
+            "ratio_learned_over_plain": float(lm.mean() / pm.mean()),
+            "iterations_sum_over_depths_mean": {"plain": float(it_p.mean()), "learned": float(it_l.mean())},
+            "depths_falling_back": int(sum(sum(1 for v in r["learned"]["fallback"] if v >= 0) for r in rows)),
+            "max_fp64_residual": {"plain": float(max(r["plain"]["fp64"] for r in rows)),
+                                  "learned": float(max(r["learned"]["fp64"] for r in rows))},
+            "checkpoint": os.path.relpath(CHECKPOINT, REPO)}
+
+
+def reference_cuda_anchor(device, runs=3):
+    """The reference's own CUDA program (built unchanged by oracle/ref_cuda.sh; maxDepth 8
+    fixed by its main.cu:69) on the 50,000-point sphere, timed by its own clock ("The whole
+    project takes", PLY in to ASCII PLY out), beside this library file to file on the same
+    file (binary PLY read, reconstruction with the reference's CG schedule, ASCII PLY write)."""
+    import re
+    import shutil
+    import poissonrecon_gpu_gb300 as pg
+    from poissonrecon_gpu_gb300 import shapes
+    if not os.path.exists(REF_CUDA):
+        return {"unavailable": "the reference's CUDA program is not built here (oracle/ref_cuda.sh)"}
+    work = tempfile.mkdtemp(prefix="prgpu_refcuda_")
+    try:
+        xyz, nrm = shapes.sphere(50000, seed=0)
+        src = os.path.join(work, "bunny.points.ply")   # the file name the reference's main() opens
+        with open(src, "wb") as fh:
+            fh.write(b"ply\nformat binary_little_endian 1.0\nelement vertex %d\n" % len(xyz))
+            for k in ("x", "y", "z", "nx", "ny", "nz"):
+                fh.write(b"property float %s\n" % k.encode())
+            fh.write(b"end_header\n")
+            fh.write(np.concatenate([xyz, nrm], 1).astype("<f4").tobytes())
+        ref_s, ref_stage = [], {}
+        for _ in range(runs):
+            p = subprocess.run([REF_CUDA, "pipeline"], env=dict(os.environ, PRGPU_REF_IO_DIR=work),
+                               capture_output=True, text=True, timeout=300)
+            m = re.search(r"The whole project takes ([0-9.]+)s", p.stdout)
+            if not m:
+                return {"unavailable": "the reference's program did not finish: %s" % p.stderr[-200:]}
+            ref_s.append(float(m.group(1)))
+            for ln in p.stdout.splitlines():
+                mm = re.match(r"(.*?) takes:? ?([0-9.]+)(ms|s)", ln.strip())
+                if mm:
+                    ref_stage[mm.group(1)] = float(mm.group(2)) * (1e-3 if mm.group(3) == "ms" else 1.0)
+        r = pg.Reconstructor(depth=8, device=device)
+        out_ply = os.path.join(work, "ours.ply")
+        ours = []
+        for _ in range(max(runs, 3)):
+            t0 = time.perf_counter()
+            px, pn = pg.read_points(src)
+            v, f = r.reconstruct(px, pn)
+            pg.write_mesh(out_ply, v, f, binary=False)
+            ours.append(time.perf_counter() - t0)
+        r.close()
+        t_ref, t_ours = float(np.median(ref_s)), float(np.median(ours))
+        return {"workload": "sphere 50000 points, maxDepth 8, reference CG schedule, PLY in to ASCII PLY out",
+                "reference_s": t_ref, "reference_runs_s": ref_s, "reference_stages_s": ref_stage,
+                "ours_s": t_ours, "ours_points_per_s": len(xyz) / t_ours, "reference_points_per_s": len(xyz) / t_ref,
+                "speedup": t_ref / t_ours,
+                "note": "the reference's own clock, which starts after CUDA initialisation; its process then "
+                        "crashes in host-side teardown after printing it"}
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
 def max_over_ranks(values, device):
     """Replicas: every rank times its own reconstruction; the job's time is the slowest rank's."""
     import torch
@@ -380,6 +491,9 @@ def main():
     }
     if world == 1:
         out["file_e2e"] = file_io_pass(r, xyz, nrm, max(args.steps, 3))
+        if args.solver_seeds > 0:
+            out["solver_study"] = solver_study(args.solver_seeds, local)
+        out["reference_cuda_build"] = reference_cuda_anchor(local)
     if os.environ.get("PRGPU_BENCH_NO_CPU") != "1":
         cpu, _ = cpu_reference(args, 1, 0)
         out["cpu_baseline"] = cpu

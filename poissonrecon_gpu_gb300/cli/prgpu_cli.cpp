@@ -1,6 +1,7 @@
 // prgpu: command-line front end of the library.
 //   prgpu --in points.ply --out mesh.ply [--depth 8] [--binary] [--relative TOL]
-//         [--maxIter N] [--device K] [--weld] [--density] [--cascadic] [--stats]
+//         [--maxIter N] [--device K] [--weld] [--density] [--cascadic] [--refine]
+//         [--stable-basis] [--learned CHECKPOINT] [--stats]
 // The reference takes its input/output paths and maxDepth at compile time
 // (main.cu:69,3251-3252); the flag names follow the Kazhdan-style "--name value"
 // convention of its CmdLineParser (CmdLineParser.cu:205-240).
@@ -15,7 +16,8 @@
 static void usage() {
     fprintf(stderr,
             "usage: prgpu --in <points.ply|.bnpts|ascii> --out <mesh.ply> [--depth D] [--binary]\n"
-            "             [--relative TOL] [--maxIter N] [--device K] [--weld] [--density] [--cascadic] [--stats]\n");
+            "             [--relative TOL] [--maxIter N] [--device K] [--weld] [--density] [--cascadic]\n"
+            "             [--refine] [--stable-basis] [--learned CHECKPOINT] [--stats]\n");
 }
 
 int main(int argc, char** argv) {
@@ -24,6 +26,7 @@ int main(int argc, char** argv) {
     prgpu_params p;
     prgpu_params_default(&p);
     int binary = 0, stats = 0;
+    const char* learned = nullptr;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
         auto next = [&]() -> const char* {
@@ -40,6 +43,9 @@ int main(int argc, char** argv) {
         else if (a == "--relative") { p.solve_mode = PRGPU_SOLVE_RELATIVE; p.cg_tol = atof(next()); }
         else if (a == "--maxIter") p.cg_max_iter = atoi(next());
         else if (a == "--device") p.device = atoi(next());
+        else if (a == "--refine") p.refine = 1;
+        else if (a == "--stable-basis") p.stable_basis = 1;
+        else if (a == "--learned") { learned = next(); p.learned = 1; }
         else if (a == "--stats") stats = 1;
         else { usage(); return 2; }
     }
@@ -51,6 +57,11 @@ int main(int argc, char** argv) {
     if (rc) { fprintf(stderr, "read failed (%d): %s\n", rc, prgpu_last_error()); return 1; }
     void* ctx = nullptr;
     if ((rc = prgpu_create(&p, &ctx))) { fprintf(stderr, "create failed (%d): %s\n", rc, prgpu_last_error()); return 1; }
+    if (learned && (rc = prgpu_load_preconditioner(ctx, learned))) {
+        fprintf(stderr, "preconditioner failed (%d): %s\n", rc, prgpu_last_error());
+        prgpu_destroy(ctx);
+        return 1;
+    }
     prgpu_mesh m;
     rc = prgpu_reconstruct(ctx, xyz, nrm, n, &m);
     if (rc) { fprintf(stderr, "reconstruction failed (%d): %s\n", rc, prgpu_last_error()); prgpu_destroy(ctx); return 1; }

@@ -91,16 +91,24 @@ struct FcgArgs {
     int refine;             // relative mode: FP64 true-residual check and refinement
 };
 
-constexpr int FCG_TILE_GROUPS = CG_BLOCK / 8;
-constexpr i64 FCG_MIN_ROWS = 256;
+// A kernel that allocates tensor memory runs one block per SM (the occupancy the
+// driver grants such kernels), so the block is large: 768 threads, all of which
+// share the gathers, the matrix-vector product and the reductions; for the
+// preconditioner they form three groups of 256 threads, each with its own MLP
+// tile stream, TMEM columns (128 of the block's 512), mbarrier and named barrier.
+constexpr int FCG_GROUPS = 3;
+constexpr int FCG_THREADS = 256 * FCG_GROUPS;
+constexpr int FCG_WARPS = FCG_THREADS / 32;
 constexpr int FCG_WARP_TILES = 2;
-constexpr int FCG_DSMEM = 16384 + 8192 + 8192 + 1024;   // feature tile, W1, W2 (+ alignment)
+constexpr i64 FCG_MIN_ROWS = 256;
+constexpr int FCG_DSMEM = 8192 + 8192 + FCG_GROUPS * 16384 + 1024;   // W1, W2, feature tiles (+ alignment)
 
 // sum of FCG_NV doubles over the blocks of a partition, in a fixed order, returned
 // to every thread; false when a wait gave up (error flag set)
 __device__ bool fcg_reduce(FcgSync* ps, double* partial, int first_block, int nblocks, int slot,
                            double (&v)[FCG_NV], const FcgArgs& a, double* sh, int* sh_flag, double* sh_val) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
 #pragma unroll
     for (int j = 0; j < FCG_NV; ++j) {
         double t = v[j];
@@ -111,7 +119,7 @@ __device__ bool fcg_reduce(FcgSync* ps, double* partial, int first_block, int nb
     if (threadIdx.x == 0) {
         for (int j = 0; j < FCG_NV; ++j) {
             double s = 0.0;
-            for (int k = 0; k < CG_BLOCK / 32; ++k) s += sh[k * FCG_NV + j];
+            for (int k = 0; k < nw; ++k) s += sh[k * FCG_NV + j];
             partial[(i64)blockIdx.x * 4 + j] = s;
         }
         __threadfence();
@@ -136,7 +144,7 @@ __device__ bool fcg_reduce(FcgSync* ps, double* partial, int first_block, int nb
         if (threadIdx.x == 0) {
             for (int j = 0; j < FCG_NV; ++j) {
                 double s = 0.0;
-                for (int k = 0; k < CG_BLOCK / 32; ++k) s += sh[k * FCG_NV + j];
+                for (int k = 0; k < nw; ++k) s += sh[k * FCG_NV + j];
                 ps->res[slot][j] = s;
                 sh_val[j] = s;
             }
@@ -165,47 +173,50 @@ __device__ bool fcg_reduce(FcgSync* ps, double* partial, int first_block, int nb
     return sh_flag[2] != 0;
 }
 
-__global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDepth* __restrict__ deps,
-                                                      const int* __restrict__ block_depth) {
+__global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgDepth* __restrict__ deps,
+                                                          const int* __restrict__ block_depth) {
     extern __shared__ __align__(1024) uint8_t dsm[];
-    uint8_t* sx = dsm;
-    uint8_t* sw1 = dsm + 16384;
-    uint8_t* sw2 = sw1 + 8192;
-    __shared__ float sp[FCG_TILE_GROUPS * 64 * FCG_WARP_TILES];   // product staging; r' blocks in phase B
+    uint8_t* sw1 = dsm;
+    uint8_t* sw2 = dsm + 8192;
+    __shared__ float sp[FCG_WARPS * FCG_WARP_TILES * 4 * 64];   // product staging; r' blocks per group in phase B
     __shared__ float sst[27];
     __shared__ float scn[27];
     __shared__ float sb[192];
-    __shared__ float red[CG_BLOCK];
-    __shared__ float ss[128];
-    __shared__ double sh[(CG_BLOCK / 32) * FCG_NV];
+    __shared__ float red[FCG_GROUPS][256];
+    __shared__ float ss[FCG_GROUPS][128];
+    __shared__ double sh[FCG_WARPS * FCG_NV];
     __shared__ double sh_val[FCG_NV];
     __shared__ int sh_flag[3];
-    __shared__ uint64_t bar;
+    __shared__ int gflag[FCG_GROUPS];
+    __shared__ uint64_t bars[FCG_GROUPS];
     __shared__ uint32_t tslot;
     const int d = block_depth[blockIdx.x];
     const CgDepth& dp = deps[d];
+    const int grp = threadIdx.x >> 8, lt = threadIdx.x & 255, gbar = 1 + grp;
     if (threadIdx.x < 32) {
-        tmem_alloc(&tslot, 128);
+        tmem_alloc(&tslot, 512);
         tmem_relinquish();
     }
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        mbar_fence_init();
+    if (threadIdx.x < FCG_GROUPS) {
+        mbar_init(&bars[threadIdx.x], 1);
+        gflag[threadIdx.x] = 0;
     }
+    if (threadIdx.x == 0) mbar_fence_init();
     if (threadIdx.x < 27) {
         sst[threadIdx.x] = dp.st[threadIdx.x];
         scn[threadIdx.x] = a.cnorm[27 * d + threadIdx.x];
     }
     MlpSmem m;
     stage_mlp_smem(a.wt, sw1, sw2, sb, m);
+    uint8_t* sx = dsm + 16384 + grp * 16384;   // this group's feature / activation tile
     const float cls[4] = {dp.cls[0], dp.cls[1], dp.cls[2], dp.cls[3]};
     const float icen = 1.f / a.centre[d];
     const float dfeat = (float)d * (1.f / 16.f);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tbase = tslot;
-    MmaSync ms{&bar, 0};
+    const uint32_t tbase = tslot + (uint32_t)(grp * 128);
+    uint32_t phase = 0;
     FcgSync* psync = &a.sync[d];
     const int rank = blockIdx.x - dp.first_block;
     const i64 stride = (i64)dp.nblocks * blockDim.x;
@@ -245,6 +256,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
     auto phase_b = [&](bool init, float al, const float* pnew) -> bool {
         const float nal = -al;
         double acc[FCG_NV] = {0.0, 0.0, 0.0};
+        bool gok = true;
         if (plain) {
             FSum s0;
             for (i64 t = start; t < n; t += stride) {
@@ -261,13 +273,13 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
             acc[0] = s0.value();
             acc[1] = acc[0];
         } else {
-            float* sv = sp;                                                 // 16 groups x 64 cells
-            uint8_t* spr = reinterpret_cast<uint8_t*>(sp + 16 * 64);        // their presence, one byte each
+            float* sv = sp + grp * 2048;                                     // 16 groups x 64 cells
+            uint8_t* spr = reinterpret_cast<uint8_t*>(sv + 16 * 64);         // their presence, one byte each
             const i64 ntile = (n + 127) / 128;
-            for (i64 tile = rank; tile < ntile; tile += dp.nblocks) {
+            for (i64 tile = (i64)rank * FCG_GROUPS + grp; tile < ntile; tile += (i64)dp.nblocks * FCG_GROUPS) {
                 // the row's own vectors, loaded before the staging gathers so that both are in flight
-                const bool own = threadIdx.x < 128 && tile * 128 + threadIdx.x < n;
-                const i64 iown = lo + tile * 128 + threadIdx.x;
+                const bool own = lt < 128 && tile * 128 + lt < n;
+                const i64 iown = lo + tile * 128 + lt;
                 float own_r = 0.f, own_q = 0.f, own_x = 0.f, own_p = 0.f;
                 if (own) {
                     own_r = rcur[iown];
@@ -277,7 +289,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
                         own_p = pnew[iown];
                     }
                 }
-                for (int e = threadIdx.x; e < 16 * 64; e += blockDim.x) {
+                for (int e = lt; e < 16 * 64; e += 256) {
                     const int gl = e >> 6, cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
                     const i64 G = tile * 16 + gl;
                     const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
@@ -290,9 +302,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
                     sv[e] = val;
                     spr[e] = (cn != -1) ? 1 : 0;
                 }
-                __syncthreads();
+                group_sync(gbar);
                 {
-                    const int row = threadIdx.x >> 1, h = threadIdx.x & 1;
+                    const int row = lt >> 1, h = lt & 1;
                     const int gl = row >> 3, ch = row & 7;
                     const int cx = (ch >> 2) & 1, cy = (ch >> 1) & 1, cz = ch & 1;
                     const bool valid = tile * 128 + row < n;
@@ -311,7 +323,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
 #pragma unroll
                         for (int j = 0; j < 5; ++j)   // features 27..31: coefficients of neighbours 0..4
                             f[27 + j] = spr[gl * 64 + (cx + j / 9) * 16 + (cy + (j / 3) % 3) * 4 + (cz + j % 3)] ? scn[j] : 0.f;
-                        ss[row] = valid ? s : 0.f;
+                        ss[grp][row] = valid ? s : 0.f;
                     } else {
 #pragma unroll
                         for (int u = 0; u < 22; ++u) {   // features 32..53: coefficients of neighbours 5..26
@@ -332,33 +344,36 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
                     }
                 }
                 float y = 0.f;
-                if (!mlp_forward_tile(sx, m, tbase, ms, red, y)) {
-                    mma_ok = false;
+                if (!mlp_forward_tile_group(sx, m, tbase, &bars[grp], phase, red[grp], y, lt, gbar, &gflag[grp])) {
+                    gok = false;
                     break;
                 }
                 if (own) {
-                    const i64 i = iown;
                     const float rc = own_r;
                     float rn = rc;
                     if (!init) {
-                        a.x[i] = fmaf(al, own_p, own_x);
+                        a.x[iown] = fmaf(al, own_p, own_x);
                         rn = fmaf(nal, own_q, rc);
-                        rnext[i] = rn;
+                        rnext[iown] = rn;
                     }
-                    const float s = ss[threadIdx.x];
+                    const float s = ss[grp][lt];
                     const float zi = s > 0.f ? s * y * icen : 0.f;
-                    a.z[i] = zi;
+                    a.z[iown] = zi;
                     acc[0] += (double)rn * (double)rn;
                     acc[1] += (double)zi * (double)rn;
                     acc[2] += (double)zi * (double)rc;
                 }
-                __syncthreads();
+                group_sync(gbar);
             }
         }
-        if (!mma_ok && threadIdx.x == 0) atomicExch(a.err, PRGPU_ERR_TIMEOUT);
+        if (!gok) {
+            mma_ok = false;
+            if (lt == 0) atomicExch(a.err, PRGPU_ERR_TIMEOUT);
+        }
 #pragma unroll
         for (int j = 0; j < FCG_NV; ++j) v[j] = acc[j];
-        return reduce(v) && mma_ok;
+        const bool r = reduce(v);
+        return r && !*(volatile int*)a.err;
     };
 
     double rz_prev = bb, rr_prev = bb;
@@ -431,8 +446,8 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
             const int ch = lane & 7, gl = lane >> 3;
             const int sx_ = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
             float* wsp = sp + wib * (FCG_WARP_TILES * 4 * 64);
-            const i64 wstride = (i64)dp.nblocks * (CG_BLOCK / 32) * FCG_WARP_TILES;
-            for (i64 tile = ((i64)rank * (CG_BLOCK / 32) + wib) * FCG_WARP_TILES; tile * 4 < ng; tile += wstride) {
+            const i64 wstride = (i64)dp.nblocks * FCG_WARPS * FCG_WARP_TILES;
+            for (i64 tile = ((i64)rank * FCG_WARPS + wib) * FCG_WARP_TILES; tile * 4 < ng; tile += wstride) {
                 __syncwarp();
                 int cn[FCG_WARP_TILES * 8];
 #pragma unroll
@@ -527,11 +542,11 @@ __global__ void __launch_bounds__(CG_BLOCK, 3) k_fcg_all(FcgArgs a, const CgDept
         a.state[d].status = ok ? 0 : PRGPU_ERR_TIMEOUT;
     }
     // every MMA was waited for, except after a wait that gave up: wait (bounded) for it
-    if (!mma_ok) mbar_wait(&bar, ms.phase, 1ll << 22);
+    if (!mma_ok && lt == 0 && gflag[grp]) mbar_wait(&bars[grp], phase ^ 1u, MBAR_LIMIT);   // the wait that gave up
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (threadIdx.x < 32) tmem_dealloc(tbase, 128);
+    if (threadIdx.x < 32) tmem_dealloc(tslot, 512);
 }
 
 void stage_solve_learned(Ctx& c) {
@@ -561,16 +576,19 @@ void stage_solve_learned(Ctx& c) {
     float* dcentre = dalloc<float>(D + 1, s);
     CK(cudaMemcpyAsync(dcn, cn.data(), cn.size() * 4, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(dcentre, centre.data(), centre.size() * 4, cudaMemcpyHostToDevice, s));
-    // the largest shared-memory carveout, so that the three blocks per SM that the
-    // registers allow also fit the shared memory (and the occupancy query says so)
+    // the largest shared-memory carveout: the block holds about 120 KB
     CK(cudaFuncSetAttribute(k_fcg_all, cudaFuncAttributeMaxDynamicSharedMemorySize, FCG_DSMEM));
     CK(cudaFuncSetAttribute(k_fcg_all, cudaFuncAttributePreferredSharedMemoryCarveout,
                             (int)cudaSharedmemCarveoutMaxShared));
     int sms = 0, per_sm = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fcg_all, CG_BLOCK, FCG_DSMEM));
-    // each block holds 128 TMEM columns: at most 4 blocks per SM fit the SM's 512
-    per_sm = std::max(1, std::min(per_sm, 4));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fcg_all, FCG_THREADS, FCG_DSMEM));
+    if (per_sm < 1) {
+        set_last_error("the flexible CG kernel cannot be resident on an SM");
+        throw Error{PRGPU_ERR_LIMIT, {0}};
+    }
+    // the block allocates all 512 TMEM columns of its SM: one block per SM
+    per_sm = 1;
     c.solver_blocks = sms * per_sm;
     std::vector<CgDepth> deps;
     std::vector<int> block_depth;
@@ -620,7 +638,7 @@ void stage_solve_learned(Ctx& c) {
     a.refine = c.params.refine;
     void* kargs[] = {(void*)&a, (void*)&ddeps, (void*)&dbd};
     const int kt = c.kbegin("fcg", 0.0);
-    CK(cudaLaunchCooperativeKernel((void*)k_fcg_all, dim3((unsigned)nblk), dim3(CG_BLOCK), kargs, FCG_DSMEM, s));
+    CK(cudaLaunchCooperativeKernel((void*)k_fcg_all, dim3((unsigned)nblk), dim3(FCG_THREADS), kargs, FCG_DSMEM, s));
     ++g_kernel_launches;
     c.kend(kt);
     std::vector<FcgState> hs(D + 1);

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_forward(MlpWeights wt, const __n
     if (!ok && threadIdx.x == 0) atomicExch(err, PRGPU_ERR_TIMEOUT);
     // every MMA this CTA issued has been waited for (or the CTA gave up above after
     // a bounded wait; wait once more for the last commit before releasing TMEM)
-    if (!ok) mbar_wait(&bar, ms.phase, MBAR_LIMIT);
+    if (!ok) mbar_wait(&bar, ms.phase ^ 1u, MBAR_LIMIT);   // the commit whose wait gave up
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train(TrainArgs a) {
     }
     if (!ok) {
         if (threadIdx.x == 0) atomicExch(a.err, PRGPU_ERR_TIMEOUT);
-        mbar_wait(&bar, ms.phase, MBAR_LIMIT);
+        mbar_wait(&bar, ms.phase ^ 1u, MBAR_LIMIT);   // the commit whose wait gave up
     }
     tc_fence_after();
     if (threadIdx.x < 32) tmem_dealloc(tb, 512);

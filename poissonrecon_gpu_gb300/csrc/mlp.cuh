@@ -116,6 +116,67 @@ __device__ __forceinline__ bool mlp_forward_tile(uint8_t* sx, const MlpSmem& m, 
 // ---------------------------------------------------------------------------
 // standalone forward over feature rows (bf16 [n][64]) -> y[n]
 // ---------------------------------------------------------------------------
+// The same forward pass for one of several 256-thread groups of a larger block
+// (the flexible CG runs three): lt is the thread's index in its group, bar_id
+// the group's named barrier (1..15), flag a shared word the group sets when an
+// MMA wait gives up.  The group's warps keep the TMEM lane mapping of
+// mlp_forward_tile (warp lt/32 reads lanes 32*((lt/32)&3)..), since groups start
+// at multiples of 8 warps.
+__device__ __forceinline__ void group_sync(int bar_id) {
+    asm volatile("bar.sync %0, 256;" ::"r"(bar_id) : "memory");
+}
+__device__ __forceinline__ bool group_wait(uint64_t* bar, uint32_t& phase, int bar_id, volatile int* flag) {
+    if (!mbar_wait(bar, phase, MBAR_LIMIT)) *flag = 1;
+    phase ^= 1u;
+    group_sync(bar_id);
+    return *flag == 0;
+}
+__device__ __forceinline__ bool mlp_forward_tile_group(uint8_t* sx, const MlpSmem& m, uint32_t tbase, uint64_t* bar,
+                                                       uint32_t& phase, float* red, float& y, int lt, int bar_id,
+                                                       volatile int* flag) {
+    const int w = lt >> 5, lane = lt & 31, q = w & 3, hc = w >> 2;
+    const int row = 32 * q + lane, k0 = 32 * hc;
+    const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16);
+    constexpr uint32_t ID = idesc_bf16_f32(128, 64);
+    fence_async_smem();
+    group_sync(bar_id);
+    if (lt == 0) {
+        tc_fence_after();
+        mma_k64(tbase, sx, 128, m.w1, 64, ID, 0);
+        mma_commit(bar);
+    }
+    if (!group_wait(bar, phase, bar_id, flag)) return false;
+    tc_fence_after();
+    float v[32];
+    tmem_ld32(tl + k0, v);
+#pragma unroll
+    for (int c = 0; c < 32; c += 8) {
+        __align__(16) __nv_bfloat16 hb[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) hb[u] = __float2bfloat16_rn(fmaxf(v[c + u] + m.b1[k0 + c + u], 0.f));
+        *reinterpret_cast<uint4*>(sx + op_offset(128, row, k0 + c)) = *reinterpret_cast<const uint4*>(hb);
+    }
+    tc_fence_before();
+    fence_async_smem();
+    group_sync(bar_id);
+    if (lt == 0) {
+        tc_fence_after();
+        mma_k64(tbase + 64, sx, 128, m.w2, 64, ID, 0);
+        mma_commit(bar);
+    }
+    if (!group_wait(bar, phase, bar_id, flag)) return false;
+    tc_fence_after();
+    tmem_ld32(tl + 64 + k0, v);
+    float part = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) part = fmaf(fmaxf(v[c] + m.b2[k0 + c], 0.f), m.w3[k0 + c], part);
+    red[lt] = part;
+    tc_fence_before();
+    group_sync(bar_id);
+    y = (lt < 128) ? red[lt] + red[lt + 128] + m.b3 : 0.f;
+    return true;
+}
+
 __device__ __forceinline__ void stage_mlp_smem(const MlpWeights& wt, uint8_t* sw1, uint8_t* sw2, float* sb, MlpSmem& m) {
     load_weight_tile(wt.w1, sw1, false);
     load_weight_tile(wt.w2, sw2, false);

@@ -189,7 +189,10 @@ def test_useless_network_falls_back_to_plain_cg(trained, tmp_path):
     v, f = r.reconstruct(xyz, nrm)
     st = r.stats()
     fb = st["cg_fallback"]
-    assert all(k == 0 for k in fb[1:]), fb
+    cnt = r.get("count")
+    # depths of at least 256 rows start with the network and fall back at once; smaller ones
+    # run plain CG throughout (-1)
+    assert all((k == 0) if cnt[d] >= 256 else (k == -1) for d, k in enumerate(fb) if d > 0), fb
     assert np.all(np.array(st["cg_rel_residual"]) <= 1e-6 * 1.0001)
     # plain CG from the start: the same iterations as the plain solver, within reduction order
     assert np.all(np.abs(np.array(st["cg_iters"]) - np.array(plain.stats()["cg_iters"])) <= 1)
