@@ -160,3 +160,21 @@ def test_superquadric_d10_in_a_batch_matches_oracle(lib_built, oracle_mod):
     sv, sf = s.reconstruct(xyz, nrm)
     s.close()
     assert np.array_equal(sv, gv) and np.array_equal(sf, gf)
+
+
+def test_c2_precision_against_fp64_oracle(c2, lib_built, oracle_mod):
+    """The torus at maxDepth 10 against the FP64 oracle run (see test_gpu_precision.py): with the
+    reference's single-precision basis evaluation, and with params.stable_basis."""
+    import os
+    import sys
+    import poissonrecon_gpu_gb300 as pg
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_gpu_precision import _keep, precision_row
+    o, xyz = c2["o"], c2["xyz"]
+    nrm = o._nrm
+    for stable, (imp, iso) in ((False, (0.15, 2e-2)), (True, (1e-3, 1e-5))):
+        row = precision_row(pg, oracle_mod, "torus 1M, maxDepth 10", xyz, nrm, D, o=o, stable=stable)
+        _keep(row)
+        assert row["implicit_rel_err"] <= imp, row
+        assert row["iso_rel_err"] <= iso, row
+        assert all(0 <= r <= 1e-6 * 1.0001 for r in row["fp64_residual_per_depth"]), row
