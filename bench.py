@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--solver-seeds", type=int, default=200, help="held-out shapes of the learned-vs-plain "
                     "solver study (0: skip)")
+    ap.add_argument("--solver-only", action="store_true", help="run only the learned-vs-plain solver study "
+                    "(--solver-seeds shapes) and print it as one JSON line")
     ap.add_argument("--clocks-csv", default=None, help="where to keep the nvidia-smi clock samples "
                     "(default: a temporary directory)")
     ap.add_argument("--shape", default="torus", choices=["torus", "sphere", "displaced_sphere"],
@@ -391,6 +393,11 @@ def main():
                "config": config(args, "n/a (host)"), "impl": "reference", "cpu_baseline": cpu,
                "e2e": {"value": cpu["value"], "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
+        return
+
+    if args.solver_only:
+        if rank == 0:
+            print(json.dumps({"solver_study": solver_study(max(args.solver_seeds, 1), local)}))
         return
 
     import torch

@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
     __shared__ int gflag[FCG_GROUPS];
     __shared__ uint64_t bars[FCG_GROUPS];
     __shared__ uint32_t tslot;
+    __shared__ int2 cellmap[64];   // per cell of a 4x4x4 block: (parent-neighbour j, child of it)
     const int d = block_depth[blockIdx.x];
     const CgDepth& dp = deps[d];
     const int grp = threadIdx.x >> 8, lt = threadIdx.x & 255, gbar = 1 + grp;
@@ -205,6 +206,11 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
     if (threadIdx.x < 27) {
         sst[threadIdx.x] = dp.st[threadIdx.x];
         scn[threadIdx.x] = a.cnorm[27 * d + threadIdx.x];
+    }
+    if (threadIdx.x < 64) {
+        const int cell = threadIdx.x, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
+        cellmap[cell] = make_int2(9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1),
+                                  (((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1));
     }
     MlpSmem m;
     stage_mlp_smem(a.wt, sw1, sw2, sb, m);
@@ -289,18 +295,31 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
                         own_p = pnew[iown];
                     }
                 }
-                for (int e = lt; e < 16 * 64; e += 256) {
-                    const int gl = e >> 6, cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
-                    const i64 G = tile * 16 + gl;
-                    const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
-                    const int cn = (G < ng) ? a.gn[(i64)jp * a.ngroups + gfirst + G] : -1;
-                    float val = 0.f;
-                    if (cn != -1) {
-                        const i64 node = cn + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1));
-                        val = init ? rcur[node] : fmaf(nal, a.q[node], rcur[node]);
+                // the group-table entries of the four cells first, then their values: 4 and 8
+                // independent loads in flight per thread
+                int cns[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = lt + 256 * u;
+                    const i64 G = tile * 16 + (e >> 6);
+                    cns[u] = (G < ng) ? a.gn[(i64)cellmap[e & 63].x * a.ngroups + gfirst + G] : -1;
+                }
+                float rv[4], qv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = lt + 256 * u;
+                    rv[u] = qv[u] = 0.f;
+                    if (cns[u] != -1) {
+                        const i64 node = cns[u] + cellmap[e & 63].y;
+                        rv[u] = rcur[node];
+                        if (!init) qv[u] = a.q[node];
                     }
-                    sv[e] = val;
-                    spr[e] = (cn != -1) ? 1 : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = lt + 256 * u;
+                    sv[e] = init ? rv[u] : fmaf(nal, qv[u], rv[u]);
+                    spr[e] = (cns[u] != -1) ? 1 : 0;
                 }
                 group_sync(gbar);
                 {

@@ -149,11 +149,17 @@ __device__ __forceinline__ bool mlp_forward_tile_group(uint8_t* sx, const MlpSme
     tc_fence_after();
     float v[32];
     tmem_ld32(tl + k0, v);
+    // bias in fp32, then two columns per conversion and per ReLU: rounding to bf16 keeps
+    // the sign, so ReLU after rounding gives the values of ReLU before it
+    const __nv_bfloat162 zero2 = __floats2bfloat162_rn(0.f, 0.f);
 #pragma unroll
     for (int c = 0; c < 32; c += 8) {
-        __align__(16) __nv_bfloat16 hb[8];
+        __align__(16) __nv_bfloat162 hb[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) hb[u] = __float2bfloat16_rn(fmaxf(v[c + u] + m.b1[k0 + c + u], 0.f));
+        for (int u = 0; u < 4; ++u)
+            hb[u] = __hmax2(__floats2bfloat162_rn(v[c + 2 * u] + m.b1[k0 + c + 2 * u],
+                                                  v[c + 2 * u + 1] + m.b1[k0 + c + 2 * u + 1]),
+                            zero2);
         *reinterpret_cast<uint4*>(sx + op_offset(128, row, k0 + c)) = *reinterpret_cast<const uint4*>(hb);
     }
     tc_fence_before();
