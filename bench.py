@@ -14,6 +14,10 @@ values + iso-value, marching cubes with subdivision, mesh to host.
           flexible CG against plain CG, on held-out unions of ellipsoids at maxDepth 9
   reference_cuda_build : the reference's own CUDA program on the 50,000-point sphere at
           maxDepth 8 (its compile-time depth), beside this library on the same file
+  kernel_roofline : every kernel timer's algorithmic bytes over its time, as a fraction of
+          the measured HBM copy bandwidth, and the whole step's
+  large_config : the 30M-point displaced sphere at maxDepth 12 (--large 1, the default):
+          throughput, stages, per-kernel rooflines, plain against learned solve
 Timing: CUDA events on the library's stream, per step, L2 flushed (256 MiB
 write) between steps; clocks sampled with nvidia-smi during the timed steps.
 
@@ -56,6 +60,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--solver-seeds", type=int, default=200, help="held-out shapes of the learned-vs-plain "
                     "solver study (0: skip)")
+    ap.add_argument("--large", type=int, default=1, help="1: also run the 30M-point, maxDepth-12 configuration "
+                    "once (large_config object); 0: skip it")
     ap.add_argument("--solver-only", action="store_true", help="run only the learned-vs-plain solver study "
                     "(--solver-seeds shapes) and print it as one JSON line")
     ap.add_argument("--clocks-csv", default=None, help="where to keep the nvidia-smi clock samples "
@@ -351,6 +357,127 @@ def reference_cuda_anchor(device, runs=3):
         shutil.rmtree(work, ignore_errors=True)
 
 
+class Steps:
+    """One reconstruction as a step: device-resident (input already in HBM) or through
+    prgpu_reconstruct with pinned host buffers; timed with CUDA events on the library's stream,
+    L2 flushed before each step."""
+
+    def __init__(self, r, xyz, nrm, dev, flush):
+        import torch
+        self.r, self.n, self.dev, self.flush = r, len(xyz), dev, flush
+        self.h_xyz = torch.from_numpy(xyz).pin_memory()
+        self.h_nrm = torch.from_numpy(nrm).pin_memory()
+        self.d_xyz = self.h_xyz.to(dev)
+        self.d_nrm = self.h_nrm.to(dev)
+        self.stream = torch.cuda.ExternalStream(r.stream(), device=dev)
+
+    def device_step(self):
+        r = self.r
+        r.set_points_device(self.d_xyz.data_ptr(), self.d_nrm.data_ptr(), self.n)
+        r.build_octree()
+        r.compute_rhs()
+        r.solve()
+        r.eval_points()
+        r.extract_mesh()
+
+    def host_step(self):
+        import poissonrecon_gpu_gb300 as pg
+        m = pg.Mesh()
+        rc = pg._lib().prgpu_reconstruct(self.r._h, self.h_xyz.data_ptr(), self.h_nrm.data_ptr(), self.n,
+                                         ctypes.byref(m))
+        if rc not in (0, 5):
+            raise pg.PrgpuError(rc, "prgpu_reconstruct")
+        return m.n_vertices, m.n_triangles
+
+    def timed(self, step, k):
+        import torch
+        ms, out = [], None
+        for _ in range(k):
+            self.flush.fill_(1.0)
+            torch.cuda.synchronize(self.dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            out = step()
+            e1.record(self.stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms, out
+
+
+def kernel_roofline(stats, peaks, ms_per_step):
+    """Every kernel timer's algorithmic bytes per launch over its CUDA-event time, as a fraction of
+    the measured HBM copy bandwidth, and the whole step's algorithmic bytes over its time."""
+    peak = peaks.get("hbm_gbs", 6800.0)
+    out, total = {}, 0.0
+    for name, k in (stats.get("kernels") or {}).items():
+        if k["bytes"] <= 0 or k["ms"] <= 0:
+            continue
+        gbs = k["bytes"] / (k["ms"] * 1e-3) / 1e9
+        out[name] = {"ms_per_launch": round(k["ms"] / max(k["launches"], 1), 4),
+                     "gb_per_launch": round(k["bytes"] / max(k["launches"], 1) / 1e9, 4),
+                     "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+        total += k["bytes"] / max(k["launches"], 1)
+    step_gbs = total / (ms_per_step * 1e-3) / 1e9
+    return {"kernels": out, "step_algorithmic_gb": round(total / 1e9, 3), "step_achieved_gbs": round(step_gbs, 1),
+            "step_frac": round(step_gbs / peak, 4), "peak": peak}
+
+
+def large_config(device, peaks, steps=2, warmup=1):
+    """The 30M-point displaced sphere (4-octave value-noise displacement, amplitude 0.05) at maxDepth
+    12, every depth to relative residual 1e-6: device-resident and end-to-end throughput, stage
+    times, per-kernel rooflines, and the solve with plain CG against the learned preconditioner
+    (the shipped checkpoint, trained at maxDepth 9; plain CG takes over any depth where the
+    network's steps do not reduce the residual)."""
+    import torch
+    import poissonrecon_gpu_gb300 as pg
+    from poissonrecon_gpu_gb300 import shapes
+    dev = torch.device("cuda", device)
+    t0 = time.perf_counter()
+    xyz, nrm = shapes.displaced_sphere(30_000_000, seed=0, device=dev)
+    t_gen = time.perf_counter() - t0
+    n = len(xyz)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    kw = dict(depth=12, solve_mode=pg.SOLVE_RELATIVE, cg_tol=1e-6, cg_max_iter=10000, device=device)
+    r = pg.Reconstructor(**kw)
+    run = Steps(r, xyz, nrm, dev, flush)
+    for _ in range(warmup):
+        run.device_step()
+    dev_ms, _ = run.timed(run.device_step, steps)
+    e2e_ms, (nv, nt) = run.timed(run.host_step, 1)
+    r.set_profiling(True)
+    prof_ms, _ = run.timed(run.device_step, 1)
+    st = r.stats()
+    r.set_profiling(False)
+    solve = {}
+    for name in ("plain", "learned"):
+        if name == "learned":
+            if not os.path.exists(CHECKPOINT):
+                break
+            r.close()
+            r = pg.Reconstructor(preconditioner=CHECKPOINT, **kw)
+            r.set_points_device(run.d_xyz.data_ptr(), run.d_nrm.data_ptr(), n)
+            r.build_octree()
+            r.compute_rhs()
+        ts = []
+        for _ in range(3):
+            r.solve()
+            ts.append(r.stats()["ms"]["solve"])
+        s2 = r.stats()
+        solve[name] = {"ms": float(np.median(ts)), "iters": s2["cg_iters"], "fallback": s2.get("cg_fallback"),
+                       "rel_residual_max": float(max(s2["cg_rel_residual"]))}
+    r.close()
+    t_dev = float(np.mean(dev_ms))
+    return {"workload": "displaced sphere 30000000 points, maxDepth 12, CG to relative residual 1e-06",
+            "value": n / (t_dev * 1e-3), "unit": "points/s", "ms_per_step": t_dev, "steps": steps,
+            "e2e": {"value": n / (e2e_ms[0] * 1e-3), "ms_per_step": e2e_ms[0], "h2d_bytes_per_step": 24 * n,
+                    "d2h_bytes_per_step": int(12 * nv + 12 * nt)},
+            "nodes": st.get("nodes"), "mesh": {"vertices": nv, "triangles": nt}, "stages_ms": st.get("ms"),
+            "profiled_ms_per_step": prof_ms[0], "roofline": kernel_roofline(st, peaks, prof_ms[0]),
+            "solve": solve, "generate_s": round(t_gen, 2),
+            "data": "synthetic, generated on the GPU with torch (shapes.displaced_sphere, device=)"}
+
+
 def max_over_ranks(values, device):
     """Replicas: every rank times its own reconstruction; the job's time is the slowest rank's."""
     import torch
@@ -411,44 +538,11 @@ def main():
 
     xyz, nrm = workload(args)
     n = len(xyz)
-    h_xyz = torch.from_numpy(xyz).pin_memory()
-    h_nrm = torch.from_numpy(nrm).pin_memory()
-    d_xyz = h_xyz.to(dev)
-    d_nrm = h_nrm.to(dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MiB > L2
-
     r = pg.Reconstructor(depth=args.depth, solve_mode=pg.SOLVE_RELATIVE, cg_tol=args.tol, cg_max_iter=10000,
                          device=local)
-    stream = torch.cuda.ExternalStream(r.stream(), device=dev)
-
-    def device_step():
-        r.set_points_device(d_xyz.data_ptr(), d_nrm.data_ptr(), n)
-        r.build_octree()
-        r.compute_rhs()
-        r.solve()
-        r.eval_points()
-        r.extract_mesh()
-
-    def host_step():
-        m = pg.Mesh()
-        rc = pg._lib().prgpu_reconstruct(r._h, h_xyz.data_ptr(), h_nrm.data_ptr(), n, ctypes.byref(m))
-        if rc not in (0, 5):
-            raise pg.PrgpuError(rc, "prgpu_reconstruct")
-        return m.n_vertices, m.n_triangles
-
-    def timed(step, k):
-        ms = []
-        for _ in range(k):
-            flush.fill_(1.0)
-            torch.cuda.synchronize(dev)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            out = step()
-            e1.record(stream)
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        return ms, out
+    run = Steps(r, xyz, nrm, dev, flush)
+    device_step, host_step, timed = run.device_step, run.host_step, run.timed
 
     for _ in range(args.warmup):
         device_step()
@@ -485,6 +579,7 @@ def main():
                 "h2d_bytes_per_step": int(24 * n), "d2h_bytes_per_step": int(12 * nv + 12 * nt)},
         "gpu_launches": int(launches),
         "roofline": roofline(stats, peaks, measured_traffic(args)),
+        "kernel_roofline": kernel_roofline(stats, peaks, float(np.mean(prof_ms))),
         "profiled_ms_per_step": float(np.mean(prof_ms)),
         "clocks": clk.summary(),
         "stages_ms": stats.get("ms"),
@@ -501,11 +596,17 @@ def main():
         if args.solver_seeds > 0:
             out["solver_study"] = solver_study(args.solver_seeds, local)
         out["reference_cuda_build"] = reference_cuda_anchor(local)
+        if args.large:
+            r.close()
+            r = None
+            torch.cuda.empty_cache()
+            out["large_config"] = large_config(local, peaks)
     if os.environ.get("PRGPU_BENCH_NO_CPU") != "1":
         cpu, _ = cpu_reference(args, 1, 0)
         out["cpu_baseline"] = cpu
     print(json.dumps(out))
-    r.close()
+    if r is not None:
+        r.close()
 
 
 if __name__ == "__main__":

@@ -24,13 +24,23 @@ _DTYPES = {
     "dot": np.float64, "ddot": np.float64, "d2dot": np.float64, "stencil": np.float32,
     "vfield": np.float32, "divergence": np.float32, "x": np.float32,
     "cg_iters": np.int32, "cg_rr": np.float32, "point_value": np.float32,
-    "mesh_v": np.float32, "mesh_f": np.int32, "has_tri": np.int32, "has_int": np.int32,
+    "mesh_v": np.float32, "mesh_f": np.int32, "mesh_vkey": np.int64, "has_tri": np.int32, "has_int": np.int32,
     "batch_tri": np.int64, "center": np.float32, "scale": np.float32, "iso": np.float32,
     "subdivide_roots": np.int64,
     "vcells": np.int64,
     "vfield64": np.float64, "divergence64": np.float64, "x64": np.float64, "point_value64": np.float64,
     "cg_iters64": np.int32, "stencil64": np.float64, "iso64": np.float64,
 }
+
+
+def weld(v: np.ndarray, f: np.ndarray, vkey: np.ndarray):
+    """The weld option's rule on the oracle's mesh: one vertex per finest-lattice edge across
+    subdivision batches (the reference keeps one per edge and batch, main.cu:3799-4564).  A
+    welded vertex sits where the first triangle corner on its edge, in triangle order, puts it.
+    v [nv, 3], f [nt, 3], vkey [nv] (orc_get "mesh_vkey"); returns (vertices in key order, faces)."""
+    corners = np.asarray(f, dtype=np.int64).ravel()
+    keys, first, inv = np.unique(np.asarray(vkey)[corners], return_index=True, return_inverse=True)
+    return np.asarray(v).reshape(-1, 3)[corners[first]], inv.reshape(-1, 3).astype(np.int32)
 
 
 def build(force: bool = False) -> str:

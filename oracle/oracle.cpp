@@ -300,6 +300,7 @@ static void init_static_tables() {
 struct Mesh {
     std::vector<float> v;   // 3 per vertex, normalised coordinates
     std::vector<int> f;     // 3 per triangle
+    std::vector<i64> vkey;  // per vertex: its lattice edge (lattice_edge_key), for the weld check
 };
 
 struct Ctx {
@@ -1043,9 +1044,25 @@ static inline double sqdist(const float* a, const float* b) {
     return (double)(dx * dx + dy * dy + dz * dz);
 }
 
-static void append_batch(Ctx& c, const std::vector<float>& vbuf, const std::vector<int>& tbuf) {
+// the finest-lattice edge a vertex lies on: its lower corner's lattice coordinates (corner
+// positions are node centres +- half widths, dyadic, so pos * 2^D is an exact integer) and
+// the edge's axis.  Not a reference quantity: it identifies the vertices that the weld
+// option (one vertex per lattice edge across subdivision batches) merges.
+static inline i64 lattice_edge_key(const float* p1, const float* p2, int dim, int D) {
+    const float s = (float)(1 << D);
+    i64 key = 0;
+    for (int i = 0; i < 3; ++i) {
+        const float lo = (i == dim) ? std::min(p1[i], p2[i]) : p1[i];
+        key = (key << 20) | (i64)std::llround((double)lo * s);
+    }
+    return key * 3 + dim;
+}
+
+static void append_batch(Ctx& c, const std::vector<float>& vbuf, const std::vector<int>& tbuf,
+                         const std::vector<i64>& kbuf) {
     int prev = (int)(c.mesh.v.size() / 3);
     c.mesh.v.insert(c.mesh.v.end(), vbuf.begin(), vbuf.end());
+    c.mesh.vkey.insert(c.mesh.vkey.end(), kbuf.begin(), kbuf.end());
     for (int t : tbuf) c.mesh.f.push_back(t + prev);
     c.batch_tri.push_back((i64)tbuf.size() / 3);
 }
@@ -1061,7 +1078,7 @@ static inline void interpolate(const float* p1, const float* p2, int dim, float 
 static void marching_cubes(Ctx& c) {
     const int D = c.D;
     const i64 M = c.M;
-    c.mesh.v.clear(); c.mesh.f.clear(); c.batch_tri.clear();
+    c.mesh.v.clear(); c.mesh.f.clear(); c.mesh.vkey.clear(); c.batch_tri.clear();
     std::vector<float> cen(3 * M);
     for (i64 i = 0; i < M; ++i) node_center((u64)c.key[i], c.depth[i], D, &cen[3 * i]);
     std::vector<int> nodeVert(8 * M, 0), nodeEdge(12 * M, 0), nodeFace(6 * M, 0);
@@ -1261,11 +1278,13 @@ static void marching_cubes(Ctx& c) {
         int nv = 0;
         for (size_t e = 0; e < E.size(); ++e) { vexAddr[e] = nv; nv += vexNums[e]; }
         std::vector<float> vbuf(3 * (size_t)nv);
+        std::vector<i64> kbuf((size_t)nv);
         for (size_t e = 0; e < E.size(); ++e) {
             if (!vexNums[e]) continue;
             int o = E[e].owner, k = E[e].kind;
             int v1 = nodeVert[8 * (i64)o + MC.edge_v[k][0]] - 1, v2 = nodeVert[8 * (i64)o + MC.edge_v[k][1]] - 1;
             interpolate(V[v1].pos, V[v2].pos, k >> 2, vval[v1], vval[v2], &vbuf[3 * (size_t)vexAddr[e]]);
+            kbuf[vexAddr[e]] = lattice_edge_key(V[v1].pos, V[v2].pos, k >> 2, D);
         }
         std::vector<int> tbuf;
         for (i64 i = c.base[D]; i < M; ++i) {
@@ -1294,7 +1313,7 @@ static void marching_cubes(Ctx& c) {
                 }
             }
         }
-        append_batch(c, vbuf, tbuf);
+        append_batch(c, vbuf, tbuf, kbuf);
     }
     // --- leaves above the finest depth (ProcessLeafNodesAtOtherDepth main.cu:2957-2986) ---
     c.has_tri.assign(c.base[D], 0);
@@ -1471,11 +1490,13 @@ static void marching_cubes(Ctx& c) {
         for (size_t e = 0; e < SE.size(); ++e) { vexAddr[e] = nvx; nvx += vexNums[e]; }
         if (nvx == 0) { c.batch_tri.push_back(0); return; }
         std::vector<float> vbuf(3 * (size_t)nvx);
+        std::vector<i64> kbuf((size_t)nvx);
         for (size_t e = 0; e < SE.size(); ++e) {
             if (!vexNums[e]) continue;
             i64 o = SE[e].owner - MM; int k = SE[e].kind;
             int v1 = nv.vvertices[8 * o + MC.edge_v[k][0]] - 1, v2 = nv.vvertices[8 * o + MC.edge_v[k][1]] - 1;
             interpolate(SV[v1].pos, SV[v2].pos, k >> 2, sval[v1], sval[v2], &vbuf[3 * (size_t)vexAddr[e]]);
+            kbuf[vexAddr[e]] = lattice_edge_key(SV[v1].pos, SV[v2].pos, k >> 2, D);
         }
         std::vector<int> tbuf;
         for (i64 i = first_D; i < nv_nodes; ++i) {
@@ -1486,7 +1507,7 @@ static void marching_cubes(Ctx& c) {
                 for (int q = 0; q < 3; ++q)
                     tbuf.push_back(vexAddr[nv.vedges[12 * i + MC.tri_edges[cat][3 * t + q]] - 1]);
         }
-        append_batch(c, vbuf, tbuf);
+        append_batch(c, vbuf, tbuf, kbuf);
     };
 
     auto rebuild_neighbours = [&](NodeView& nv, i64 lo, i64 hi, int d) {  // computeRebuildNeighbor
@@ -1679,6 +1700,7 @@ const void* orc_get(void* h, const char* name, int64_t* count) {
     if (n == "point_value") RET(c->point_value);
     if (n == "mesh_v") RET(c->mesh.v);
     if (n == "mesh_f") RET(c->mesh.f);
+    if (n == "mesh_vkey") RET(c->mesh.vkey);
     if (n == "has_tri") RET(c->has_tri);
     if (n == "has_int") RET(c->has_int);
     if (n == "batch_tri") RET(c->batch_tri);

@@ -183,8 +183,13 @@ def _value_noise(p, seed, base_freq=4.0, octaves=4, persistence=0.5):
 
 
 def displaced_sphere(n: int = 30_000_000, radius: float = 0.35, amplitude: float = 0.05, seed: int = 0,
-                     chunk: int = 2_000_000):
-    """Sphere radially displaced by 4-octave value noise; normals from the analytic gradient."""
+                     chunk: int = 2_000_000, device=None):
+    """Sphere radially displaced by 4-octave value noise; normals from the analytic gradient.
+    With a torch CUDA device the directions are drawn and displaced there (float64, the same
+    noise tables and formulas; a different seeded sample of the same distribution), which takes
+    well under a second for 30M points instead of about a minute on the host."""
+    if device is not None:
+        return _displaced_sphere_torch(n, radius, amplitude, seed, device)
     rng = np.random.default_rng(seed)
     ps, ns = [], []
     for start in range(0, n, chunk):
@@ -198,4 +203,56 @@ def displaced_sphere(n: int = 30_000_000, radius: float = 0.35, amplitude: float
         nv = _unit(d - amplitude * gt / rad[:, None])
         ps.append(p.astype(np.float32))
         ns.append(nv.astype(np.float32))
+    return np.concatenate(ps), np.concatenate(ns)
+
+
+def _displaced_sphere_torch(n, radius, amplitude, seed, device, chunk=8_000_000):
+    import torch
+    rng = np.random.default_rng(seed)
+    table = torch.tensor(rng.uniform(-1, 1, 4096), dtype=torch.float64, device=device)
+    perm = torch.tensor(rng.permutation(4096), dtype=torch.int64, device=device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    ps, ns = [], []
+    for start in range(0, n, chunk):
+        m = min(chunk, n - start)
+        d = torch.randn((m, 3), generator=gen, dtype=torch.float64, device=device)
+        d = d / torch.linalg.norm(d, dim=1, keepdim=True)
+        total = torch.zeros(m, dtype=torch.float64, device=device)
+        grad = torch.zeros((m, 3), dtype=torch.float64, device=device)
+        amp, freq, norm = 1.0, 4.0, 0.0
+        for _ in range(4):
+            q = d * freq
+            i0 = torch.floor(q).to(torch.int64)
+            f = q - i0
+            sm = f * f * (3 - 2 * f)
+            ds = 6 * f * (1 - f)
+            v = torch.zeros(m, dtype=torch.float64, device=device)
+            g = torch.zeros((m, 3), dtype=torch.float64, device=device)
+            for dx in (0, 1):
+                for dy in (0, 1):
+                    for dz in (0, 1):
+                        h = perm[((i0[:, 0] + dx) * 73856093 ^ (i0[:, 1] + dy) * 19349663 ^
+                                  (i0[:, 2] + dz) * 83492791) & 4095]
+                        c = table[h]
+                        wx = sm[:, 0] if dx else 1 - sm[:, 0]
+                        wy = sm[:, 1] if dy else 1 - sm[:, 1]
+                        wz = sm[:, 2] if dz else 1 - sm[:, 2]
+                        v += c * wx * wy * wz
+                        g[:, 0] += c * (ds[:, 0] if dx else -ds[:, 0]) * wy * wz
+                        g[:, 1] += c * wx * (ds[:, 1] if dy else -ds[:, 1]) * wz
+                        g[:, 2] += c * wx * wy * (ds[:, 2] if dz else -ds[:, 2])
+            total += amp * v
+            grad += amp * freq * g
+            norm += amp
+            amp *= 0.5
+            freq *= 2
+        h, g = total / norm, grad / norm
+        rad = radius + amplitude * h
+        p = 0.5 + rad[:, None] * d
+        gt = g - (g * d).sum(1, keepdim=True) * d
+        nv = d - amplitude * gt / rad[:, None]
+        nv = nv / torch.linalg.norm(nv, dim=1, keepdim=True)
+        ps.append(p.float().cpu().numpy())
+        ns.append(nv.float().cpu().numpy())
     return np.concatenate(ps), np.concatenate(ns)

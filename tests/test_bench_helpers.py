@@ -70,3 +70,32 @@ def test_clock_summary(tmp_path):
     s = c.summary()
     assert s["sm_max_mhz"] == 2070.0 and s["samples"] == 2
     assert s["sm_mhz"] == 2065.0 and s["reasons"] == ["sw_power_cap"]
+
+
+def test_kernel_roofline_covers_every_timer():
+    stats = {"kernels": {"cg": {"ms": 30.0, "launches": 10, "bytes": 5.0e10},
+                         "splat": {"ms": 8.0, "launches": 10, "bytes": 7.0e9},
+                         "lists": {"ms": 1.0, "launches": 5, "bytes": 0}}}
+    k = bench.kernel_roofline(stats, {"hbm_gbs": 6000.0}, 20.0)
+    assert set(k["kernels"]) == {"cg", "splat"}
+    assert abs(k["kernels"]["splat"]["achieved_gbs"] - 0.7e9 / 0.8e-3 / 1e9) < 0.1
+    # the step's algorithmic bytes (5.7 GB per step) over the step time
+    assert abs(k["step_algorithmic_gb"] - 5.7) < 1e-6
+    assert abs(k["step_frac"] - 5.7 / 20e-3 / 6000.0) < 1e-4
+
+
+def test_displaced_sphere_on_a_torch_device():
+    torch = __import__("pytest").importorskip("torch")
+    from poissonrecon_gpu_gb300 import shapes
+    xyz, nrm = shapes.displaced_sphere(5000, seed=1, device=torch.device("cpu"))
+    assert xyz.shape == (5000, 3) and xyz.dtype == np.float32
+    r = np.linalg.norm(xyz - 0.5, axis=1)
+    assert r.min() > 0.35 - 0.05 - 1e-3 and r.max() < 0.35 + 0.05 + 1e-3
+    assert np.allclose(np.linalg.norm(nrm, axis=1), 1.0, atol=1e-5)
+    # the normal leans away from the radial direction only as far as the displacement slopes
+    radial = (xyz - 0.5) / r[:, None]
+    assert np.all((nrm * radial).sum(1) > 0.3)
+    # the same distribution as the host generator's sample
+    xh, _ = shapes.displaced_sphere(5000, seed=1)
+    rh = np.linalg.norm(xh - 0.5, axis=1)
+    assert np.all(np.abs(np.quantile(r, [0.1, 0.5, 0.9]) - np.quantile(rh, [0.1, 0.5, 0.9])) < 3e-3)

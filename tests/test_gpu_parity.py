@@ -136,6 +136,37 @@ def test_mesh_matches_oracle(staged):
     assert np.array_equal(tg, to)
 
 
+def test_weld_matches_oracle(staged, oracle_mod):
+    """weld = 1 against the oracle's mesh welded by the same rule (oracle.weld: one vertex per
+    finest-lattice edge across subdivision batches, placed where the first triangle corner on that
+    edge puts it): given the oracle's solution and iso-value, the same number of vertices, the
+    same vertex positions and the same triangles."""
+    import poissonrecon_gpu_gb300 as pg
+    o = staged["o"]
+    w = pg.Reconstructor(depth=staged["depth"], weld=True)
+    w.set_points(o._xyz, o._nrm)
+    w.build_octree()
+    w.compute_rhs()
+    w.set("x", o.get("x"))
+    w.eval_points()
+    w.set("iso", np.float32([o.get("iso")[0]]))
+    w.extract_mesh()
+    gv, gf = w.mesh()
+    w.close()
+    o.marching_cubes()
+    ov, of = oracle_mod.weld(o.get("mesh_v"), o.get("mesh_f").reshape(-1, 3), o.get("mesh_vkey"))
+    c, s = o.get("center"), o.get("scale")[0]
+    ov = (ov * s).astype(np.float32) + c
+    # unwelded, the oracle has a vertex per lattice edge and batch: the weld merges some
+    assert len(ov) < len(o.get("mesh_v")) // 3
+    assert len(gv) == len(ov) and len(gf) == len(of)
+    row = [("", np.float32)] * 3
+    assert np.array_equal(np.sort(gv.view(row).ravel()), np.sort(ov.view(row).ravel()))
+    tg = np.sort(gv[gf].reshape(len(gf), 9).view([("", np.float32)] * 9).ravel())
+    to = np.sort(ov[of].reshape(len(of), 9).view([("", np.float32)] * 9).ravel())
+    assert np.array_equal(tg, to)
+
+
 def _hausdorff(a, b):
     from scipy.spatial import cKDTree
     return max(cKDTree(b).query(a)[0].max(), cKDTree(a).query(b)[0].max())

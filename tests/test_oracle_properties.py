@@ -78,3 +78,37 @@ def test_duplicate_points_share_leaves(oracle_mod):
     starts = pidx[leaf][nz]
     assert np.all(np.diff(starts) > 0)
     assert np.array_equal(np.sort(o.get("sort_idx")), np.arange(len(xyz2)))
+
+
+def test_weld_rule(oracle_mod):
+    """oracle.weld (the weld option's rule): each vertex lies on the lattice edge its key names;
+    welding keeps the triangles, moves each corner at most along its own lattice edge, and
+    closes the seams between subdivision batches."""
+    from poissonrecon_gpu_gb300 import shapes
+    xyz, nrm = shapes.torus(30000, seed=2)
+    D = 7
+    o = oracle_mod.Oracle(D, threads=4)
+    o.set_points(xyz, nrm)
+    o.reconstruct()
+    v, f, k = o.get("mesh_v").reshape(-1, 3), o.get("mesh_f").reshape(-1, 3), o.get("mesh_vkey")
+    assert len(k) == len(v) and len(np.unique(k)) < len(k)
+    axis = k % 3
+    lat = k // 3
+    lc = np.stack([(lat >> 40) & 0xFFFFF, (lat >> 20) & 0xFFFFF, lat & 0xFFFFF], 1).astype(np.float64) / (1 << D)
+    t = v.astype(np.float64) - lc
+    on = np.ones(len(v), bool)
+    for ax in range(3):
+        sel = axis == ax
+        others = [q for q in range(3) if q != ax]
+        on[sel] &= np.all(t[sel][:, others] == 0, axis=1)
+        on[sel] &= (t[sel, ax] >= 0) & (t[sel, ax] <= 1.0 / (1 << D))
+    assert on.all()
+    wv, wf = oracle_mod.weld(v, f, k)
+    assert len(wf) == len(f) and len(wv) == len(np.unique(k[f.ravel()]))
+    assert np.abs(wv[wf] - v[f]).max() <= 1.0 / (1 << D)
+
+    def open_edges(ff):
+        e = np.sort(np.concatenate([ff[:, [0, 1]], ff[:, [1, 2]], ff[:, [2, 0]]]), axis=1)
+        _, cnt = np.unique(e, axis=0, return_counts=True)
+        return int((cnt == 1).sum())
+    assert open_edges(wf) * 50 < open_edges(f)
