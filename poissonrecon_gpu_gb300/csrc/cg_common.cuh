@@ -45,6 +45,14 @@ struct CgDepth {
     int sym;
 };
 
+// Shared-memory layout of a tile of 4 sibling groups' 4x4x4 blocks in the matrix-vector
+// product.  For each stencil entry the lanes of a warp read the 8 children of 4 groups,
+// at cell offsets {0,1,4,5,16,17,20,21} plus a constant from the group's block start;
+// group gl's block starts 0, 2, 8 or 10 words past a multiple of 32, so the 32 reads fall
+// in 32 distinct banks (with blocks 64 words apart, 4 groups hit the same banks).
+constexpr int CG_TILE_WORDS = 272;
+__host__ __device__ constexpr int cg_block_base(int gl) { return gl * 66 + (gl >> 1) * 4; }
+
 __host__ __device__ constexpr int stencil_class(int j) {
     return (j / 9 != 1) + ((j / 3) % 3 != 1) + (j % 3 != 1);
 }

@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
     extern __shared__ __align__(1024) uint8_t dsm[];
     uint8_t* sw1 = dsm;
     uint8_t* sw2 = dsm + 8192;
-    __shared__ float sp[FCG_WARPS * FCG_WARP_TILES * 4 * 64];   // product staging; r' blocks per group in phase B
+    __shared__ float sp[FCG_WARPS * FCG_WARP_TILES * CG_TILE_WORDS];   // product staging; r' blocks per group in phase B
     __shared__ float sst[27];
     __shared__ float scn[27];
     __shared__ float sb[192];
@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
             const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
             const int ch = lane & 7, gl = lane >> 3;
             const int sx_ = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
-            float* wsp = sp + wib * (FCG_WARP_TILES * 4 * 64);
+            float* wsp = sp + wib * (FCG_WARP_TILES * CG_TILE_WORDS);
             const i64 wstride = (i64)dp.nblocks * FCG_WARPS * FCG_WARP_TILES;
             for (i64 tile = ((i64)rank * FCG_WARPS + wib) * FCG_WARP_TILES; tile * 4 < ng; tile += wstride) {
                 __syncwarp();
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
                 for (int mm = 0; mm < FCG_WARP_TILES * 8; ++mm) {
                     const int e = lane + 32 * mm;
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
-                    wsp[e] = (cn[mm] != -1)
+                    wsp[(e >> 8) * CG_TILE_WORDS + cg_block_base((e >> 6) & 3) + cell] = (cn[mm] != -1)
                                  ? pdir(cn[mm] + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)))
                                  : 0.f;
                 }
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
                 for (int tt = 0; tt < FCG_WARP_TILES; ++tt) {
                     const i64 g = (tile + tt) * 4 + gl;
                     if (g < ng) {
-                        const float* blk = wsp + tt * 256 + gl * 64;
+                        const float* blk = wsp + tt * CG_TILE_WORDS + cg_block_base(gl);
                         float o = 0.f;
                         if (dp.sym) {
 #pragma unroll

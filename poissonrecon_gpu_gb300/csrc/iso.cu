@@ -1071,6 +1071,23 @@ __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, 
     return own;
 }
 
+// sign of a bound [lo, hi] of a brick's corner values against iso: 1 (all above), -1 (all
+// below), 0 (not proven).  The margin m = (2 cnt + 2 BR_WEXT + 8) u A + 4u (|lo| + |hi| + 2|iso|),
+// A = 1.01 amax, covers the evaluation's FMA chain and this bound's own float arithmetic.  It is
+// evaluated in float: every operation of it rounds by at most u relative and every term is
+// non-negative, so scaling by 1 + 2^-16 bounds the exact value from above; the tests are made as
+// lo - iso > m and iso - hi > m, whose float differences are within u of exact, which the extra
+// 2u (|lo| + |hi| + 2|iso|) covers.  (A non-finite bound compares false: not proven.)
+__device__ __forceinline__ signed char bound_sign(float lo, float hi, float amax, int cnt, float iso) {
+    const float u = 5.9604644775390625e-08f;   // 2^-24
+    const float A = amax * 1.01f;
+    const float m = ((2.0f * (float)cnt + (2.0f * BR_WEXT + 8.0f)) * u * A +
+                     6.0f * u * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(iso)) + 1e-30f) * (1.0f + 1.52587890625e-05f);
+    if (lo - iso > m) return 1;
+    if (iso - hi > m) return -1;
+    return 0;
+}
+
 // one warp per super-brick (4^3 bricks of leaves with lattice edge >= 64): the
 // same bound over all its corners; decided only when every window it needs fits
 // the row tables (away from the leaf's boundary).  ssign = 1, -1 or 0.
@@ -1083,7 +1100,6 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
     const int lane = threadIdx.x & 31;
     const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
-    const double u = 5.9604644775390625e-08;   // 2^-24
     for (i64 si = warp; si < nsuper; si += nwarps) {
         int dd = 0;
         while (dd < D - 1 && dl.soff[dd + 1] <= si) ++dd;
@@ -1149,13 +1165,7 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
             amax += __shfl_xor_sync(0xffffffffu, amax, o);
             cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
         }
-        if (lane == 0) {
-            const double iso = (double)v.iso, A = (double)amax * 1.01;
-            const double margin = (2.0 * cnt + 2.0 * BR_WEXT + 8.0) * u * A +
-                                  4.0 * u * (fabs((double)flo) + fabs((double)fhi) + 2.0 * fabs(iso)) + 1e-30;
-            const bool above = (double)flo - margin > iso, below = (double)fhi + margin < iso;
-            ssign[si] = !decided ? 0 : (above ? 1 : (below ? -1 : 0));
-        }
+        if (lane == 0) ssign[si] = decided ? bound_sign(flo, fhi, amax, cnt, v.iso) : 0;
     }
 }
 
@@ -1171,7 +1181,6 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
     const int lane = threadIdx.x & 31;
     const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
-    const double u = 5.9604644775390625e-08;   // 2^-24
     for (i64 bi = first + warp; bi < nbricks; bi += nwarps) {
         const VBrick B = brick_of(v, bix, bi);
         const VRoot R = v.roots[B.root];
@@ -1239,16 +1248,10 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             amax += __shfl_xor_sync(0xffffffffu, amax, o);
             cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
         }
-        if (lane == 0) {
-            // rounding of the evaluation's FMA chain, (cnt + 4) u sum|term|, plus that of
-            // this bound's own float products and sums, at most (cnt + 5) u sum|term|
-            // (factored ancestor rows) -- allowed (cnt + 2 BR_WEXT + 4)
-            const double iso = (double)v.iso, A = (double)amax * 1.01;
-            const double margin = (2.0 * cnt + 2.0 * BR_WEXT + 8.0) * u * A +
-                                  4.0 * u * (fabs((double)lo) + fabs((double)hi) + 2.0 * fabs(iso)) + 1e-30;
-            const bool above = (double)lo - margin > iso, below = (double)hi + margin < iso;
-            sign[bi] = above ? 1 : (below ? -1 : 0);
-        }
+        // rounding of the evaluation's FMA chain, (cnt + 4) u sum|term|, plus that of this
+        // bound's own float products and sums, at most (cnt + 5) u sum|term| (factored
+        // ancestor rows) -- allowed (cnt + 2 BR_WEXT + 4)
+        if (lane == 0) sign[bi] = bound_sign(lo, hi, amax, cnt, v.iso);
     }
 }
 
@@ -1309,16 +1312,16 @@ struct BrickShared {
     static constexpr int K1 = EB + 1;         // corners per axis
     // edge 2 (leaves one depth above the finest): one virtual depth, at most 5^3 window cells
     static constexpr int XW = (EB == BR) ? BR_XW : (EB == 4 ? 728 : 128);
-    float xL[BR_LEVELS * 27];                 // neighbours of the leaf and its ancestors (0: none)
-    float Bt[3 * BR_LEVELS * 4 * K1];         // [axis][depth][t][k]
+    float4 Bt[3 * BR_LEVELS * K1];            // [axis][depth][k], the four t of a corner in one vector
+    float4 xL[BR_LEVELS * 7];                 // neighbours of the leaf and its ancestors (0: none), 27 + 1 per level
     float Xw[XW];                             // window coefficients, virtual depths (0: none or inside the leaf)
     int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
     int wext[BR_LEVELS][3];
     int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
 };
 template <int EB>
-__device__ __forceinline__ float bt_at(const BrickShared<EB>& sm, int ax, int d, int t, int k) {
-    return sm.Bt[((ax * BR_LEVELS + d) * 4 + t) * BrickShared<EB>::K1 + k];
+__device__ __forceinline__ float4 bt_at(const BrickShared<EB>& sm, int ax, int d, int k) {
+    return sm.Bt[(ax * BR_LEVELS + d) * BrickShared<EB>::K1 + k];
 }
 
 // virtual-depth part of the value of corner qc (brick-local kk) whose owner
@@ -1331,20 +1334,31 @@ __device__ __forceinline__ float bt_at(const BrickShared<EB>& sm, int ax, int d,
 // here, and adding a zero product leaves the sum unchanged, so the value is the
 // same.
 template <int EB>
-__device__ __forceinline__ float brick_virtual(const BrickShared<EB>& sm, int D, int r, const int oc[3], const int qc[3],
-                                               const int kk[3]) {
+__device__ __forceinline__ float brick_virtual(const BrickShared<EB>& sm, int D, int r, const int Lc[3], const int oc[3],
+                                               const int qc[3], const int kk[3]) {
     float val = 0.f;
     for (int d = D; d > r; --d) {
         const int off = sm.woff[d];
         if (off < 0) continue;
         const int sh = D - d;
         const int V[3] = {oc[0] >> sh, oc[1] >> sh, oc[2] >> sh};
+        // a 3x3x3 block inside the leaf reads only zeros: its terms leave the sum unchanged
+        const int span = 1 << (d - r);
+        bool inside = true;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const int lo = Lc[ax] << (d - r);
+            inside &= (V[ax] - 1 >= lo) && (V[ax] + 1 < lo + span);
+        }
+        if (inside) continue;
         float bv[3][3];
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
-            const int toff = V[ax] - ((qc[ax] - 1) >> sh);
-#pragma unroll
-            for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, d, t + toff, kk[ax]);
+            const bool toff = V[ax] != ((qc[ax] - 1) >> sh);   // the owner cell is the tabulated one or the next
+            const float4 b = bt_at(sm, ax, d, kk[ax]);
+            bv[ax][0] = toff ? b.y : b.x;
+            bv[ax][1] = toff ? b.z : b.y;
+            bv[ax][2] = toff ? b.w : b.z;
         }
         const int e1 = sm.wext[d][1], e2 = sm.wext[d][2];
         const float* xw = sm.Xw + off + ((V[0] - 1 - sm.wlo[d][0]) * e1 + (V[1] - 1 - sm.wlo[d][1])) * e2 +
@@ -1362,12 +1376,18 @@ __device__ __forceinline__ float brick_virtual(const BrickShared<EB>& sm, int D,
 template <int EB>
 __device__ __forceinline__ float brick_leaf_levels(const BrickShared<EB>& sm, int r, const int kk[3], float val) {
     for (int l = r; l >= 0; --l) {
-        const float* xs = sm.xL + 27 * l;
+        float xs[28];
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            const float4 v4 = sm.xL[7 * l + q];
+            xs[4 * q] = v4.x; xs[4 * q + 1] = v4.y; xs[4 * q + 2] = v4.z; xs[4 * q + 3] = v4.w;
+        }
         float bv[3][3];
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax)
-#pragma unroll
-            for (int t = 0; t < 3; ++t) bv[ax][t] = bt_at(sm, ax, l, t, kk[ax]);
+        for (int ax = 0; ax < 3; ++ax) {
+            const float4 b = bt_at(sm, ax, l, kk[ax]);
+            bv[ax][0] = b.x; bv[ax][1] = b.y; bv[ax][2] = b.z;
+        }
 #pragma unroll
         for (int j = 0; j < 27; ++j) val = fmaf(xs[j] * bv[0][j / 9] * bv[1][(j / 3) % 3], bv[2][j % 3], val);
     }
@@ -1423,12 +1443,16 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
             if (threadIdx.x == 0) atomicAdd(nforeign + 1, 1ull);
             continue;
         }
-        for (int e = threadIdx.x; e < 27 * (r + 1); e += blockDim.x)
-            sm.xL[e] = bix.xl[(i64)lb.root * BR_LEVELS * 27 + e];
+        float* xl_s = reinterpret_cast<float*>(sm.xL);
+        for (int e = threadIdx.x; e < 28 * (r + 1); e += blockDim.x) {
+            const int l = e / 28, j = e % 28;
+            xl_s[e] = (j < 27) ? bix.xl[(i64)lb.root * BR_LEVELS * 27 + 27 * l + j] : 0.f;
+        }
+        float* bt_s = reinterpret_cast<float*>(sm.Bt);
         for (int e = threadIdx.x; e < 3 * 4 * K1 * (D + 1); e += blockDim.x) {
             const int ax = e / (4 * K1 * (D + 1)), q = e % (4 * K1 * (D + 1));
-            const int d = q / (4 * K1), t = (q % (4 * K1)) / K1, k = q % K1;
-            sm.Bt[ax * BR_LEVELS * 4 * K1 + q] = (k <= E) ? brick_bt(a, r, Lc[ax], g0[ax], d, t, k) : 0.f;
+            const int d = q / (4 * K1), k = (q % (4 * K1)) / 4, t = q % 4;
+            bt_s[ax * BR_LEVELS * 4 * K1 + q] = (k <= E) ? brick_bt(a, r, Lc[ax], g0[ax], d, t, k) : 0.f;
         }
         for (int t = threadIdx.x; t < total; t += blockDim.x) sm.Xw[t] = 0.f;
         __syncthreads();
@@ -1472,7 +1496,7 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
                 if ((i64)f < foreign_cap) foreign[f] = make_int2((int)li, e);
                 continue;
             }
-            out[e] = brick_leaf_levels(sm, r, kk, brick_virtual(sm, D, r, oc, qc, kk)) - v.iso;
+            out[e] = brick_leaf_levels(sm, r, kk, brick_virtual(sm, D, r, Lc, oc, qc, kk)) - v.iso;
         }
     }
 }

@@ -18,9 +18,12 @@
 // cells around them -- the children of the parent's 27 neighbours.  So the
 // product reads, per group, the 27 first-child indices of the parent's
 // neighbours (a table built once per solve, 13.5 bytes per row instead of the
-// 108-byte neighbour rows) and the 64 values of p in the block, staged in
+// 108-byte neighbour rows) and the 64 values of r in the block, staged in
 // shared memory.  A missing neighbour reads 0, and adding a zero product
-// leaves the sum unchanged, so q is the same as with the neighbour table.
+// leaves the sum unchanged, so the product is the same as with the neighbour
+// table.  The product is s = A r; the direction's product follows as
+// q = A p = s + beta q_prev (p = r + beta p_prev), so each cell is gathered once
+// per iteration (one vector) rather than forming p at every group that reads it.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -45,9 +48,8 @@ struct CgArgs {
     const float* b;
     float* x;
     float* r;
-    float* p;               // search direction, two buffers used alternately
-    float* p2;
-    float* q;
+    float* p;               // search direction
+    float* q;               // A p
     PartState* state;
     PartSync* sync;         // one per depth
     double* partial;        // one per block
@@ -156,7 +158,7 @@ constexpr int CG_WARP_TILES = 2;               // tiles of 4 groups a warp stage
 
 __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
                                                      const int* __restrict__ block_depth) {
-    __shared__ float sp[CG_TILE_GROUPS * 64 * CG_WARP_TILES];
+    __shared__ float sp[(CG_BLOCK / 32) * CG_WARP_TILES * CG_TILE_WORDS];
     __shared__ float sst[27];
     __shared__ double sh[CG_BLOCK / 32];
     __shared__ double sh_val;
@@ -197,10 +199,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
     int refines = 0;
     double rr_true = -1.0;
     bool restart = true;
-    // p = r + beta p is formed where p is read: from the previous direction in
-    // 'pold' (never written during the pass) into 'pnew' (each row by its own thread)
-    const float* pold = a.p2;
-    float* pnew = a.p;
+    // The product gathers r only: s = A r, then q = A p = s + beta q and p = r + beta p
+    // are formed row by row by the row's own thread (in place: no other thread reads a
+    // row's p or q during the pass)
     while (ok) {
         const bool go = (a.mode == PRGPU_SOLVE_REFERENCE) ? (r1 > a.tol2) : ((double)r1 > a.rel2 * bb);
         if (!go || k > a.max_iter) {
@@ -229,8 +230,17 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
         const bool first = restart;
         restart = false;
         const float beta = first ? 0.f : r1 / r0;
-        auto pdir = [&](i64 i) -> float { return first ? a.r[i] : fmaf(beta, pold[i], a.r[i]); };
-        // q = A p, partial p.q
+        // own row i with s_i = (A r)_i: p_i = r_i + beta p_i, q_i = s_i + beta q_i; partial p.q
+        auto own_row = [&](i64 i, float ri, float si) {
+            float pi = ri, qi = si;
+            if (!first) {
+                pi = fmaf(beta, a.p[i], ri);
+                qi = fmaf(beta, a.q[i], si);
+            }
+            a.p[i] = pi;
+            a.q[i] = qi;
+            loc.add(pi * qi);
+        };
         loc = FSum();
         if (d == 0) {
             for (i64 t = start; t < dp.n; t += stride) {
@@ -239,12 +249,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
 #pragma unroll
                 for (int j = 0; j < 27; ++j) {
                     const int nb = a.neigh[(i64)j * a.M + i];
-                    if (nb != -1 && sst[j] != 0.f) o = fmaf(sst[j], pdir(nb), o);
+                    if (nb != -1 && sst[j] != 0.f) o = fmaf(sst[j], a.r[nb], o);
                 }
-                const float pi = pdir(i);
-                pnew[i] = pi;
-                a.q[i] = o;
-                loc.add(pi * o);
+                own_row(i, a.r[i], o);
             }
         } else {
             // one warp per CG_WARP_TILES tiles of 4 groups (32 rows each); warps run independently.
@@ -254,7 +261,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
             const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
             const int ch = lane & 7, gl = lane >> 3;
             const int sx = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
-            float* wsp = sp + wib * (CG_WARP_TILES * 4 * 64);
+            float* wsp = sp + wib * (CG_WARP_TILES * CG_TILE_WORDS);
             const i64 wstride = (i64)dp.nblocks * (CG_BLOCK / 32) * CG_WARP_TILES;
             for (i64 tile = ((i64)rank * (CG_BLOCK / 32) + wib) * CG_WARP_TILES; tile * 4 < ng; tile += wstride) {
                 __syncwarp();
@@ -273,8 +280,8 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                 for (int m = 0; m < CG_WARP_TILES * 8; ++m) {
                     const int e = lane + 32 * m;
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
-                    wsp[e] = (cn[m] != -1)
-                                 ? pdir(cn[m] + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)))
+                    wsp[(e >> 8) * CG_TILE_WORDS + cg_block_base((e >> 6) & 3) + cell] = (cn[m] != -1)
+                                 ? a.r[cn[m] + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1))]
                                  : 0.f;
                 }
                 __syncwarp();
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                 for (int tt = 0; tt < CG_WARP_TILES; ++tt) {
                     const i64 g = (tile + tt) * 4 + gl;
                     if (g < ng) {
-                        const float* blk = wsp + tt * 256 + gl * 64;
+                        const float* blk = wsp + tt * CG_TILE_WORDS + cg_block_base(gl);
                         float o = 0.f;
                         if (dp.sym) {
 #pragma unroll
@@ -294,10 +301,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
                             for (int j = 0; j < 27; ++j)
                                 o = fmaf(sst[j], blk[(sx + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
                         }
-                        const float pi = blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
-                        pnew[dp.lo + 8 * g + ch] = pi;
-                        a.q[dp.lo + 8 * g + ch] = o;
-                        loc.add(pi * o);
+                        own_row(dp.lo + 8 * g + ch, blk[(sx + 1) * 16 + (sy + 1) * 4 + (sz + 1)], o);
                     }
                 }
             }
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const i64 i = dp.lo + t + u * stride;
-                    pv[u] = pnew[i]; qv[u] = a.q[i]; xv[u] = a.x[i]; rv[u] = a.r[i];
+                    pv[u] = a.p[i]; qv[u] = a.q[i]; xv[u] = a.x[i]; rv[u] = a.r[i];
                 }
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
@@ -328,7 +332,7 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
             }
             for (; t < dp.n; t += stride) {
                 const i64 i = dp.lo + t;
-                a.x[i] = fmaf(al, pnew[i], a.x[i]);
+                a.x[i] = fmaf(al, a.p[i], a.x[i]);
                 const float ri = fmaf(nal, a.q[i], a.r[i]);
                 a.r[i] = ri;
                 loc.add(ri * ri);
@@ -337,8 +341,6 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
         r0 = r1;
         r1 = (float)preduce(loc.value(), ok);
         ++k;
-        pold = pnew;
-        pnew = (pnew == a.p) ? a.p2 : a.p;
     }
     if (rank == 0 && threadIdx.x == 0) {
         ps->iters = k - 1;
@@ -598,7 +600,6 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     float* r = dalloc<float>(M, s);
     float* p = dalloc<float>(M, s);
     float* q = dalloc<float>(M, s);
-    float* p2 = dalloc<float>(M, s);
     // sibling-group table for the matrix-vector products
     const i64 ngroups = (M - 1) / 8;
     ensure_group_table(c);
@@ -639,7 +640,6 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     a.x = c.x;
     a.r = r;
     a.p = p;
-    a.p2 = p2;
     a.q = q;
     a.state = st;
     a.sync = psync;
@@ -675,14 +675,14 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
         c.cg_refines[d] = hs[d].refines;
     }
     if (kt >= 0) {
-        // compulsory per row and iteration: the group table (27 indices per 8 rows), the
-        // previous direction and r read once, p and q written, then p/q/x/r read and x/r
-        // written (8 words)
+        // compulsory per row and iteration: the group table (27 indices per 8 rows); r read
+        // once by the product, p and q read and written; then p/q/x/r read and x/r written
+        // (11 words)
         double bytes = 0;
-        for (int d = d0; d <= d1; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 8 * 4);
+        for (int d = d0; d <= d1; ++d) bytes += (double)hs[d].iters * (double)c.count[d] * (13.5 + 11 * 4);
         c.kpending[kt].bytes = bytes;
     }
-    dfree(r, s); dfree(p, s); dfree(p2, s); dfree(q, s);
+    dfree(r, s); dfree(p, s); dfree(q, s);
     dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(psync, s); dfree(partial, s); dfree(err, s);
     if (herr) {
         set_last_error("solver barrier timed out");

@@ -147,6 +147,7 @@ def test_weld_matches_oracle(staged, oracle_mod):
     w.set_points(o._xyz, o._nrm)
     w.build_octree()
     w.compute_rhs()
+    w.solve()
     w.set("x", o.get("x"))
     w.eval_points()
     w.set("iso", np.float32([o.get("iso")[0]]))
