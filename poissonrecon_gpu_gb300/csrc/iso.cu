@@ -822,19 +822,6 @@ __device__ i64 shell_node(const VArgs& v, int L, int r, const int Lc[3], int d, 
     return descend(nd, an, r, d, N);
 }
 
-// interval of x * X * Y * Z (X, Y, Z intervals), in float: each end is within
-// 3u of the exact product's end
-__device__ __forceinline__ void term_interval(float x, const float* lo, const float* hi, float& tlo, float& thi) {
-    float a = x, b = x;
-    for (int ax = 0; ax < 3; ++ax) {
-        const float c0 = a * lo[ax], c1 = a * hi[ax], c2 = b * lo[ax], c3 = b * hi[ax];
-        a = fminf(fminf(c0, c1), fminf(c2, c3));
-        b = fmaxf(fmaxf(c0, c1), fmaxf(c2, c3));
-    }
-    tlo = a;
-    thi = b;
-}
-
 // the leaf's ancestor levels l <= r of a bound, factored by axis: for every
 // (l, jx, jy) the three z terms x[j] * Z[jz] (scalar times interval) are summed,
 // then multiplied by the intervals Y[jy] and X[jx].  Interval arithmetic is
@@ -1088,6 +1075,83 @@ __device__ __forceinline__ signed char bound_sign(float lo, float hi, float amax
     return 0;
 }
 
+// Shell terms of a bound at virtual depth d: the window cells outside the leaf that hold a
+// real node, each term x * X * Y * Z over the row tables' ranges RW.
+//  * Nodes: a cell's node is found by descending from the leaf's neighbour at depth r.  When
+//    d - r > SHELL_K the warp first finds the nodes of the (at most 2 x 2 x 2) cells of depth
+//    d - SHELL_K that cover the window ("anchors", one lane each) and each cell descends only
+//    SHELL_K levels from its anchor; cells under an absent anchor are skipped, and a window
+//    with no anchor is skipped whole.  The path through the anchor is the same path, so the
+//    node is the same.
+//  * The lanes run over the cells of all boxes in turn (a lane's next cell continues into the
+//    next box), so boxes smaller than a warp leave fewer lanes idle.
+//  * An RW range always contains 0 (lo <= 0 <= hi), and float rounding is monotone, so
+//    [a, b] x [lo, hi] = [min(b lo, a hi), max(a lo, b hi)]: exactly the min and max of the four
+//    rounded products, in 4 multiplies and 2 min/max instead of 4 and 6.
+constexpr int SHELL_K = 4;   // 2^SHELL_K = 16 >= the window's extent: at most 2 anchors per axis
+__device__ __forceinline__ void shell_terms(const VArgs& v, int L, int r, const int Lc[3], int d, int D,
+                                            const int wlo[3], const int ext[3], const float* const row[3],
+                                            int lane, int* __restrict__ anchor, float& lo, float& hi, float& amax,
+                                            int& cnt) {
+    const float* __restrict__ xv = v.e.x;
+    const bool anch = d - r > SHELL_K;
+    int alo[3] = {0, 0, 0};
+    if (anch) {
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) alo[ax] = wlo[ax] >> SHELL_K;   // floor, also below 0
+        int an = -1;
+        if (lane < 8) {
+            const int A[3] = {alo[0] + ((lane >> 2) & 1), alo[1] + ((lane >> 1) & 1), alo[2] + (lane & 1)};
+            an = (int)shell_node(v, L, r, Lc, d - SHELL_K, A);
+        }
+        if (__ballot_sync(0xffffffffu, an >= 0) == 0) return;   // no real node near this window
+        __syncwarp();                                            // the previous depth's readers are done
+        if (lane < 8) anchor[lane] = an;
+        __syncwarp();
+    }
+    const int span = 1 << (d - r);
+    const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
+    Box3 bxs[6];
+    const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
+    const float2* rw[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) rw[ax] = reinterpret_cast<const float2*>(row[ax] + ROW_RW * (D + 1)) + d * BR_WEXT;
+    int g = lane, first = 0;
+    for (int q = 0; q < nbx; ++q) {
+        const Box3 bx = bxs[q];
+        const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
+        const float inv12 = 1.0f / (float)n12, inv2 = 1.0f / (float)bx.n[2];
+        for (; g < first + ncell; g += 32) {
+            const int t = g - first;
+            const int i0 = small_div(t, inv12), rem = t - i0 * n12, i1 = small_div(rem, inv2),
+                      i2 = rem - i1 * bx.n[2];
+            const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
+            i64 node;
+            if (anch) {
+                const int an = anchor[(((N[0] >> SHELL_K) - alo[0]) << 2) | (((N[1] >> SHELL_K) - alo[1]) << 1) |
+                                      ((N[2] >> SHELL_K) - alo[2])];
+                if (an < 0) continue;
+                node = descend(v.e.nd, an, d - SHELL_K, d, N);
+            } else {
+                node = shell_node(v, L, r, Lc, d, N);
+            }
+            if (node < 0) continue;
+            const float x = xv[node];
+            const float2 X = rw[0][N[0] - wlo[0]], Y = rw[1][N[1] - wlo[1]], Z = rw[2][N[2] - wlo[2]];
+            const float p0 = x * X.x, p1 = x * X.y;
+            float a = fminf(p0, p1), b = fmaxf(p0, p1);
+            const float a1 = fminf(b * Y.x, a * Y.y), b1 = fmaxf(a * Y.x, b * Y.y);
+            a = fminf(b1 * Z.x, a1 * Z.y);
+            b = fmaxf(a1 * Z.x, b1 * Z.y);
+            lo += a;
+            hi += b;
+            amax += fmaxf(fabsf(a), fabsf(b));
+            ++cnt;
+        }
+        first += ncell;
+    }
+}
+
 // one warp per super-brick (4^3 bricks of leaves with lattice edge >= 64): the
 // same bound over all its corners; decided only when every window it needs fits
 // the row tables (away from the leaf's boundary).  ssign = 1, -1 or 0.
@@ -1095,6 +1159,7 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
                                                      const i64* __restrict__ srow_prefix,
                                                      const float* __restrict__ srows, const float* __restrict__ xl_all,
                                                      i64 nsuper, signed char* __restrict__ ssign) {
+    __shared__ int s_anchor[256 / 32][8];
     const EvalArgs& a = v.e;
     const int D = a.D;
     const int lane = threadIdx.x & 31;
@@ -1131,33 +1196,7 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
             }
             if (!cross) continue;
             if (ext[0] > BR_WEXT || ext[1] > BR_WEXT || ext[2] > BR_WEXT) { decided = false; break; }
-            const int span = 1 << (d - r);
-            const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
-            Box3 bxs[6];
-            const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
-            for (int q = 0; q < nbx; ++q) {
-                const Box3& bx = bxs[q];
-                const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
-                const float inv12 = 1.0f / (float)n12, inv2 = 1.0f / (float)bx.n[2];
-                for (int t = lane; t < ncell; t += 32) {
-                    const int i0 = small_div(t, inv12), rem = t - i0 * n12, i1 = small_div(rem, inv2),
-                              i2 = rem - i1 * bx.n[2];
-                    const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
-                    const i64 node = shell_node(v, L, r, Lc, d, N);
-                    if (node < 0) continue;
-                    float blo[3], bhi[3];
-                    for (int ax = 0; ax < 3; ++ax) {
-                        const int n = N[ax] - wlo[ax];
-                        blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2];
-                        bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2 + 1];
-                    }
-                    float tl, th;
-                    term_interval(a.x[node], blo, bhi, tl, th);
-                    flo += tl; fhi += th;
-                    amax += fmaxf(fabsf(tl), fabsf(th));
-                    ++cnt;
-                }
-            }
+            shell_terms(v, L, r, Lc, d, D, wlo, ext, row, lane, s_anchor[threadIdx.x >> 5], flo, fhi, amax, cnt);
         }
         for (int o = 16; o; o >>= 1) {
             flo += __shfl_xor_sync(0xffffffffu, flo, o);
@@ -1172,10 +1211,15 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
 // one warp per brick: the bound over the corners the brick's leaf owns;
 // sign[bi] = 1 (all above iso), -1 (all below) or 0 (not proven)
 constexpr int BB_BLOCK = 256;
+// A single-brick leaf whose own real corners change sign ('has_tri') is left unproven at once:
+// its brick's corners include the leaf's corners, so its bound straddles iso (and a brick left
+// unproven is only evaluated exactly, which changes no value).
 __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bix, i64 first, i64 nbricks,
                                                           const i64* __restrict__ sprefix,
                                                           const signed char* __restrict__ ssign,
+                                                          const int* __restrict__ has_tri,
                                                           signed char* __restrict__ sign) {
+    __shared__ int s_anchor[BB_BLOCK / 32][8];
     const EvalArgs& a = v.e;
     const int D = a.D;
     const int lane = threadIdx.x & 31;
@@ -1193,6 +1237,10 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             }
         }
         const int r = R.depth, S = 1 << (D - r), L = R.node, E = brick_edge(D, r), nb = S / E;
+        if (nb == 1 && has_tri[L]) {
+            if (lane == 0) sign[bi] = 0;
+            continue;
+        }
         int Lc[3];
         key_coords(a.nd.key[L], r, D, Lc);
         const int g0[3] = {Lc[0] * S + B.b[0] * E, Lc[1] * S + B.b[1] * E, Lc[2] * S + B.b[2] * E};
@@ -1214,33 +1262,7 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
             }
             if (!cross) continue;
             // only window cells outside the leaf can hold a real node
-            const int span = 1 << (d - r);
-            const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
-            Box3 bxs[6];
-            const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
-            for (int q = 0; q < nbx; ++q) {
-                const Box3& bx = bxs[q];
-                const int n12 = bx.n[1] * bx.n[2], ncell = bx.n[0] * n12;
-                const float inv12 = 1.0f / (float)n12, inv2 = 1.0f / (float)bx.n[2];
-                for (int t = lane; t < ncell; t += 32) {
-                    const int i0 = small_div(t, inv12), rem = t - i0 * n12, i1 = small_div(rem, inv2),
-                              i2 = rem - i1 * bx.n[2];
-                    const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
-                    const i64 node = shell_node(v, L, r, Lc, d, N);
-                    if (node < 0) continue;
-                    float blo[3], bhi[3];
-                    for (int ax = 0; ax < 3; ++ax) {
-                        const int n = N[ax] - wlo[ax];
-                        blo[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2];
-                        bhi[ax] = row[ax][ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2 + 1];
-                    }
-                    float tl, th;
-                    term_interval(a.x[node], blo, bhi, tl, th);
-                    lo += tl; hi += th;
-                    amax += fmaxf(fabsf(tl), fabsf(th));
-                    ++cnt;
-                }
-            }
+            shell_terms(v, L, r, Lc, d, D, wlo, ext, row, lane, s_anchor[threadIdx.x >> 5], lo, hi, amax, cnt);
         }
         for (int o = 16; o; o >>= 1) {
             lo += __shfl_xor_sync(0xffffffffu, lo, o);
@@ -2113,13 +2135,13 @@ void stage_mesh(Ctx& c) {
         }
         // bricks of leaves with lattice edge >= 16 come first (roots are in depth order)
         k_brick_bound<<<grid_for(nbig * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, 0, nbig, dspre,
-                                                                                         ssign, bsign);
+                                                                                         ssign, c.d_has_tri, bsign);
         CK_LAUNCH();
         c.kend(kb);
         const int kb2 = c.kbegin("brick_bound_small", (double)(nbricks - nbig) * 3);
         if (nbricks > nbig) {
             k_brick_bound<<<grid_for((nbricks - nbig) * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(
-                va, bix, nbig, nbricks, dspre, ssign, bsign);
+                va, bix, nbig, nbricks, dspre, ssign, c.d_has_tri, bsign);
             CK_LAUNCH();
         }
         k_brick_cull<<<grid_for(nbricks, 256), 256, 0, s>>>(va, bix, root_of, bsign, nbricks, culled);
