@@ -72,15 +72,23 @@ inline unsigned grid_for(i64 n, int block, i64 cap = (i64)152 * 64) {
 // keys: 3 bits per level, level 1 most significant; x bit 2, y bit 1, z bit 0.
 // A node at depth d keeps its key in the full-depth layout (levels below d = 0).
 // ---------------------------------------------------------------------------
+// every third bit of v (bits 0, 3, 6, ...), packed: the Morton compaction by masks
+__host__ __device__ inline uint32_t morton_compact3(u64 v) {
+    v &= 0x1249249249249249ull;
+    v = (v ^ (v >> 2)) & 0x10c30c30c30c30c3ull;
+    v = (v ^ (v >> 4)) & 0x100f00f00f00f00full;
+    v = (v ^ (v >> 8)) & 0x001f0000ff0000ffull;
+    v = (v ^ (v >> 16)) & 0x001f00000000ffffull;
+    v = (v ^ (v >> 32)) & 0x00000000001fffffull;
+    return (uint32_t)v;
+}
+// cell coordinates at depth d of a key (3D bits, level l's triple x y z at bit 3(D-l))
 __host__ __device__ inline void key_coords(u64 key, int d, int D, int xyz[3]) {
-    int x = 0, y = 0, z = 0;
-    for (int l = 1; l <= d; ++l) {
-        int sh = 3 * (D - l);
-        x = (x << 1) | (int)((key >> (sh + 2)) & 1);
-        y = (y << 1) | (int)((key >> (sh + 1)) & 1);
-        z = (z << 1) | (int)((key >> sh) & 1);
-    }
-    xyz[0] = x; xyz[1] = y; xyz[2] = z;
+    const u64 k = d > 0 ? key >> (3 * (D - d)) : 0ull;
+    const uint32_t m = (1u << d) - 1u;
+    xyz[0] = (int)(morton_compact3(k >> 2) & m);
+    xyz[1] = (int)(morton_compact3(k >> 1) & m);
+    xyz[2] = (int)(morton_compact3(k) & m);
 }
 __host__ __device__ inline u64 coords_key(int x, int y, int z, int d, int D) {
     u64 k = 0;

@@ -222,24 +222,32 @@ __device__ __forceinline__ float level_sum_u(const EvalArgs& a, i64 node, int d,
     }
     return val;
 }
+// from a node to the root: a parent is one depth up and its cell coordinates are the
+// child's halved, so the node's key is decoded once
 __device__ __forceinline__ float walk_up_u(const EvalArgs& a, i64 node, const int u[3], float val) {
+    if (node == -1) return val;
+    int d = a.nd.depth[node];
+    int xyz[3];
+    key_coords(a.nd.key[node], d, a.D, xyz);
     while (node != -1) {
-        const int d = a.nd.depth[node];
-        int xyz[3];
-        key_coords(a.nd.key[node], d, a.D, xyz);
         val = level_sum_u(a, node, d, xyz, u, val);
         node = a.nd.parent[node];
+        --d;
+        xyz[0] >>= 1; xyz[1] >>= 1; xyz[2] >>= 1;
     }
     return val;
 }
 
 __device__ __forceinline__ float walk_up(const EvalArgs& a, i64 node, const float q[3], float val) {
+    if (node == -1) return val;
+    int d = a.nd.depth[node];
+    int xyz[3];
+    key_coords(a.nd.key[node], d, a.D, xyz);
     while (node != -1) {
-        const int d = a.nd.depth[node];
-        int xyz[3];
-        key_coords(a.nd.key[node], d, a.D, xyz);
         val = level_sum(a, node, d, xyz, q, val);
         node = a.nd.parent[node];
+        --d;
+        xyz[0] >>= 1; xyz[1] >>= 1; xyz[2] >>= 1;
     }
     return val;
 }
@@ -322,12 +330,14 @@ __device__ float owner_corner_value(const EvalArgs& a, i64 o, int kind, float is
         val = walk_up_u(a, o, u, val);
         const int exceed = c_vid[kind];
         i64 node = o;
+        int cx[3] = {xyz[0], xyz[1], xyz[2]};
         for (int dd = d + 1; dd <= a.D; ++dd) {
             const int c0 = a.nd.child0[node];
             if (c0 == -1) break;
-            node = c0 + exceed;
-            int cx[3];
-            key_coords(a.nd.key[node], dd, a.D, cx);
+            node = c0 + exceed;   // child 'exceed': its coordinates are the parent's doubled plus its bits
+            cx[0] = (cx[0] << 1) | ((exceed >> 2) & 1);
+            cx[1] = (cx[1] << 1) | ((exceed >> 1) & 1);
+            cx[2] = (cx[2] << 1) | (exceed & 1);
             val = level_sum_u(a, node, dd, cx, u, val);
         }
     }
@@ -554,12 +564,14 @@ __global__ void __launch_bounds__(128, 6) k_coarse_corner_values(EvalArgs a, i64
                     const int exceed = c_vid[kind];
                     i64 node = i;
                     float v = val[kind];
+                    int cx[3] = {xyz[0], xyz[1], xyz[2]};
                     for (int dd = d + 1; dd <= D; ++dd) {
                         const int c0 = nd.child0[node];
                         if (c0 == -1) break;
                         node = c0 + exceed;
-                        int cx[3];
-                        key_coords(nd.key[node], dd, D, cx);
+                        cx[0] = (cx[0] << 1) | ((exceed >> 2) & 1);
+                        cx[1] = (cx[1] << 1) | ((exceed >> 1) & 1);
+                        cx[2] = (cx[2] << 1) | (exceed & 1);
                         v = level_sum_u(a, node, dd, cx, u, v);
                     }
                     val[kind] = v;
