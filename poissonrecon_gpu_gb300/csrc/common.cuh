@@ -90,14 +90,23 @@ __host__ __device__ inline void key_coords(u64 key, int d, int D, int xyz[3]) {
     xyz[1] = (int)(morton_compact3(k >> 1) & m);
     xyz[2] = (int)(morton_compact3(k) & m);
 }
+// bit i of x to bit 3i (21 bits): the Morton spread by masks
+__host__ __device__ inline u64 morton_spread3(uint32_t x) {
+    u64 v = x & 0x1fffffu;
+    v = (v | (v << 32)) & 0x001f00000000ffffull;
+    v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+// the key of the depth-d cell (x, y, z): the low d bits of each coordinate, interleaved
 __host__ __device__ inline u64 coords_key(int x, int y, int z, int d, int D) {
-    u64 k = 0;
-    for (int l = 1; l <= d; ++l) {
-        int b = d - l;
-        u64 g = ((u64)((x >> b) & 1) << 2) | ((u64)((y >> b) & 1) << 1) | (u64)((z >> b) & 1);
-        k |= g << (3 * (D - l));
-    }
-    return k;
+    if (d <= 0) return 0ull;
+    const uint32_t m = (1u << d) - 1u;
+    const u64 k = (morton_spread3((uint32_t)x & m) << 2) | (morton_spread3((uint32_t)y & m) << 1) |
+                  morton_spread3((uint32_t)z & m);
+    return k << (3 * (D - d));
 }
 
 // ---------------------------------------------------------------------------

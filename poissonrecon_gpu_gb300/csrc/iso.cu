@@ -1055,6 +1055,25 @@ __global__ void k_brick_xl(VArgs v, int nroots, float* __restrict__ xl) {
     }
 }
 
+// lower_face_owner with the batch membership of the leaf's 27 neighbours looked up once
+// (member[j]: batch_member's answer for the leaf at offset j, 13 = the leaf itself)
+__device__ __forceinline__ int lower_face_owner_cached(const VArgs& v, const VRoot& R, const int Lc[3], const int qc[3],
+                                                       const int* member, int oc[3]) {
+    const int D = v.e.D, sh = D - R.depth, lim = 1 << D;
+    u64 best = ~0ull;
+    int own = -1;
+    for (int eo = 0; eo < 8; ++eo) {
+        const int cell[3] = {qc[0] - (eo & 1), qc[1] - ((eo >> 1) & 1), qc[2] - ((eo >> 2) & 1)};
+        if (cell[0] < 0 || cell[1] < 0 || cell[2] < 0 || cell[0] >= lim || cell[1] >= lim || cell[2] >= lim) continue;
+        const int j = 9 * ((cell[0] >> sh) - Lc[0] + 1) + 3 * ((cell[1] >> sh) - Lc[1] + 1) + ((cell[2] >> sh) - Lc[2] + 1);
+        const int m = member[j];
+        if (m < 0) continue;
+        const u64 kk = cell_key_D(cell, D);
+        if (kk < best) { best = kk; own = m; oc[0] = cell[0]; oc[1] = cell[1]; oc[2] = cell[2]; }
+    }
+    return own;
+}
+
 // owner of a lower-face corner (min key among batch cells sharing it)
 __device__ __forceinline__ int lower_face_owner(const VArgs& v, const VRoot& R, const int Lc[3], const int qc[3],
                                                 int oc[3]) {
@@ -1352,6 +1371,7 @@ struct BrickShared {
     int wlo[BR_LEVELS][3];                    // window origin (cell coordinates at that depth)
     int wext[BR_LEVELS][3];
     int woff[BR_LEVELS];                      // offset into Xw, -1 when no corner reaches outside the leaf
+    int member[27];                           // batch_member of the leaf at each neighbour offset
 };
 template <int EB>
 __device__ __forceinline__ float4 bt_at(const BrickShared<EB>& sm, int ax, int d, int k) {
@@ -1489,6 +1509,12 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
             bt_s[ax * BR_LEVELS * 4 * K1 + q] = (k <= E) ? brick_bt(a, r, Lc[ax], g0[ax], d, t, k) : 0.f;
         }
         for (int t = threadIdx.x; t < total; t += blockDim.x) sm.Xw[t] = 0.f;
+        if (fposs && threadIdx.x < 27) {
+            const int j = threadIdx.x;
+            const int cell[3] = {(Lc[0] + j / 9 - 1) << (D - r), (Lc[1] + (j / 3) % 3 - 1) << (D - r),
+                                 (Lc[2] + j % 3 - 1) << (D - r)};
+            sm.member[j] = batch_member(v, R, Lc, cell);
+        }
         __syncthreads();
         // only window cells outside the leaf can hold a real node
         for (int d = r + 1; d <= D; ++d) {
@@ -1517,20 +1543,34 @@ __global__ void __launch_bounds__(NT) k_brick_eval(VArgs v, BrickIndex bix, cons
         __syncthreads();
         float* out = blat + lb.lat;
         const int ncorner = E1 * E1 * E1;
-        for (int e = threadIdx.x; e < ncorner; e += blockDim.x) {
+        const int lane = threadIdx.x & 31;
+        // the warp's lanes take the same iterations (e = e0 + lane), so the foreign slots are
+        // claimed with one atomic per warp
+        for (int e0 = threadIdx.x - lane; e0 < ncorner; e0 += blockDim.x) {
+            const int e = e0 + lane;
+            const bool valid = e < ncorner;
             const int kk[3] = {e / (E1 * E1), (e / E1) % E1, e % E1};
             const int uu = lb.b[0] * E + kk[0], ww = lb.b[1] * E + kk[1], zz = lb.b[2] * E + kk[2];
             const int qc[3] = {g0[0] + kk[0], g0[1] + kk[1], g0[2] + kk[2]};
             // owner cell: the cell below the corner on every axis, except on the leaf's lower faces
             int oc[3] = {qc[0] - 1 + (uu == 0), qc[1] - 1 + (ww == 0), qc[2] - 1 + (zz == 0)};
             int own = L;
-            if (fposs && (uu == 0 || ww == 0 || zz == 0)) own = lower_face_owner(v, R, Lc, qc, oc);
-            if (own != L) {   // owned by another leaf of the batch: filled by k_foreign_fill
-                const unsigned long long f = atomicAdd(nforeign, 1ull);
-                if ((i64)f < foreign_cap) foreign[f] = make_int2((int)li, e);
-                continue;
+            if (valid && fposs && (uu == 0 || ww == 0 || zz == 0))
+                own = lower_face_owner_cached(v, R, Lc, qc, sm.member, oc);
+            // owned by another leaf of the batch: filled by k_foreign_fill
+            const bool isf = valid && own != L;
+            const unsigned fm = __ballot_sync(0xffffffffu, isf);
+            if (fm) {
+                const int leader = __ffs(fm) - 1;
+                unsigned long long base = 0;
+                if (lane == leader) base = atomicAdd(nforeign, (unsigned long long)__popc(fm));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (isf) {
+                    const unsigned long long f = base + (unsigned long long)__popc(fm & ((1u << lane) - 1u));
+                    if ((i64)f < foreign_cap) foreign[f] = make_int2((int)li, e);
+                }
             }
-            out[e] = brick_leaf_levels(sm, r, kk, brick_virtual(sm, D, r, Lc, oc, qc, kk)) - v.iso;
+            if (valid && !isf) out[e] = brick_leaf_levels(sm, r, kk, brick_virtual(sm, D, r, Lc, oc, qc, kk)) - v.iso;
         }
     }
 }
