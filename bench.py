@@ -488,7 +488,10 @@ def max_over_ranks(values, device):
 
 
 def roofline(stats, peaks, traffic):
+    """The dominant kernel's roofline.  A timer with sub-timers ("divergence" and its
+    "divergence_*" kernels) spans several kernels and is not a candidate; its kernels are."""
     ks = stats.get("kernels", {})
+    ks = {n: k for n, k in ks.items() if not any(m.startswith(n + "_") for m in ks)}
     if not ks:
         return None
     name, k = max(ks.items(), key=lambda kv: kv[1]["ms"])
