@@ -487,11 +487,13 @@ def max_over_ranks(values, device):
     return [float(x) for x in t]
 
 
+# library timers that span several kernels, each of which also has its own timer
+AGGREGATE_TIMERS = {"divergence"}   # divergence_d, divergence_d1, divergence_groups, divergence_root
+
+
 def roofline(stats, peaks, traffic):
-    """The dominant kernel's roofline.  A timer with sub-timers ("divergence" and its
-    "divergence_*" kernels) spans several kernels and is not a candidate; its kernels are."""
-    ks = stats.get("kernels", {})
-    ks = {n: k for n, k in ks.items() if not any(m.startswith(n + "_") for m in ks)}
+    """The dominant kernel's roofline (an aggregate timer is not a kernel; its kernels are)."""
+    ks = {n: k for n, k in stats.get("kernels", {}).items() if n not in AGGREGATE_TIMERS}
     if not ks:
         return None
     name, k = max(ks.items(), key=lambda kv: kv[1]["ms"])

@@ -41,6 +41,7 @@ void Ctx::free_nodes() {
     dfree(nodes.dnum, s); dfree(nodes.parent, s); dfree(nodes.child0, s); dfree(nodes.depth, s);
     dfree(nodes.neigh, s);
     dfree(gn, s);
+    dfree(gn_rows, s);
     nodes.M = 0;
 }
 void Ctx::free_all() {

@@ -51,6 +51,9 @@ struct CgDepth {
 // group gl's block starts 0, 2, 8 or 10 words past a multiple of 32, so the 32 reads fall
 // in 32 distinct banks (with blocks 64 words apart, 4 groups hit the same banks).
 constexpr int CG_TILE_WORDS = 272;
+// The sibling-group table row by row for the solvers: a group's 27 first-child indices (and a
+// pad), so a warp's consecutive groups are one contiguous run of the table.
+constexpr int GN_ROW = 28;
 __host__ __device__ constexpr int cg_block_base(int gl) { return gl * 66 + (gl >> 1) * 4; }
 
 __host__ __device__ constexpr int stencil_class(int j) {

@@ -141,6 +141,7 @@ struct Ctx {
     std::vector<i64> roots_per_depth;   // subdivided leaves by depth
     i64 virtual_cells = 0;
     int* gn = nullptr;                  // sibling-group table (ensure_group_table), freed with the nodes
+    int* gn_rows = nullptr;             // the same table row by row, GN_ROW ints per group (ensure_group_rows)
     i64 total_bricks = 0, live_bricks = 0;   // subdivided leaves: bricks, and those not culled
     i64 foreign_corners = 0;                 // brick corners owned by another leaf of the batch
     i64 foreign_slow = 0;                    // of those, evaluated because the owner's brick was culled

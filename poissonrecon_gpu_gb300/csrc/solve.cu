@@ -44,6 +44,7 @@ struct CgArgs {
     i64 M;
     const int* neigh;       // 27 x M
     const int* gn;          // 27 x ngroups: first child of each neighbour of a sibling group's parent, or -1
+    const int* gnr;         // the same, GN_ROW per group
     i64 ngroups;            // sibling groups (nodes 1..M-1, 8 per group)
     const float* b;
     float* x;
@@ -153,12 +154,22 @@ __global__ void k_group_table(NodeArrays nd, i64 ngroups, int* __restrict__ gn) 
     }
 }
 
+// the group table row by row (GN_ROW per group; the pad entry -1)
+__global__ void k_group_rows(const int* __restrict__ gn, i64 ngroups, int* __restrict__ rows) {
+    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < ngroups * GN_ROW; e += (i64)gridDim.x * blockDim.x) {
+        const i64 g = e / GN_ROW;
+        const int jp = (int)(e % GN_ROW);
+        rows[e] = (jp < 27) ? gn[(i64)jp * ngroups + g] : -1;
+    }
+}
+
 constexpr int CG_TILE_GROUPS = CG_BLOCK / 8;   // sibling groups per tile, one thread per row
 constexpr int CG_WARP_TILES = 2;               // tiles of 4 groups a warp stages at once
 
 __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
                                                      const int* __restrict__ block_depth) {
     __shared__ float sp[(CG_BLOCK / 32) * CG_WARP_TILES * CG_TILE_WORDS];
+    __shared__ int sgn[(CG_BLOCK / 32) * CG_WARP_TILES * 4 * GN_ROW];
     __shared__ float sst[27];
     __shared__ double sh[CG_BLOCK / 32];
     __shared__ double sh_val;
@@ -255,15 +266,26 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
             }
         } else {
             // one warp per CG_WARP_TILES tiles of 4 groups (32 rows each); warps run independently.
-            // All group-table entries of the tiles are loaded before any gather, so each warp
-            // has 2 * CG_WARP_TILES * 8 independent loads in flight per round trip.
+            // The tiles' group-table rows are one contiguous run, read coalesced into shared
+            // memory; then every lane has 2 * CG_WARP_TILES * 8 independent gathers in flight.
             const i64 gfirst = (dp.lo - 1) >> 3, ng = dp.n >> 3;
             const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
             const int ch = lane & 7, gl = lane >> 3;
             const int sx = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
             float* wsp = sp + wib * (CG_WARP_TILES * CG_TILE_WORDS);
+            int* wgn = sgn + wib * (CG_WARP_TILES * 4 * GN_ROW);
             const i64 wstride = (i64)dp.nblocks * (CG_BLOCK / 32) * CG_WARP_TILES;
             for (i64 tile = ((i64)rank * (CG_BLOCK / 32) + wib) * CG_WARP_TILES; tile * 4 < ng; tile += wstride) {
+                __syncwarp();
+                {
+                    const i64 row0 = (gfirst + tile * 4) * GN_ROW;
+                    const i64 nvalid = min((i64)CG_WARP_TILES * 4, ng - tile * 4) * GN_ROW;
+#pragma unroll
+                    for (int k = 0; k < (CG_WARP_TILES * 4 * GN_ROW + 31) / 32; ++k) {
+                        const int idx = lane + 32 * k;
+                        if (idx < CG_WARP_TILES * 4 * GN_ROW) wgn[idx] = (idx < nvalid) ? a.gnr[row0 + idx] : -1;
+                    }
+                }
                 __syncwarp();
                 // the 4x4x4 block of each group: cell (bx,by,bz) is child ((bx+1)&1, ...) of the
                 // parent's neighbour ((bx+1)>>1, ...) in 0..2 per axis
@@ -271,10 +293,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
 #pragma unroll
                 for (int m = 0; m < CG_WARP_TILES * 8; ++m) {
                     const int e = lane + 32 * m;
-                    const i64 g = tile * 4 + (e >> 6);
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
                     const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
-                    cn[m] = (g < ng) ? a.gn[(i64)jp * a.ngroups + gfirst + g] : -1;
+                    cn[m] = wgn[(e >> 6) * GN_ROW + jp];
                 }
 #pragma unroll
                 for (int m = 0; m < CG_WARP_TILES * 8; ++m) {
@@ -349,6 +370,18 @@ __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth*
         ps->rr_true = rr_true;
         ps->refines = refines;
         ps->status = ok ? 0 : PRGPU_ERR_TIMEOUT;
+    }
+}
+
+// the group table row by row, built once per octree
+void ensure_group_rows(Ctx& c) {
+    if (c.gn_rows) return;
+    ensure_group_table(c);
+    const i64 ngroups = (c.nodes.M - 1) / 8;
+    c.gn_rows = dalloc<int>(std::max<i64>(ngroups * GN_ROW, 1), c.stream);
+    if (ngroups > 0) {
+        k_group_rows<<<grid_for(ngroups * GN_ROW, 256), 256, 0, c.stream>>>(c.gn, ngroups, c.gn_rows);
+        CK_LAUNCH();
     }
 }
 
@@ -602,7 +635,7 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     float* q = dalloc<float>(M, s);
     // sibling-group table for the matrix-vector products
     const i64 ngroups = (M - 1) / 8;
-    ensure_group_table(c);
+    ensure_group_rows(c);
     const int* gn = c.gn;
     // co-resident capacity
     int dev = c.device, sms = 0, per_sm = 0;
@@ -635,6 +668,7 @@ void stage_solve_depths(Ctx& c, int d0, int d1, int mode, const float* rhs) {
     a.M = M;
     a.neigh = c.nodes.neigh;
     a.gn = gn;
+    a.gnr = c.gn_rows;
     a.ngroups = ngroups;
     a.b = rhs ? rhs : c.divergence;
     a.x = c.x;

@@ -57,7 +57,7 @@ def test_roofline_of_the_dominant_timer():
     assert abs(r["frac"] - r["achieved"] / 6772.9) < 1e-4
     assert r["traffic"] == 123 and r["peak_source"].startswith("measured")
     assert bench.roofline({"kernels": {}}, {}, {}) is None
-    # a timer spanning several kernels (it has sub-timers) is not the dominant kernel
+    # a timer spanning several kernels is not the dominant kernel
     agg = {"kernels": dict(stats["kernels"], divergence={"ms": 40.0, "launches": 10, "bytes": 1e9},
                            divergence_groups={"ms": 20.0, "launches": 10, "bytes": 0})}
     assert bench.roofline(agg, {"hbm_gbs": 6772.9}, {})["kernel"] == "cg"
