@@ -290,6 +290,15 @@ int prgpu_mlp_forward(void* trainer, const uint16_t* features, int64_t n, float*
 int prgpu_mlp_gradients(void* trainer, const uint16_t* features, const float* targets, int64_t n, float* grad,
                         double* loss);
 
+/* Density-based depth (not in the reference, whose maxDepth is a compile-time constant,
+ * main.cu:69): the octree of the cloud is built at max_depth on the device, occupied[d]
+ * (nodes of depth d holding at least one point, max_depth+1 entries, may be NULL) counted, and
+ * *depth set to the largest d in 2..max_depth whose mean points per occupied node
+ * n / occupied[d] is at least samples_per_node (2 when none is).  Kazhdan's samples-per-node
+ * rule applied to the whole cloud: sparse clouds get a coarser octree. */
+int prgpu_choose_depth(const float* xyz, const float* nrm, int64_t n, int32_t max_depth, double samples_per_node,
+                       int32_t device, int32_t* depth, int64_t* occupied);
+
 /* PLY I/O (PointStream.inl:160-239 input; PlyWriteTriangles plyfile.cu:2769-2836 output).
  * prgpu_read_points returns library-owned arrays valid until the next call. */
 int prgpu_read_points(const char* path, int64_t* n, const float** xyz, const float** nrm);

@@ -33,6 +33,23 @@ _DTYPES = {
 }
 
 
+def occupied_per_depth(o) -> np.ndarray:
+    """Nodes of each depth holding at least one point, from the oracle's octree (pnum, base)."""
+    base, pnum = o.get("base"), o.get("pnum")
+    return np.array([int((pnum[base[d]:base[d + 1]] > 0).sum()) for d in range(len(base) - 1)], np.int64)
+
+
+def choose_depth(n: int, occupied, max_depth: int, samples_per_node: float) -> int:
+    """The density-based depth rule of prgpu_choose_depth: the largest d in 2..max_depth with
+    n / occupied[d] >= samples_per_node (2 when none is).  Kazhdan's samples-per-node criterion
+    over the whole cloud; the reference fixes maxDepth at compile time (main.cu:69)."""
+    best = 2
+    for d in range(2, max_depth + 1):
+        if occupied[d] > 0 and n / occupied[d] >= samples_per_node:
+            best = d
+    return best
+
+
 def weld(v: np.ndarray, f: np.ndarray, vkey: np.ndarray):
     """The weld option's rule on the oracle's mesh: one vertex per finest-lattice edge across
     subdivision batches (the reference keeps one per edge and batch, main.cu:3799-4564).  A

@@ -116,6 +116,7 @@ SIGNATURES = {
     "prgpu_read_points": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_I64), ctypes.POINTER(_VP),
                                          ctypes.POINTER(_VP)]),
     "prgpu_write_mesh_ply": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Mesh), _I32]),
+    "prgpu_choose_depth": (ctypes.c_int, [_VP, _VP, _I64, _I32, ctypes.c_double, _I32, ctypes.POINTER(_I32), _VP]),
 }
 
 _LIB = None
@@ -305,6 +306,17 @@ class Reconstructor:
         buf = ctypes.create_string_buffer(1 << 16)
         _check(_lib().prgpu_stats_json(self._h, buf, len(buf)), "prgpu_stats_json")
         return json.loads(buf.value.decode())
+
+
+def choose_depth(xyz, nrm, max_depth: int = 10, samples_per_node: float = 8.0, device: int = 0):
+    """Density-based depth (prgpu_choose_depth): the finest depth <= max_depth whose occupied
+    nodes hold samples_per_node points each on average.  Returns (depth, occupied nodes per depth)."""
+    xyz, nrm = _f32(xyz), _f32(nrm)
+    d = ctypes.c_int32(0)
+    occ = np.zeros(max_depth + 1, np.int64)
+    _check(_lib().prgpu_choose_depth(xyz.ctypes.data, nrm.ctypes.data, len(xyz), max_depth, float(samples_per_node),
+                                     device, ctypes.byref(d), occ.ctypes.data), "prgpu_choose_depth")
+    return int(d.value), occ
 
 
 # ---- reference-named helpers -------------------------------------------------

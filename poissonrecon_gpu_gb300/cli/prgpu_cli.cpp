@@ -1,7 +1,7 @@
 // prgpu: command-line front end of the library.
 //   prgpu --in points.ply --out mesh.ply [--depth 8] [--binary] [--relative TOL]
 //         [--maxIter N] [--device K] [--weld] [--density] [--cascadic] [--refine]
-//         [--stable-basis] [--learned CHECKPOINT] [--stats]
+//         [--stable-basis] [--learned CHECKPOINT] [--samples-per-node K] [--stats]
 // The reference takes its input/output paths and maxDepth at compile time
 // (main.cu:69,3251-3252); the flag names follow the Kazhdan-style "--name value"
 // convention of its CmdLineParser (CmdLineParser.cu:205-240).
@@ -17,7 +17,9 @@ static void usage() {
     fprintf(stderr,
             "usage: prgpu --in <points.ply|.bnpts|ascii> --out <mesh.ply> [--depth D] [--binary]\n"
             "             [--relative TOL] [--maxIter N] [--device K] [--weld] [--density] [--cascadic]\n"
-            "             [--refine] [--stable-basis] [--learned CHECKPOINT] [--stats]\n");
+            "             [--refine] [--stable-basis] [--learned CHECKPOINT] [--samples-per-node K] [--stats]\n"
+            "  --samples-per-node K: the depth is the finest (at most --depth) whose occupied nodes\n"
+            "                        hold K points each on average\n");
 }
 
 int main(int argc, char** argv) {
@@ -27,6 +29,7 @@ int main(int argc, char** argv) {
     prgpu_params_default(&p);
     int binary = 0, stats = 0;
     const char* learned = nullptr;
+    double samples_per_node = 0.0;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
         auto next = [&]() -> const char* {
@@ -46,6 +49,7 @@ int main(int argc, char** argv) {
         else if (a == "--refine") p.refine = 1;
         else if (a == "--stable-basis") p.stable_basis = 1;
         else if (a == "--learned") { learned = next(); p.learned = 1; }
+        else if (a == "--samples-per-node") samples_per_node = atof(next());
         else if (a == "--stats") stats = 1;
         else { usage(); return 2; }
     }
@@ -55,6 +59,15 @@ int main(int argc, char** argv) {
     const float *xyz = nullptr, *nrm = nullptr;
     int rc = prgpu_read_points(in, &n, &xyz, &nrm);
     if (rc) { fprintf(stderr, "read failed (%d): %s\n", rc, prgpu_last_error()); return 1; }
+    if (samples_per_node > 0.0) {
+        int32_t d = 0;
+        if ((rc = prgpu_choose_depth(xyz, nrm, n, p.depth, samples_per_node, p.device, &d, nullptr))) {
+            fprintf(stderr, "depth choice failed (%d): %s\n", rc, prgpu_last_error());
+            return 1;
+        }
+        fprintf(stderr, "depth %d (at most %d, %.1f points per node)\n", d, p.depth, samples_per_node);
+        p.depth = d;
+    }
     void* ctx = nullptr;
     if ((rc = prgpu_create(&p, &ctx))) { fprintf(stderr, "create failed (%d): %s\n", rc, prgpu_last_error()); return 1; }
     if (learned && (rc = prgpu_load_preconditioner(ctx, learned))) {

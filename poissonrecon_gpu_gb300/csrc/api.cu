@@ -165,6 +165,18 @@ struct CallScope {
 
 static Ctx* as_ctx(void* p) { return (Ctx*)p; }
 
+// nodes holding at least one point, per depth (the level of node i from the level bases)
+__global__ void k_occupied(const int* __restrict__ pnum, const i64* __restrict__ base, int D,
+                           unsigned long long* __restrict__ occ) {
+    const i64 M = base[D + 1];
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (i64)gridDim.x * blockDim.x) {
+        if (pnum[i] <= 0) continue;
+        int d = 0;
+        while (d < D && base[d + 1] <= i) ++d;
+        atomicAdd(&occ[d], 1ull);
+    }
+}
+
 extern "C" {
 
 int prgpu_params_default(prgpu_params* p) {
@@ -666,6 +678,59 @@ int prgpu_set_array(void* h, const char* name, const void* src, int64_t bytes) {
     CK(cudaStreamSynchronize(c->stream));
     return PRGPU_OK;
     API_END
+}
+
+int prgpu_choose_depth(const float* xyz, const float* nrm, int64_t n, int32_t max_depth, double samples_per_node,
+                       int32_t device, int32_t* depth, int64_t* occupied) {
+    if (!xyz || !nrm || n <= 0 || !depth || !(samples_per_node > 0.0)) {
+        set_last_error("prgpu_choose_depth: points, a depth pointer and samples_per_node > 0 are required");
+        return PRGPU_ERR_ARG;
+    }
+    prgpu_params p;
+    prgpu_params_default(&p);
+    p.depth = max_depth;
+    p.device = device;
+    void* h = nullptr;
+    int rc = prgpu_create(&p, &h);
+    if (rc) return rc;
+    Ctx* c = as_ctx(h);
+    std::vector<unsigned long long> occ(max_depth + 1, 0);
+    rc = prgpu_set_points(h, xyz, nrm, n);
+    if (!rc) rc = prgpu_build_octree(h);
+    if (!rc) {
+        API_BEGIN_CTX(c)
+        cudaStream_t s = c->stream;
+        i64* dbase = dalloc<i64>(max_depth + 2, s);
+        unsigned long long* docc = dalloc<unsigned long long>(max_depth + 1, s);
+        CK(cudaMemcpyAsync(dbase, c->base.data(), (max_depth + 2) * sizeof(i64), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(docc, 0, (max_depth + 1) * sizeof(unsigned long long), s));
+        k_occupied<<<grid_for(c->nodes.M, 256), 256, 0, s>>>(c->nodes.pnum, dbase, max_depth, docc);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(occ.data(), docc, (max_depth + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        dfree(dbase, s);
+        dfree(docc, s);
+        rc = PRGPU_OK;
+        }
+        catch (const prgpu::Error& e) {
+            scope_.fail();
+            rc = e.status;
+        }
+        catch (...) {
+            scope_.fail();
+            prgpu::set_last_error("unexpected host exception");
+            rc = PRGPU_ERR_CUDA;
+        }
+    }
+    prgpu_destroy(h);
+    if (rc) return rc;
+    int best = 2;
+    for (int d = 2; d <= max_depth; ++d)
+        if (occ[d] > 0 && (double)n / (double)occ[d] >= samples_per_node) best = d;
+    *depth = best;
+    if (occupied)
+        for (int d = 0; d <= max_depth; ++d) occupied[d] = (int64_t)occ[d];
+    return PRGPU_OK;
 }
 
 int prgpu_stats_json(void* h, char* buf, int64_t len) {

@@ -179,6 +179,7 @@ struct CgDepth;
 void partition_depths(const Ctx& c, int d0, int d1, int G, std::vector<CgDepth>& deps, std::vector<int>& block_depth);
 void cascade_rhs(Ctx& c, int d, float* rhs);   // depth d's rows of an M-row device buffer
 void ensure_group_table(Ctx& c);
+void ensure_group_rows(Ctx& c);
 void stage_points(Ctx& c);
 void stage_mesh(Ctx& c);
 

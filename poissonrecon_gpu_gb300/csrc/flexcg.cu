@@ -70,6 +70,7 @@ struct FcgArgs {
     i64 M;
     const int* neigh;       // 27 x M
     const int* gn;          // group table
+    const int* gnr;         // the group table row by row (GN_ROW per group)
     i64 ngroups;
     const float* b;
     float* x;
@@ -191,6 +192,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
     __shared__ uint64_t bars[FCG_GROUPS];
     __shared__ uint32_t tslot;
     __shared__ int2 cellmap[64];   // per cell of a 4x4x4 block: (parent-neighbour j, child of it)
+    __shared__ int sgn[FCG_WARPS * FCG_WARP_TILES * 4 * GN_ROW];   // group-table rows: per warp (product) or per group (features)
     const int d = block_depth[blockIdx.x];
     const CgDepth& dp = deps[d];
     const int grp = threadIdx.x >> 8, lt = threadIdx.x & 255, gbar = 1 + grp;
@@ -295,14 +297,20 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
                         own_p = pnew[iown];
                     }
                 }
-                // the group-table entries of the four cells first, then their values: 4 and 8
-                // independent loads in flight per thread
+                // the tile's 16 group-table rows (one contiguous run) through shared memory, then
+                // the four cells' values: 4 and 8 independent loads in flight per thread
+                int* sg = sgn + grp * (16 * GN_ROW);
+                {
+                    const i64 row0 = (gfirst + tile * 16) * GN_ROW;
+                    const i64 nvalid = min((i64)16, ng - tile * 16) * GN_ROW;
+                    for (int k = lt; k < 16 * GN_ROW; k += 256) sg[k] = (k < nvalid) ? a.gnr[row0 + k] : -1;
+                }
+                group_sync(gbar);
                 int cns[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int e = lt + 256 * u;
-                    const i64 G = tile * 16 + (e >> 6);
-                    cns[u] = (G < ng) ? a.gn[(i64)cellmap[e & 63].x * a.ngroups + gfirst + G] : -1;
+                    cns[u] = sg[(e >> 6) * GN_ROW + cellmap[e & 63].x];
                 }
                 float rv[4], qv[4];
 #pragma unroll
@@ -465,17 +473,24 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
             const int ch = lane & 7, gl = lane >> 3;
             const int sx_ = (ch >> 2) & 1, sy = (ch >> 1) & 1, sz = ch & 1;
             float* wsp = sp + wib * (FCG_WARP_TILES * CG_TILE_WORDS);
+            int* wgn = sgn + wib * (FCG_WARP_TILES * 4 * GN_ROW);
             const i64 wstride = (i64)dp.nblocks * FCG_WARPS * FCG_WARP_TILES;
             for (i64 tile = ((i64)rank * FCG_WARPS + wib) * FCG_WARP_TILES; tile * 4 < ng; tile += wstride) {
+                __syncwarp();
+                {
+                    const i64 row0 = (gfirst + tile * 4) * GN_ROW;
+                    const i64 nvalid = min((i64)FCG_WARP_TILES * 4, ng - tile * 4) * GN_ROW;
+                    for (int k = lane; k < FCG_WARP_TILES * 4 * GN_ROW; k += 32)
+                        wgn[k] = (k < nvalid) ? a.gnr[row0 + k] : -1;
+                }
                 __syncwarp();
                 int cn[FCG_WARP_TILES * 8];
 #pragma unroll
                 for (int mm = 0; mm < FCG_WARP_TILES * 8; ++mm) {
                     const int e = lane + 32 * mm;
-                    const i64 g = tile * 4 + (e >> 6);
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
                     const int jp = 9 * ((bx + 1) >> 1) + 3 * ((by + 1) >> 1) + ((bz + 1) >> 1);
-                    cn[mm] = (g < ng) ? a.gn[(i64)jp * a.ngroups + gfirst + g] : -1;
+                    cn[mm] = wgn[(e >> 6) * GN_ROW + jp];
                 }
 #pragma unroll
                 for (int mm = 0; mm < FCG_WARP_TILES * 8; ++mm) {
@@ -585,7 +600,7 @@ void stage_solve_learned(Ctx& c) {
     float* p = dalloc<float>(M, s);
     float* p2 = dalloc<float>(M, s);
     float* q = dalloc<float>(M, s);
-    ensure_group_table(c);
+    ensure_group_rows(c);
     std::vector<float> cn(27 * (D + 1)), centre(D + 1);
     for (int d = 0; d <= D; ++d) {
         centre[d] = c.stencil[27 * d + 13];
@@ -633,6 +648,7 @@ void stage_solve_learned(Ctx& c) {
     a.M = M;
     a.neigh = c.nodes.neigh;
     a.gn = c.gn;
+    a.gnr = c.gn_rows;
     a.ngroups = (M - 1) / 8;
     a.b = c.divergence;
     a.x = c.x;

@@ -112,3 +112,26 @@ def test_weld_rule(oracle_mod):
         _, cnt = np.unique(e, axis=0, return_counts=True)
         return int((cnt == 1).sum())
     assert open_edges(wf) * 50 < open_edges(f)
+
+
+def test_density_depth_rule(oracle_mod):
+    """oracle.occupied_per_depth against the Morton prefixes of the sorted points, and the
+    density-based depth rule: sparser clouds (fewer points on the same surface) get coarser."""
+    from poissonrecon_gpu_gb300 import shapes
+    D = 9
+    depths = []
+    for n in (2000, 20000, 200000):
+        xyz, nrm = shapes.sphere(n, seed=4)
+        o = oracle_mod.Oracle(D, threads=4)
+        o.set_points(xyz, nrm)
+        o.build_octree()
+        occ = oracle_mod.occupied_per_depth(o)
+        key = o.get("key")[o.get("base")[D]:][o.get("pnum")[o.get("base")[D]:] > 0]
+        for d in range(D + 1):
+            assert occ[d] == len(np.unique(key >> (3 * (D - d)))), (n, d)
+        depths.append(oracle_mod.choose_depth(n, occ, D, 8.0))
+        # n / occupied is non-increasing in depth, and the rule picks the last depth meeting it
+        dd = depths[-1]
+        assert dd == 2 or n / occ[dd] >= 8.0
+        assert dd == D or n / occ[dd + 1] < 8.0
+    assert depths[0] < depths[1] < depths[2]
