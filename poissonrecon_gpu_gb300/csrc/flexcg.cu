@@ -78,7 +78,6 @@ struct FcgArgs {
     float* rb;
     float* z;
     float* p;               // search direction, two buffers used alternately
-    float* p2;
     float* q;
     FcgState* state;
     FcgSync* sync;          // one per depth
@@ -417,8 +416,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
     int k = 1;
     bool restart = true;
     float beta = 0.f;
-    const float* pold = a.p2;
-    float* pnew = a.p;
+    float* pnew = a.p;   // p and q are updated in place, each row by its own thread
     int refines = 0;
     double rr_true = -1.0;
     while (ok) {
@@ -451,9 +449,19 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
             continue;
         }
         const float* zsrc = plain ? rcur : a.z;
-        auto pdir = [&](i64 i) -> float { return restart ? zsrc[i] : fmaf(beta, pold[i], zsrc[i]); };
-        // phase A: p = z + beta p_old where it is read, q = A p, partial p.q
+        // phase A: s = A z (z gathered once per cell), then row by row p = z + beta p and
+        // q = A p = s + beta q, partial p.q
         FSum loc;
+        auto own_row = [&](i64 i, float zi, float si) {
+            float pi = zi, qi = si;
+            if (!restart) {
+                pi = fmaf(beta, pnew[i], zi);
+                qi = fmaf(beta, a.q[i], si);
+            }
+            pnew[i] = pi;
+            a.q[i] = qi;
+            loc.add(pi * qi);
+        };
         if (d == 0) {
             for (i64 t = start; t < n; t += stride) {
                 const i64 i = lo + t;
@@ -461,12 +469,9 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
 #pragma unroll
                 for (int j = 0; j < 27; ++j) {
                     const int nb = a.neigh[(i64)j * a.M + i];
-                    if (nb != -1 && sst[j] != 0.f) o = fmaf(sst[j], pdir(nb), o);
+                    if (nb != -1 && sst[j] != 0.f) o = fmaf(sst[j], zsrc[nb], o);
                 }
-                const float pi = pdir(i);
-                pnew[i] = pi;
-                a.q[i] = o;
-                loc.add(pi * o);
+                own_row(i, zsrc[i], o);
             }
         } else {
             const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -497,7 +502,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
                     const int e = lane + 32 * mm;
                     const int cell = e & 63, bx = cell >> 4, by = (cell >> 2) & 3, bz = cell & 3;
                     wsp[(e >> 8) * CG_TILE_WORDS + cg_block_base((e >> 6) & 3) + cell] = (cn[mm] != -1)
-                                 ? pdir(cn[mm] + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1)))
+                                 ? zsrc[cn[mm] + ((((bx + 1) & 1) << 2) | (((by + 1) & 1) << 1) | ((bz + 1) & 1))]
                                  : 0.f;
                 }
                 __syncwarp();
@@ -517,10 +522,7 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
                             for (int j = 0; j < 27; ++j)
                                 o = fmaf(sst[j], blk[(sx_ + j / 9) * 16 + (sy + (j / 3) % 3) * 4 + (sz + j % 3)], o);
                         }
-                        const float pi = blk[(sx_ + 1) * 16 + (sy + 1) * 4 + (sz + 1)];
-                        pnew[lo + 8 * g + ch] = pi;
-                        a.q[lo + 8 * g + ch] = o;
-                        loc.add(pi * o);
+                        own_row(lo + 8 * g + ch, blk[(sx_ + 1) * 16 + (sy + 1) * 4 + (sz + 1)], o);
                     }
                 }
             }
@@ -563,8 +565,6 @@ __global__ void __launch_bounds__(FCG_THREADS, 1) k_fcg_all(FcgArgs a, const CgD
         }
         rr_prev = rr;
         ++k;
-        pold = pnew;
-        pnew = (pnew == a.p) ? a.p2 : a.p;
     }
     if (rank == 0 && threadIdx.x == 0) {
         a.state[d].iters = k - 1;
@@ -598,7 +598,6 @@ void stage_solve_learned(Ctx& c) {
     float* rb = dalloc<float>(M, s);
     float* z = dalloc<float>(M, s);
     float* p = dalloc<float>(M, s);
-    float* p2 = dalloc<float>(M, s);
     float* q = dalloc<float>(M, s);
     ensure_group_rows(c);
     std::vector<float> cn(27 * (D + 1)), centre(D + 1);
@@ -656,7 +655,6 @@ void stage_solve_learned(Ctx& c) {
     a.rb = rb;
     a.z = z;
     a.p = p;
-    a.p2 = p2;
     a.q = q;
     a.state = st;
     a.sync = psync;
@@ -701,7 +699,7 @@ void stage_solve_learned(Ctx& c) {
         bytes += (double)hs[d].iters * (double)c.count[d] * (2 * 13.5 + 4 * 4 + 9 * 4);
     }
     if (kt >= 0) c.kpending[kt].bytes = bytes;
-    dfree(ra, s); dfree(rb, s); dfree(z, s); dfree(p, s); dfree(p2, s); dfree(q, s);
+    dfree(ra, s); dfree(rb, s); dfree(z, s); dfree(p, s); dfree(q, s);
     dfree(dcn, s); dfree(dcentre, s); dfree(ddeps, s); dfree(dbd, s); dfree(st, s); dfree(psync, s);
     dfree(partial, s); dfree(err, s);
     if (herr) {
