@@ -829,6 +829,7 @@ __device__ i64 shell_node(const VArgs& v, int L, int r, const int Lc[3], int d, 
     const int s2 = d - r;
     const int dx = (N[0] >> s2) - Lc[0], dy = (N[1] >> s2) - Lc[1], dz = (N[2] >> s2) - Lc[2];
     if (!dx && !dy && !dz) return -1;
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) return -1;   // not a neighbour's cell
     const int an = nd.neigh[(i64)(9 * (dx + 1) + 3 * (dy + 1) + (dz + 1)) * nd.M + L];
     if (an == -1) return -1;
     return descend(nd, an, r, d, N);
@@ -1108,36 +1109,71 @@ __device__ __forceinline__ signed char bound_sign(float lo, float hi, float amax
 
 // Shell terms of a bound at virtual depth d: the window cells outside the leaf that hold a
 // real node, each term x * X * Y * Z over the row tables' ranges RW.
-//  * Nodes: a cell's node is found by descending from the leaf's neighbour at depth r.  When
-//    d - r > SHELL_K the warp first finds the nodes of the (at most 2 x 2 x 2) cells of depth
-//    d - SHELL_K that cover the window ("anchors", one lane each) and each cell descends only
-//    SHELL_K levels from its anchor; cells under an absent anchor are skipped, and a window
-//    with no anchor is skipped whole.  The path through the anchor is the same path, so the
-//    node is the same.
+//  * Nodes: a cell's node is found by descending from the leaf's neighbour at depth r, through
+//    two levels of "anchors" the warp finds first: the cells of depth d - 4 covering the window
+//    (at most 2 per axis, one lane each; when d - r > 4) and of depth d - 2 (at most 4 per axis,
+//    two per lane, each descending 2 levels from its depth d - 4 anchor; when d - r > 2).  A
+//    cell then descends 2 levels from its anchor; cells under an absent anchor are skipped,
+//    and a window without any anchor is skipped whole.  The path through the anchors is the
+//    same path, so the node is the same.
 //  * The lanes run over the cells of all boxes in turn (a lane's next cell continues into the
 //    next box), so boxes smaller than a warp leave fewer lanes idle.
 //  * An RW range always contains 0 (lo <= 0 <= hi), and float rounding is monotone, so
 //    [a, b] x [lo, hi] = [min(b lo, a hi), max(a lo, b hi)]: exactly the min and max of the four
 //    rounded products, in 4 multiplies and 2 min/max instead of 4 and 6.
-constexpr int SHELL_K = 4;   // 2^SHELL_K = 16 >= the window's extent: at most 2 anchors per axis
+// The window's extent is at most 12 < 16 cells per axis: at most 2 anchors of depth d - 4 and
+// 4 of depth d - 2 per axis.
+constexpr int SHELL_ANCHORS = 8 + 64;   // ints of shared memory per warp
 __device__ __forceinline__ void shell_terms(const VArgs& v, int L, int r, const int Lc[3], int d, int D,
                                             const int wlo[3], const int ext[3], const float* const row[3],
                                             int lane, int* __restrict__ anchor, float& lo, float& hi, float& amax,
                                             int& cnt) {
     const float* __restrict__ xv = v.e.x;
-    const bool anch = d - r > SHELL_K;
-    int alo[3] = {0, 0, 0};
+    const NodeArrays& nd = v.e.nd;
+    const bool anch = d - r > 2;
+    int blo[3] = {0, 0, 0};
     if (anch) {
+        int* a4 = anchor;        // depth d - 4
+        int* a2 = anchor + 8;    // depth d - 2, 4 x 4 x 4
+        // only anchors that cover window cells are looked up: those lie in the leaf's
+        // neighbours (the window reaches at most 2 cells beyond the leaf)
+        int alo[3], ahi[3], bhi[3];
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) alo[ax] = wlo[ax] >> SHELL_K;   // floor, also below 0
-        int an = -1;
-        if (lane < 8) {
-            const int A[3] = {alo[0] + ((lane >> 2) & 1), alo[1] + ((lane >> 1) & 1), alo[2] + (lane & 1)};
-            an = (int)shell_node(v, L, r, Lc, d - SHELL_K, A);
+        for (int ax = 0; ax < 3; ++ax) {
+            alo[ax] = wlo[ax] >> 4;   // floor, also below 0
+            blo[ax] = wlo[ax] >> 2;
+            ahi[ax] = (wlo[ax] + ext[ax] - 1) >> 4;
+            bhi[ax] = (wlo[ax] + ext[ax] - 1) >> 2;
         }
-        if (__ballot_sync(0xffffffffu, an >= 0) == 0) return;   // no real node near this window
-        __syncwarp();                                            // the previous depth's readers are done
-        if (lane < 8) anchor[lane] = an;
+        __syncwarp();                 // the previous depth's readers are done
+        if (d - r > 4) {
+            int an = -1;
+            if (lane < 8) {
+                const int A[3] = {alo[0] + ((lane >> 2) & 1), alo[1] + ((lane >> 1) & 1), alo[2] + (lane & 1)};
+                if (A[0] <= ahi[0] && A[1] <= ahi[1] && A[2] <= ahi[2]) an = (int)shell_node(v, L, r, Lc, d - 4, A);
+            }
+            if (__ballot_sync(0xffffffffu, an >= 0) == 0) return;   // no real node near this window
+            if (lane < 8) a4[lane] = an;
+            __syncwarp();
+        }
+        int any = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = lane + 32 * h;
+            const int B[3] = {blo[0] + (q >> 4), blo[1] + ((q >> 2) & 3), blo[2] + (q & 3)};
+            int bn = -1;
+            if (B[0] > bhi[0] || B[1] > bhi[1] || B[2] > bhi[2]) {
+                // covers no window cell
+            } else if (d - r > 4) {
+                const int an = a4[(((B[0] >> 2) - alo[0]) << 2) | (((B[1] >> 2) - alo[1]) << 1) | ((B[2] >> 2) - alo[2])];
+                bn = an < 0 ? -1 : (int)descend(nd, an, d - 4, d - 2, B);
+            } else {
+                bn = (int)shell_node(v, L, r, Lc, d - 2, B);
+            }
+            a2[q] = bn;
+            any |= bn >= 0;
+        }
+        if (__ballot_sync(0xffffffffu, any) == 0) return;
         __syncwarp();
     }
     const int span = 1 << (d - r);
@@ -1147,6 +1183,7 @@ __device__ __forceinline__ void shell_terms(const VArgs& v, int L, int r, const 
     const float2* rw[3];
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) rw[ax] = reinterpret_cast<const float2*>(row[ax] + ROW_RW * (D + 1)) + d * BR_WEXT;
+    const int* a2 = anchor + 8;
     int g = lane, first = 0;
     for (int q = 0; q < nbx; ++q) {
         const Box3 bx = bxs[q];
@@ -1159,10 +1196,9 @@ __device__ __forceinline__ void shell_terms(const VArgs& v, int L, int r, const 
             const int N[3] = {bx.lo[0] + i0, bx.lo[1] + i1, bx.lo[2] + i2};
             i64 node;
             if (anch) {
-                const int an = anchor[(((N[0] >> SHELL_K) - alo[0]) << 2) | (((N[1] >> SHELL_K) - alo[1]) << 1) |
-                                      ((N[2] >> SHELL_K) - alo[2])];
-                if (an < 0) continue;
-                node = descend(v.e.nd, an, d - SHELL_K, d, N);
+                const int bn = a2[(((N[0] >> 2) - blo[0]) << 4) | (((N[1] >> 2) - blo[1]) << 2) | ((N[2] >> 2) - blo[2])];
+                if (bn < 0) continue;
+                node = descend(nd, bn, d - 2, d, N);
             } else {
                 node = shell_node(v, L, r, Lc, d, N);
             }
@@ -1190,7 +1226,7 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
                                                      const i64* __restrict__ srow_prefix,
                                                      const float* __restrict__ srows, const float* __restrict__ xl_all,
                                                      i64 nsuper, signed char* __restrict__ ssign) {
-    __shared__ int s_anchor[256 / 32][8];
+    __shared__ int s_anchor[256 / 32][SHELL_ANCHORS];
     const EvalArgs& a = v.e;
     const int D = a.D;
     const int lane = threadIdx.x & 31;
@@ -1250,7 +1286,7 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
                                                           const signed char* __restrict__ ssign,
                                                           const int* __restrict__ has_tri,
                                                           signed char* __restrict__ sign) {
-    __shared__ int s_anchor[BB_BLOCK / 32][8];
+    __shared__ int s_anchor[BB_BLOCK / 32][SHELL_ANCHORS];
     const EvalArgs& a = v.e;
     const int D = a.D;
     const int lane = threadIdx.x & 31;
