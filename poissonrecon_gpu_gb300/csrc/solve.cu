@@ -166,7 +166,10 @@ __global__ void k_group_rows(const int* __restrict__ gn, i64 ngroups, int* __res
 constexpr int CG_TILE_GROUPS = CG_BLOCK / 8;   // sibling groups per tile, one thread per row
 constexpr int CG_WARP_TILES = 2;               // tiles of 4 groups a warp stages at once
 
-__global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
+// 5 blocks per SM (48 registers): the partitions' warps wait on gathers and grid reductions, and
+// 40 warps per SM hide more of that latency than 32 (measured: 2.41 -> 1.90 ms on the 1M-point
+// torus at maxDepth 10; 6 blocks spill more and are slower again)
+__global__ void __launch_bounds__(CG_BLOCK, 5) k_cg_all(CgArgs a, const CgDepth* __restrict__ deps,
                                                      const int* __restrict__ block_depth) {
     __shared__ float sp[(CG_BLOCK / 32) * CG_WARP_TILES * CG_TILE_WORDS];
     __shared__ int sgn[(CG_BLOCK / 32) * CG_WARP_TILES * 4 * GN_ROW];
