@@ -21,7 +21,7 @@ __device__ __forceinline__ float finest_center(int off, int D) {
 // are staged once per group; each lane then runs its node's (neighbour, point)
 // pairs in neighbour order in one flat loop, so that the lanes stay together.
 constexpr int SPLAT_BLOCK = 128;
-__global__ void __launch_bounds__(SPLAT_BLOCK) k_splat(NodeArrays nd, const int* __restrict__ gn, i64 ngroups_all,
+__global__ void __launch_bounds__(SPLAT_BLOCK, 8) k_splat(NodeArrays nd, const int* __restrict__ gn, i64 ngroups_all,
                                                        i64 gfirst, i64 ng, i64 lo, int D, CPoly f,
                                                        const float* __restrict__ pts, const float* __restrict__ nrm,
                                                        float* __restrict__ vfield, int stable) {
