@@ -1263,7 +1263,9 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
                 window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wlo[ax], ext[ax], c);
                 cross |= c;
             }
-            if (!cross) continue;
+            // the windows of successive depths are nested (in finest cells), so once a window
+            // lies inside the leaf so do all finer ones
+            if (!cross) break;
             if (ext[0] > BR_WEXT || ext[1] > BR_WEXT || ext[2] > BR_WEXT) { decided = false; break; }
             shell_terms(v, L, r, Lc, d, D, wlo, ext, row, lane, s_anchor[threadIdx.x >> 5], flo, fhi, amax, cnt);
         }
@@ -1329,7 +1331,7 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
                 window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wlo[ax], ext[ax], c);
                 cross |= c;
             }
-            if (!cross) continue;
+            if (!cross) break;   // nested windows: the finer ones lie inside the leaf too
             // only window cells outside the leaf can hold a real node
             shell_terms(v, L, r, Lc, d, D, wlo, ext, row, lane, s_anchor[threadIdx.x >> 5], lo, hi, amax, cnt);
         }

@@ -46,3 +46,21 @@ def test_anchor_indices_stay_in_the_neighbourhood():
                             for N in range(wlo, wlo + ext):
                                 assert 0 <= (N >> 2) - blo <= 3
     assert checked > 500
+
+
+def test_windows_leave_the_leaf_only_at_coarse_depths():
+    """The bounds stop at the first depth whose window lies inside the leaf: the windows of
+    successive depths are nested, so crossing the leaf's boundary is monotone in depth."""
+    n = 0
+    for D in range(4, 13):
+        for r in range(1, D):
+            S = 1 << (D - r)
+            for E in sorted({min(S, 8), 32 if S >= 64 else min(S, 8)}):
+                nb = S // E
+                for Lc in range(min(1 << r, 4)):
+                    for b in range(nb):
+                        crosses = [_window_axis(Lc * S + b * E, E, Lc, r, d, D)[2] for d in range(r + 1, D + 1)]
+                        first_inside = crosses.index(False) if False in crosses else len(crosses)
+                        assert not any(crosses[first_inside:])
+                        n += 1
+    assert n > 1000
