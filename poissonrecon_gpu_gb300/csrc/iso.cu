@@ -2208,14 +2208,15 @@ void stage_mesh(Ctx& c) {
         CK_LAUNCH();
         // compulsory: the range part of every brick row and the leaves' neighbour x once, the
         // sign written and read, the culled flag written
-        const int kb = c.kbegin("brick_bound", (double)nrows * (6 + 2 * BR_WEXT) * (D + 1) * 4 +
-                                                   (double)nr * BR_LEVELS * 27 * 4 + (double)nbricks * 3);
         signed char* ssign = nullptr;
         if (nsuper > 0) {
             ssign = dalloc<signed char>(nsuper, s);
+            const int ksb = c.kbegin("super_bound", (double)nsrows * (6 + 2 * BR_WEXT) * (D + 1) * 4 +
+                                                        (double)nr * BR_LEVELS * 27 * 4 + (double)nsuper);
             k_super_bound<<<grid_for(nsuper * 32, 256, (i64)c.sms * 8), 256, 0, s>>>(va, bix.dl, dsrpre, srows, xl,
                                                                                     nsuper, ssign);
             CK_LAUNCH();
+            c.kend(ksb);
             if (c.profile) {   // statistics only
                 std::vector<signed char> hs(nsuper);
                 CK(cudaMemcpyAsync(hs.data(), ssign, nsuper, cudaMemcpyDeviceToHost, s));
@@ -2226,6 +2227,8 @@ void stage_mesh(Ctx& c) {
             }
         }
         // bricks of leaves with lattice edge >= 16 come first (roots are in depth order)
+        const int kb = c.kbegin("brick_bound", (double)nrows * (6 + 2 * BR_WEXT) * (D + 1) * 4 +
+                                                   (double)nr * BR_LEVELS * 27 * 4 + (double)nbricks * 3);
         k_brick_bound<<<grid_for(nbig * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, 0, nbig, dspre,
                                                                                          ssign, c.d_has_tri, bsign);
         CK_LAUNCH();
