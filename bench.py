@@ -192,16 +192,28 @@ def cpu_reference(args, steps, warmup):
 TRAFFIC = os.path.join(REPO, "profiles", "dram_traffic_torus1M_d10.md")
 
 
-def measured_traffic(args):
-    """DRAM bytes per launch of each kernel timer, from the committed ncu summary of this workload."""
+def measured_table(args):
+    """Per kernel timer, from the committed ncu summary of this workload: DRAM bytes per launch
+    ('traffic') and, where a full-section capture measured it, the issue-slot use ('issue')."""
     if args.shape != "torus" or args.points != 1_000_000 or args.depth != 10 or not os.path.exists(TRAFFIC):
         return {}
     out = {}
     for line in open(TRAFFIC):
         cols = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cols) == 6 and cols[4].isdigit():
-            out[cols[0]] = int(cols[4])
+        if len(cols) >= 6 and cols[4].isdigit():
+            row = {"traffic": int(cols[4])}
+            if len(cols) >= 7:
+                try:
+                    row["issue"] = float(cols[6]) / 100.0
+                except ValueError:
+                    pass
+            out[cols[0]] = row
     return out
+
+
+def measured_traffic(args):
+    """DRAM bytes per launch of each kernel timer, from the committed ncu summary of this workload."""
+    return {k: v["traffic"] for k, v in measured_table(args).items()}
 
 
 def file_io_pass(r, xyz, nrm, steps):
@@ -491,8 +503,10 @@ def max_over_ranks(values, device):
 AGGREGATE_TIMERS = {"divergence"}   # divergence_d, divergence_d1, divergence_groups, divergence_root
 
 
-def roofline(stats, peaks, traffic):
-    """The dominant kernel's roofline (an aggregate timer is not a kernel; its kernels are)."""
+def roofline(stats, peaks, traffic, issue=None):
+    """The dominant kernel's roofline (an aggregate timer is not a kernel; its kernels are).
+    issue: per timer, the fraction of issue slots ncu saw busy (an issue-bound kernel shows a
+    low HBM fraction and a high issue fraction)."""
     ks = {n: k for n, k in stats.get("kernels", {}).items() if n not in AGGREGATE_TIMERS}
     if not ks:
         return None
@@ -504,7 +518,8 @@ def roofline(stats, peaks, traffic):
     return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic.get(name),
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback",
-            "launch_ms": round(per_launch_ms, 4), "algorithmic_bytes_per_launch": bytes_per_launch}
+            "launch_ms": round(per_launch_ms, 4), "algorithmic_bytes_per_launch": bytes_per_launch,
+            "sm_issue_active": (issue or {}).get(name)}
 
 
 def main():
@@ -583,7 +598,8 @@ def main():
         "e2e": {"value": n * world / (t_e2e * 1e-3), "unit": "points/s", "ms_per_step": t_e2e,
                 "h2d_bytes_per_step": int(24 * n), "d2h_bytes_per_step": int(12 * nv + 12 * nt)},
         "gpu_launches": int(launches),
-        "roofline": roofline(stats, peaks, measured_traffic(args)),
+        "roofline": roofline(stats, peaks, measured_traffic(args),
+                             {k: v["issue"] for k, v in measured_table(args).items() if "issue" in v}),
         "kernel_roofline": kernel_roofline(stats, peaks, float(np.mean(prof_ms))),
         "profiled_ms_per_step": float(np.mean(prof_ms)),
         "clocks": clk.summary(),
