@@ -982,7 +982,10 @@ __device__ __forceinline__ int row_edge(int D, int r, int super) {
 }
 
 // one thread per (brick row, depth); rows numbered root by root (row_prefix), 3 x bricks-per-edge each
-__global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, float* __restrict__ rows) {
+// (rows of a single-brick leaf whose real corners change sign are skipped: k_brick_bound leaves
+// such a brick unproven without reading them)
+__global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, const int* __restrict__ has_tri,
+                             float* __restrict__ rows) {
     const EvalArgs& a = v.e;
     const int D = a.D;
     const i64* off = super ? dl.sroff : dl.roff;
@@ -998,6 +1001,7 @@ __global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, floa
         const int rl = (int)(loc % (3 * nbk));
         const int4 rd = make_int4(root, rl / nbk, rl % nbk, 0);   // root, axis, brick index
         const VRoot R = v.roots[rd.x];
+        if (!super && nbk == 1 && has_tri[R.node]) continue;
         const int ax = rd.y, r = R.depth, S = 1 << (D - r), B = row_edge(D, r, super);
         int Lc[3];
         key_coords(a.nd.key[R.node], r, D, Lc);
@@ -1042,19 +1046,29 @@ __global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, floa
 }
 
 // x of the 27 neighbours of each ancestor of every root (0: no neighbour)
-__global__ void k_brick_xl(VArgs v, int nroots, float* __restrict__ xl) {
+__global__ void __launch_bounds__(256) k_brick_xl(VArgs v, int nroots, float* __restrict__ xl) {
+    // one warp per root: lane 0 walks up the leaf's ancestors once, then the warp writes the
+    // 27 neighbours' x of every level
+    __shared__ int sanc[256 / 32][BR_LEVELS];
     const NodeArrays& nd = v.e.nd;
-    for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < (i64)nroots * BR_LEVELS * 27;
-         e += (i64)gridDim.x * blockDim.x) {
-        const int ri = (int)(e / (BR_LEVELS * 27)), l = (int)((e / 27) % BR_LEVELS), j = (int)(e % 27);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    for (i64 ri = warp; ri < nroots; ri += nwarps) {
         const VRoot R = v.roots[ri];
-        float x = 0.f;
-        if (l <= R.depth) {
+        __syncwarp();
+        if (lane == 0) {
             int node = R.node;
-            for (int q = R.depth; q > l; --q) node = nd.parent[node];
-            x = x_or_zero(v.e, nd.neigh[(i64)j * nd.M + node]);
+            for (int q = R.depth; q >= 0; --q) {
+                sanc[w][q] = node;
+                if (q > 0) node = nd.parent[node];
+            }
         }
-        xl[e] = x;
+        __syncwarp();
+        for (int t = lane; t < BR_LEVELS * 27; t += 32) {
+            const int l = t / 27, j = t % 27;
+            xl[ri * BR_LEVELS * 27 + t] = (l <= R.depth) ? x_or_zero(v.e, nd.neigh[(i64)j * nd.M + sanc[w][l]]) : 0.f;
+        }
     }
 }
 
@@ -2189,15 +2203,15 @@ void stage_mesh(Ctx& c) {
         }
         c.kend(kg);
         const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
-        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nrows, 0, rows);
+        k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nrows, 0, c.d_has_tri, rows);
         CK_LAUNCH();
         float* srows = nullptr;
         if (nsrows > 0) {
             srows = dalloc<float>(nsrows * ROW_PER_DEPTH * (D + 1), s);
-            k_brick_rows<<<grid_for(nsrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nsrows, 1, srows);
+            k_brick_rows<<<grid_for(nsrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nsrows, 1, c.d_has_tri, srows);
             CK_LAUNCH();
         }
-        k_brick_xl<<<grid_for((i64)nr * BR_LEVELS * 27, 256), 256, 0, s>>>(va, nr, xl);
+        k_brick_xl<<<grid_for((i64)nr * 32, 256), 256, 0, s>>>(va, nr, xl);
         CK_LAUNCH();
         c.kend(kr);
         unsigned char* culled = dalloc<unsigned char>(nbricks, s);
