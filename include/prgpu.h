@@ -241,9 +241,9 @@ int prgpu_cg_csr(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* 
  * library (about 3 MiB per GPU that loads the library, held until exit), so n
  * is limited to 262144 rows (PRGPU_ERR_LIMIT beyond).  All calls share that
  * array: calls that overlap on the GPU race and must be serialised by the
- * caller.  The first call on a device looks up the array's address; make it
- * before any stream capture.  Runs on 'stream' (a cudaStream_t, NULL = legacy
- * default stream) and returns after the solve has finished. */
+ * caller.  Runs on 'stream' (a cudaStream_t, NULL = legacy default stream) and
+ * returns after the solve has finished, so it cannot be captured into a CUDA
+ * graph: on a capturing stream it returns PRGPU_ERR_ARG. */
 int prgpu_cg_csr_noalloc(int32_t n, int32_t nz, const int32_t* d_rowptr, const int32_t* d_col,
                          const float* d_val, const float* d_rhs, float* d_x, float tol, int32_t max_iter,
                          void* stream, int32_t* iters);

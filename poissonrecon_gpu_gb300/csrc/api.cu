@@ -194,8 +194,8 @@ const char* prgpu_last_error(void) { return prgpu::last_error(); }
 
 int prgpu_create(const prgpu_params* p, void** out) {
     if (!p || !out) return PRGPU_ERR_ARG;
-    if (p->depth < 2 || p->depth > 15) {
-        set_last_error("depth %d outside the supported range 2..15", p->depth);
+    if (p->depth < 2 || p->depth > PRGPU_MAX_DEPTH) {
+        set_last_error("depth %d outside the supported range 2..%d", p->depth, PRGPU_MAX_DEPTH);
         return PRGPU_ERR_LIMIT;
     }
     Ctx* c = new Ctx();

@@ -17,6 +17,8 @@ namespace prgpu {
 typedef int64_t i64;
 typedef uint64_t u64;
 
+constexpr int PRGPU_MAX_DEPTH = 15;   // the largest maxDepth prgpu_create accepts
+
 // ---------------------------------------------------------------------------
 // error handling: every CUDA call inside the library goes through CK()
 // ---------------------------------------------------------------------------

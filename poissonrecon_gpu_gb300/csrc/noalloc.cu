@@ -19,8 +19,10 @@
 //     calls that overlap on the GPU (other streams, other host threads) race
 //     on it and must be serialised by the caller;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress) with that device current;
+//   * a call blocks until its solve ends (it reads the iteration count back),
+//     so it cannot be captured into a CUDA graph: on a capturing stream it
+//     returns PRGPU_ERR_ARG without touching the stream.
 #include <algorithm>
 #include <mutex>
 
@@ -206,10 +208,16 @@ extern "C" int prgpu_cg_csr_noalloc(int32_t n, int32_t nz, const int32_t* d_rowp
                        PRGPU_NOALLOC_MAX_ROWS);
         return PRGPU_ERR_LIMIT;
     }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) {
+        set_last_error("prgpu_cg_csr_noalloc: the stream is capturing; the call blocks until the solve ends and "
+                       "cannot be part of a CUDA graph");
+        return PRGPU_ERR_ARG;
+    }
     void* scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

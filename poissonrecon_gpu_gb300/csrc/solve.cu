@@ -417,6 +417,8 @@ void ensure_group_table(Ctx& c) {
 // copy of x.  One thread per node of depth d.
 // ---------------------------------------------------------------------------
 constexpr int CASCADE_MAX_DEPTH = 16;
+// prgpu_create accepts maxDepth 2..15, so the per-ancestor arrays below always fit
+static_assert(PRGPU_MAX_DEPTH < CASCADE_MAX_DEPTH, "the cascadic arrays need a slot per depth below maxDepth");
 
 struct CascadeArgs {
     int d, D;

@@ -72,3 +72,34 @@ def test_noalloc_rejects_oversized_systems(lib_built):
                                 1e-5, 10, None, None)
     assert rc == 4
     assert b"static scratch limit" in L.prgpu_last_error()
+
+
+def test_noalloc_refuses_a_capturing_stream(lib_built):
+    """The call blocks until its solve ends, so it cannot be part of a CUDA graph: on a capturing
+    stream it returns PRGPU_ERR_ARG before touching the stream, the capture stays valid, and a
+    call after the capture solves as usual."""
+    torch = pytest.importorskip("torch")
+    import poissonrecon_gpu_gb300 as pg
+    L = pg._lib()
+    dev = torch.device("cuda:0")
+    n = 4096
+    rowptr, col, val, b = _spd_csr(n, 3)
+    tI, tJ = torch.tensor(rowptr, device=dev), torch.tensor(col, device=dev)
+    tV, tb = torch.tensor(val, device=dev), torch.tensor(b, device=dev)
+    x = torch.zeros(n, dtype=torch.float32, device=dev)
+    y = torch.ones(16, device=dev)
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    it = ctypes.c_int32(0)
+    with torch.cuda.graph(g, stream=s):
+        y.mul_(2.0)
+        rc = L.prgpu_cg_csr_noalloc(n, len(val), tI.data_ptr(), tJ.data_ptr(), tV.data_ptr(), tb.data_ptr(),
+                                    x.data_ptr(), 1e-5, 10000, ctypes.c_void_p(s.cuda_stream), ctypes.byref(it))
+    assert rc == 1 and b"capturing" in L.prgpu_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(y[0]) == 2.0
+    rc = L.prgpu_cg_csr_noalloc(n, len(val), tI.data_ptr(), tJ.data_ptr(), tV.data_ptr(), tb.data_ptr(),
+                                x.data_ptr(), 1e-5, 10000, None, ctypes.byref(it))
+    assert rc == 0 and it.value > 0
