@@ -52,7 +52,7 @@ ROOT_STRIDE = 400              # CPU sample: subdivide every 400th subdivided le
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)   # enough timed work for the 200 ms clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="prgpu", choices=["prgpu", "reference"])
     ap.add_argument("--points", type=int, default=1_000_000)
