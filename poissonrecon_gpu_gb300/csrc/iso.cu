@@ -776,8 +776,16 @@ constexpr int BR_WEXT = BR + 4;    // window edge at the finest depth, with the 
 // multiple of its edge B <= 8, with the extra upper cell per axis (bricks
 // with foreign corners): at most 12^3 + 8^3 + 6^3 + 12 * 5^3 = 3956
 constexpr int BR_XW = 3968;
-// brick-row table: RA (6 per depth), RW (24 per depth)
+// super-brick row table: RA (6 per depth), RW (24 per depth)
 constexpr int ROW_RA = 0, ROW_RW = 6, ROW_PER_DEPTH = 30;
+// brick row table: 24 floats per depth d > r (the ancestors, d <= r, are one polynomial per leaf)
+//   d <= D - lg E  PW[n]  window cell n < 4: Bernstein form over the brick's corners (b0, b1, b2, M,
+//                         see bern_fit) of its function, masked as RW is; the function's knots are
+//                         multiples of its cell width 2^(D-d) >= E, so it is one quadratic piece there
+//   d >  D - lg E  RW[n]  as above (12 cells, range with 0)
+constexpr int PROW = 24;
+constexpr int PW = 4;              // window cells per axis at the depths of knot spacing >= E
+constexpr int ANC_STRIDE = 32;     // per root: Bernstein coefficients C[27] of the ancestors, S3, count, FIT
 
 __device__ __forceinline__ int brick_edge(int D, int r) { return min(1 << (D - r), BR); }
 
@@ -794,8 +802,9 @@ struct BrickIndex {                // bricks of all subdivided leaves, numbered 
     const i64* prefix;             // first brick of each root
     const i64* row_prefix;         // first brick row of each root (3 * bricks per edge rows each)
     int nroots;
-    const float* rows;             // brick-row tables, 30 (D+1) floats each
+    const float* rows;             // brick-row tables, PROW (D+1) floats each
     const float* xl;               // per root: x of the 27 neighbours of each ancestor, 16 x 27
+    const float* anc;              // per root: the ancestor polynomial, ANC_STRIDE floats
     DepthLayout dl;
 };
 struct VBrick {
@@ -818,7 +827,43 @@ __device__ __forceinline__ VBrick brick_of(const VArgs& v, const BrickIndex& bx,
     return b;
 }
 __device__ __forceinline__ const float* brick_row(const BrickIndex& bx, int D, int root, int nb, int ax, int b) {
-    return bx.rows + (bx.row_prefix[root] + (i64)ax * nb + b) * (i64)(ROW_PER_DEPTH * (D + 1));
+    return bx.rows + (bx.row_prefix[root] + (i64)ax * nb + b) * (i64)(PROW * (D + 1));
+}
+
+__device__ __forceinline__ float f4_at(const float4& f, int i) { return i == 0 ? f.x : (i == 1 ? f.y : f.z); }
+
+// Bernstein form over the corners k = 0..K (K a power of two <= 2^15) of a function tabulated
+// there, val(k), that is one quadratic piece over them in exact arithmetic: b0 = v(0), b2 = v(K),
+// b1 = 2 v(K/2) - (b0 + b2) / 2 (the quadratic Q through the three), returned as (b0, b1, b2, delta)
+// with delta >= max_k |Q(k) - v(k)|.  The tabulated values are the reference's float evaluations of
+// shifted polynomials, whose error grows about 4x per depth (near 1e-3 at depth 8 of a depth-10
+// tree), so delta is that noise rather than rounding.  Q(k) = b0 B0 + b1 B1 + b2 B2 with
+// B0 = (K-k)^2 / K^2, B1 = 2k(K-k) / K^2, B2 = k^2 / K^2 (exact in float for K <= 2^12, else rounded
+// once); its float evaluation is within 4u max|b| of Q (the 5u max|b| term), a float |a - b| is
+// within u of exact (the factor 1 + 2^-20), and the factor 1 + 2^-16 covers the last roundings.
+template <class F>
+__device__ __forceinline__ float4 bern_fit(F val, int K) {
+    const float v0 = val(0), vm = val(K >> 1), vK = val(K);
+    const float b1 = 2.0f * vm - 0.5f * (v0 + vK);
+    const float mb = fmaxf(fmaxf(fabsf(v0), fabsf(vK)), fabsf(b1));
+    const float inv = 1.0f / ((float)K * (float)K);   // a power of two: exact
+    float dmax = 0.f;
+    for (int k = 0; k <= K; ++k) {
+        const float vk = val(k);
+        const float B0 = (float)((K - k) * (K - k)) * inv, B1 = (float)(2 * k * (K - k)) * inv,
+                    B2 = (float)(k * k) * inv;
+        const float q = fmaf(v0, B0, fmaf(b1, B1, vK * B2));
+        dmax = fmaxf(dmax, fabsf(q - vk));
+    }
+    const float u = 5.9604644775390625e-08f;   // 2^-24
+    const float delta = (dmax * (1.0f + 9.5367431640625e-07f) + 5.0f * u * mb) * (1.0f + 1.52587890625e-05f);
+    return make_float4(v0, b1, vK, delta);
+}
+
+// M = max|b_i| + delta for an entry (b0, b1, b2, delta) of bern_fit: it bounds |Q| (a Bernstein
+// form lies within its coefficients' range) and |v(k)| <= |Q(k)| + delta; rounded up
+__device__ __forceinline__ float bern_m(const float4& f) {
+    return (fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fabsf(f.z)) + f.w) * (1.0f + 9.5367431640625e-07f);
 }
 
 __device__ __forceinline__ float x_or_zero(const EvalArgs& a, int node) { return node < 0 ? 0.f : a.x[node]; }
@@ -1007,8 +1052,9 @@ __global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, cons
         key_coords(a.nd.key[R.node], r, D, Lc);
         const int g0 = Lc[ax] * S + rd.z * B;
         const int c0 = rd.z * B;
-        float* out = rows + row * (i64)(ROW_PER_DEPTH * (D + 1));
+        float* out = rows + row * (i64)((super ? ROW_PER_DEPTH : PROW) * (D + 1));
         if (d <= r) {
+            if (!super) continue;   // bricks: the leaf's ancestor polynomial (k_brick_xl)
             for (int t = 0; t < 3; ++t) {
                 float mn = brick_bt(a, r, Lc[ax], g0, d, t, 0), mx = mn;
                 for (int k = 1; k <= B; ++k) {
@@ -1024,42 +1070,71 @@ __global__ void k_brick_rows(VArgs v, DepthLayout dl, i64 nrows, int super, cons
             bool cross;
             window_axis(g0, B, Lc[ax], r, d, D, 0, wlo, ext, cross);
             const int sh = D - d, lim = 1 << d;
+            // the term of window cell N at corner k: its basis value where the corner's owner cell
+            // (the lower-face corner owns its own cell) is within one cell of N, else 0
+            auto term = [&](int N, int k) {
+                const int Va = (k == 0 && c0 == 0) ? (g0 >> sh) : ((g0 + k - 1) >> sh);
+                return (N < Va - 1 || N > Va + 1) ? 0.f : lattice_basis(a, d, N, g0 + k);
+            };
+            if (!super && (1 << sh) >= B) {
+                float4* pw = reinterpret_cast<float4*>(out + d * PROW);
+                for (int n = 0; n < PW; ++n) {
+                    const int N = wlo + n;
+                    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (n < ext && N >= 0 && N < lim) f = bern_fit([&](int k) { return term(N, k); }, B);
+                    pw[n] = f;
+                }
+                continue;
+            }
+            float* rw = super ? out + ROW_RW * (D + 1) + d * BR_WEXT * 2 : out + d * PROW;
             for (int n = 0; n < BR_WEXT; ++n) {
                 const int N = wlo + n;
                 float mn = 0.f, mx = 0.f;             // 0: corners without this term
                 if (n < ext && N >= 0 && N < lim) {
                     for (int k = 0; k <= B; ++k) {
-                        // owner cell of corner k: the lower-face corner owns its own cell
-                        const int Va = (k == 0 && c0 == 0) ? (g0 >> sh) : ((g0 + k - 1) >> sh);
-                        const int Vb = Va;
-                        if (N < Va - 1 || N > Vb + 1) continue;
-                        const float b = lattice_basis(a, d, N, g0 + k);
+                        const float b = term(N, k);
                         mn = fminf(mn, b);
                         mx = fmaxf(mx, b);
                     }
                 }
-                out[ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2] = mn;
-                out[ROW_RW * (D + 1) + (d * BR_WEXT + n) * 2 + 1] = mx;
+                rw[n * 2] = mn;
+                rw[n * 2 + 1] = mx;
             }
         }
     }
 }
 
-// x of the 27 neighbours of each ancestor of every root (0: no neighbour)
-__global__ void __launch_bounds__(256) k_brick_xl(VArgs v, int nroots, float* __restrict__ xl) {
-    // one warp per root: lane 0 walks up the leaf's ancestors once, then the warp writes the
-    // 27 neighbours' x of every level
-    __shared__ int sanc[256 / 32][BR_LEVELS];
+// Per root: x of the 27 neighbours of each ancestor (0: no neighbour; xl, for the evaluation),
+// and the leaf's ancestor polynomial (anc, for the bounds).  Every ancestor function is one
+// quadratic piece per axis over the leaf (its knots are multiples of its cell width, and the leaf
+// lies in one such cell), so the ancestors' sum is one tri-quadratic over the leaf, kept in
+// Bernstein form over t = (corner - leaf origin) / S per axis:
+//   C[9i + 3j + l] = sum over levels and neighbours of x * bx_i * by_j * bz_l   (bern_fit's b)
+// (lane k computes coefficient k, per level as sum_jx bx_i (sum_jy by_j (sum_jz x bz_l))), then
+// S3 = sum |x| Mx My Mz, the number of terms and FIT = sum |x| (dx My Mz + Mx dy Mz + Mx My dz)
+// (d the fits' residuals, M = bern_m), which bounds |sum x (vx vy vz - Qx Qy Qz)| at every corner.
+// Single-brick leaves whose corners change sign are never bounded: their polynomial is left 0.
+constexpr int XL_WARPS = 4;
+__global__ void __launch_bounds__(32 * XL_WARPS) k_brick_xl(VArgs v, int nroots, const int* __restrict__ has_tri,
+                                                            float* __restrict__ xl, float* __restrict__ anc) {
+    // one warp per root: lane 0 walks up the leaf's ancestors once; the warp writes the 27
+    // neighbours' x of every level, fits the ancestor functions of all levels (lanes over
+    // level, axis, offset), then forms the polynomial
+    __shared__ int sanc[XL_WARPS][BR_LEVELS];
+    __shared__ float sx[XL_WARPS][BR_LEVELS * 27];
+    __shared__ float4 sfit[XL_WARPS][BR_LEVELS * 9];   // [level][axis][t]
     const NodeArrays& nd = v.e.nd;
+    const int D = v.e.D;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
     for (i64 ri = warp; ri < nroots; ri += nwarps) {
         const VRoot R = v.roots[ri];
-        __syncwarp();
+        const int r = R.depth, S = 1 << (D - r);
+        __syncwarp();   // the previous root's readers are done
         if (lane == 0) {
             int node = R.node;
-            for (int q = R.depth; q >= 0; --q) {
+            for (int q = r; q >= 0; --q) {
                 sanc[w][q] = node;
                 if (q > 0) node = nd.parent[node];
             }
@@ -1067,8 +1142,54 @@ __global__ void __launch_bounds__(256) k_brick_xl(VArgs v, int nroots, float* __
         __syncwarp();
         for (int t = lane; t < BR_LEVELS * 27; t += 32) {
             const int l = t / 27, j = t % 27;
-            xl[ri * BR_LEVELS * 27 + t] = (l <= R.depth) ? x_or_zero(v.e, nd.neigh[(i64)j * nd.M + sanc[w][l]]) : 0.f;
+            const float x = (l <= r) ? x_or_zero(v.e, nd.neigh[(i64)j * nd.M + sanc[w][l]]) : 0.f;
+            xl[ri * BR_LEVELS * 27 + t] = x;
+            sx[w][t] = x;
         }
+        const bool poly = !(S <= BR && has_tri[R.node]);
+        int Lc[3];
+        key_coords(nd.key[R.node], r, D, Lc);
+        if (poly) {
+            for (int f = lane; f < 9 * (r + 1); f += 32) {
+                const int l = f / 9, ax = (f % 9) / 3, t = f % 3, g0 = Lc[ax] * S;
+                sfit[w][f] = bern_fit([&](int k) { return brick_bt(v.e, r, Lc[ax], g0, l, t, k); }, S);
+            }
+        }
+        __syncwarp();
+        float c = 0.f, s3 = 0.f, fit = 0.f;
+        int cnt = 0;
+        if (poly && lane < 27) {
+            const int i = lane / 9, j = (lane / 3) % 3, lz = lane % 3;
+            for (int l = 0; l <= r; ++l) {
+                const float* xs = sx[w] + 27 * l;
+                const float4* F = sfit[w] + 9 * l;
+                float acc = 0.f;
+                for (int jx = 0; jx < 3; ++jx) {
+                    float ys = 0.f;
+                    for (int jy = 0; jy < 3; ++jy) {
+                        float zs = 0.f;
+                        for (int jz = 0; jz < 3; ++jz) zs = fmaf(xs[9 * jx + 3 * jy + jz], f4_at(F[6 + jz], lz), zs);
+                        ys = fmaf(f4_at(F[3 + jy], j), zs, ys);
+                    }
+                    acc = fmaf(f4_at(F[jx], i), ys, acc);
+                }
+                c += acc;
+                const float ax = fabsf(xs[lane]);   // the neighbour at offset (i, j, lz)
+                if (ax != 0.f) {
+                    const float Mx = bern_m(F[i]), My = bern_m(F[3 + j]), Mz = bern_m(F[6 + lz]);
+                    s3 += ax * Mx * My * Mz;
+                    fit += ax * (F[i].w * My * Mz + Mx * F[3 + j].w * Mz + Mx * My * F[6 + lz].w);
+                    ++cnt;
+                }
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+            fit += __shfl_xor_sync(0xffffffffu, fit, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        anc[ri * ANC_STRIDE + lane] =
+            lane < 27 ? c : (lane == 27 ? s3 : (lane == 28 ? (float)cnt : (lane == 29 ? fit : 0.f)));
     }
 }
 
@@ -1134,6 +1255,7 @@ __device__ __forceinline__ signed char bound_sign(float lo, float hi, float amax
 //    same path, so the node is the same.
 //  * The lanes run over the cells of all boxes in turn (a lane's next cell continues into the
 //    next box), so boxes smaller than a warp leave fewer lanes idle.
+//  * rw[ax]: the depth's RW ranges of the window cells along each axis.
 //  * An RW range always contains 0 (lo <= 0 <= hi), and float rounding is monotone, so
 //    [a, b] x [lo, hi] = [min(b lo, a hi), max(a lo, b hi)]: exactly the min and max of the four
 //    rounded products, in 4 multiplies and 2 min/max instead of 4 and 6.
@@ -1141,7 +1263,7 @@ __device__ __forceinline__ signed char bound_sign(float lo, float hi, float amax
 // 4 of depth d - 2 per axis.
 constexpr int SHELL_ANCHORS = 8 + 64;   // ints of shared memory per warp
 __device__ __forceinline__ void shell_terms(const VArgs& v, int L, int r, const int Lc[3], int d, int D,
-                                            const int wlo[3], const int ext[3], const float* const row[3],
+                                            const int wlo[3], const int ext[3], const float2* const rw[3],
                                             int lane, int* __restrict__ anchor, float& lo, float& hi, float& amax,
                                             int& cnt) {
     const float* __restrict__ xv = v.e.x;
@@ -1196,9 +1318,6 @@ __device__ __forceinline__ void shell_terms(const VArgs& v, int L, int r, const 
     const int llo[3] = {Lc[0] * span, Lc[1] * span, Lc[2] * span};
     Box3 bxs[6];
     const int nbx = outside_boxes(wlo, ext, llo, span, bxs);
-    const float2* rw[3];
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) rw[ax] = reinterpret_cast<const float2*>(row[ax] + ROW_RW * (D + 1)) + d * BR_WEXT;
     const int* a2 = anchor + 8;
     int g = lane, first = 0;
     for (int q = 0; q < nbx; ++q) {
@@ -1281,7 +1400,9 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
             // lies inside the leaf so do all finer ones
             if (!cross) break;
             if (ext[0] > BR_WEXT || ext[1] > BR_WEXT || ext[2] > BR_WEXT) { decided = false; break; }
-            shell_terms(v, L, r, Lc, d, D, wlo, ext, row, lane, s_anchor[threadIdx.x >> 5], flo, fhi, amax, cnt);
+            const float2* rw[3];
+            for (int ax = 0; ax < 3; ++ax) rw[ax] = reinterpret_cast<const float2*>(row[ax] + ROW_RW * (D + 1)) + d * BR_WEXT;
+            shell_terms(v, L, r, Lc, d, D, wlo, ext, rw, lane, s_anchor[threadIdx.x >> 5], flo, fhi, amax, cnt);
         }
         for (int o = 16; o; o >>= 1) {
             flo += __shfl_xor_sync(0xffffffffu, flo, o);
@@ -1293,21 +1414,111 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
     }
 }
 
+// Shell terms at a depth d of knot spacing >= the brick edge (d <= D - lg E): each window cell
+// outside the leaf with a real node contributes x Qx Qy Qz, Q the cell's PW entries (Bernstein
+// form over the brick), to the brick's coarse polynomial.  The window spans at most PW = 4 cells
+// per axis there (the brick lies in one cell of depth d, and its first corner's owner may lie in
+// the cell below), so 4^3 cells, two per lane.  The lanes stage their terms in shared memory in
+// lane order, then lane k < 27 adds coefficient k = 9i + 3j + l of every term,
+// C_ijl += Qx_i (Qy_j (x Qz_l)).  s3 gains |x| Mx My Mz, fit |x| (dx My Mz + Mx dy Mz + Mx My dz)
+// (as k_brick_xl's), cnt the number of terms.
+__device__ __forceinline__ void shell_poly(const VArgs& v, int L, int r, const int Lc[3], int d, const int wlo[3],
+                                           const int ext[3], const float4* const pw[3], int lane,
+                                           float2* __restrict__ stage, float& coef, float& s3, float& fit, int& cnt) {
+    int nst = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int g = lane + 32 * h, n0 = g >> 4, n1 = (g >> 2) & 3, n2 = g & 3;
+        float x = 0.f;
+        if (n0 < ext[0] && n1 < ext[1] && n2 < ext[2]) {
+            const int N[3] = {wlo[0] + n0, wlo[1] + n1, wlo[2] + n2};
+            const i64 node = shell_node(v, L, r, Lc, d, N);
+            if (node >= 0) x = v.e.x[node];
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, x != 0.f);
+        if (x != 0.f) {
+            const float4 X = pw[0][n0], Y = pw[1][n1], Z = pw[2][n2];
+            const float Mx = bern_m(X), My = bern_m(Y), Mz = bern_m(Z), ax = fabsf(x);
+            s3 += ax * Mx * My * Mz;
+            fit += ax * (X.w * My * Mz + Mx * Y.w * Mz + Mx * My * Z.w);
+            ++cnt;
+            stage[nst + __popc(m & ((1u << lane) - 1u))] = make_float2(x, __int_as_float(g));
+        }
+        nst += __popc(m);
+    }
+    __syncwarp();
+    if (lane < 27) {
+        const int i = lane / 9, j = (lane / 3) % 3, l = lane % 3;
+        for (int q = 0; q < nst; ++q) {
+            const float2 t = stage[q];
+            const int g = __float_as_int(t.y);
+            const float xz = t.x * f4_at(pw[2][g & 3], l);
+            coef = fmaf(f4_at(pw[0][g >> 4], i), f4_at(pw[1][(g >> 2) & 3], j) * xz, coef);
+        }
+    }
+    __syncwarp();   // the stage is reused by the next depth
+}
+
+// sign of a bound lo = min C + flo, hi = max C + fhi against iso: C the Bernstein coefficients over
+// the brick of its coarse polynomial P (the leaf's ancestors and the shell terms of knot spacing
+// >= E; P lies within their range over the brick's box), [flo, fhi] the interval sum of the finer
+// shell terms.  The margin is bound_sign's over A = amax + s3 (the evaluation's FMA chain over all
+// the terms, and the interval part's own arithmetic), plus fit (the fits' residuals: the corner
+// values' coarse terms lie within fit of P), plus (cnt + 72) u s3 for P's coefficients,
+// s3 = sum |x| Mx My Mz over its terms: (cnt + 26)u for forming them (at most 9 roundings per
+// level and 16 levels for the ancestors, 4 per shell term and one per further term), 40u for the
+// restriction to the brick (3 rounded factors and 27 FMAs per coefficient; the blossom rows are
+// non-negative and sum to 1) and adding the two parts.
+__device__ __forceinline__ signed char bound_sign_poly(float lo, float hi, float amax, float s3, float fit, int cnt,
+                                                       float iso) {
+    const float u = 5.9604644775390625e-08f;   // 2^-24
+    const float A = (amax + s3) * 1.01f;
+    const float m = ((2.0f * (float)cnt + (2.0f * BR_WEXT + 8.0f)) * u * A + ((float)cnt + 72.0f) * u * s3 * 1.01f +
+                     fit * 1.01f + 6.0f * u * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(iso)) + 1e-30f) *
+                    (1.0f + 1.52587890625e-05f);
+    if (lo - iso > m) return 1;
+    if (iso - hi > m) return -1;
+    return 0;
+}
+
+// row q of the blossom matrix that takes quadratic Bernstein coefficients over [0, S] to those over
+// [A, B] (0 <= A < B <= S, S a power of two <= 2^15): the blossom of the basis at (A, A), (A, B),
+// (B, B), divided by S^2 (exact in float for S <= 2^11, else rounded once); non-negative, sums to 1
+__device__ __forceinline__ void blossom_row(int A, int B, int S, int q, float out[3]) {
+    const i64 a = A, b = B, s = S;
+    i64 n0, n1, n2;
+    if (q == 0) { n0 = (s - a) * (s - a); n1 = 2 * a * (s - a); n2 = a * a; }
+    else if (q == 1) { n0 = (s - a) * (s - b); n1 = a * (s - b) + b * (s - a); n2 = a * b; }
+    else { n0 = (s - b) * (s - b); n1 = 2 * b * (s - b); n2 = b * b; }
+    const float inv = 1.0f / ((float)S * (float)S);
+    out[0] = (float)n0 * inv;
+    out[1] = (float)n1 * inv;
+    out[2] = (float)n2 * inv;
+}
+
 // one warp per brick: the bound over the corners the brick's leaf owns;
-// sign[bi] = 1 (all above iso), -1 (all below) or 0 (not proven)
+// sign[bi] = 1 (all above iso), -1 (all below) or 0 (not proven).
+//  * The coarse part, exact up to rounding and the tabulated values' noise: the leaf's ancestor
+//    polynomial (per root, k_brick_xl) and the shell terms of depths d <= D - lg E (shell_poly),
+//    bounded over the brick by the range of its Bernstein coefficients there.
+//  * The finer shell terms (depths d > D - lg E, one to three cells of the finest lattice wide
+//    around the leaf's faces) by intervals, as shell_terms sums them.
 constexpr int BB_BLOCK = 256;
 // A single-brick leaf whose own real corners change sign ('has_tri') is left unproven at once:
 // its brick's corners include the leaf's corners, so its bound straddles iso (and a brick left
 // unproven is only evaluated exactly, which changes no value).
-__global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bix, i64 first, i64 nbricks,
+// (4 blocks per SM: 64 registers, no spills; unbounded it takes 104 and halves the resident warps)
+__global__ void __launch_bounds__(BB_BLOCK, 4) k_brick_bound(VArgs v, BrickIndex bix, i64 first, i64 nbricks,
                                                           const i64* __restrict__ sprefix,
                                                           const signed char* __restrict__ ssign,
                                                           const int* __restrict__ has_tri,
                                                           signed char* __restrict__ sign) {
     __shared__ int s_anchor[BB_BLOCK / 32][SHELL_ANCHORS];
+    __shared__ float2 s_stage[BB_BLOCK / 32][PW * PW * PW];
+    __shared__ float s_coef[BB_BLOCK / 32][27];   // the leaf's ancestor polynomial
     const EvalArgs& a = v.e;
     const int D = a.D;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
     for (i64 bi = first + warp; bi < nbricks; bi += nwarps) {
@@ -1331,13 +1542,13 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
         const int g0[3] = {Lc[0] * S + B.b[0] * E, Lc[1] * S + B.b[1] * E, Lc[2] * S + B.b[2] * E};
         const float* row[3];
         for (int ax = 0; ax < 3; ++ax) row[ax] = brick_row(bix, D, B.root, nb, ax, B.b[ax]);
-        const float* xl = bix.xl + (i64)B.root * BR_LEVELS * 27;
-        float lo = 0.f, hi = 0.f, amax = 0.f;
+        const int dpoly = D - (31 - __clz(E));   // depths of knot spacing >= E
+        float lo = 0.f, hi = 0.f, amax = 0.f, s3 = 0.f, fit = 0.f, coef = 0.f;
         int cnt = 0;
-        // the leaf and its ancestors
-        ancestor_bound(xl, row, r, D, lane, lo, hi, amax, cnt);
-        // real nodes around the leaf, at the virtual depths
-        for (int d = r + 1; d <= D; ++d) {
+        bool ok = true, inside = false;
+        int d = r + 1;
+        // real nodes around the leaf, at the virtual depths: coarse ones into the polynomial
+        for (; d <= dpoly; ++d) {
             int wlo[3], ext[3];
             bool cross = false;
             for (int ax = 0; ax < 3; ++ax) {
@@ -1345,20 +1556,70 @@ __global__ void __launch_bounds__(BB_BLOCK) k_brick_bound(VArgs v, BrickIndex bi
                 window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wlo[ax], ext[ax], c);
                 cross |= c;
             }
-            if (!cross) break;   // nested windows: the finer ones lie inside the leaf too
-            // only window cells outside the leaf can hold a real node
-            shell_terms(v, L, r, Lc, d, D, wlo, ext, row, lane, s_anchor[threadIdx.x >> 5], lo, hi, amax, cnt);
+            if (!cross) { inside = true; break; }   // nested windows: the finer ones lie inside the leaf too
+            if (ext[0] > PW || ext[1] > PW || ext[2] > PW) { ok = false; break; }   // (cannot happen)
+            const float4* pw[3];
+            for (int ax = 0; ax < 3; ++ax) pw[ax] = reinterpret_cast<const float4*>(row[ax] + d * PROW);
+            shell_poly(v, L, r, Lc, d, wlo, ext, pw, lane, s_stage[w], coef, s3, fit, cnt);
+        }
+        // the finer ones by intervals; only window cells outside the leaf can hold a real node
+        if (ok && !inside) {
+            for (; d <= D; ++d) {
+                int wlo[3], ext[3];
+                bool cross = false;
+                for (int ax = 0; ax < 3; ++ax) {
+                    bool c;
+                    window_axis(g0[ax], E, Lc[ax], r, d, D, 0, wlo[ax], ext[ax], c);
+                    cross |= c;
+                }
+                if (!cross) break;
+                const float2* rw[3];
+                for (int ax = 0; ax < 3; ++ax) rw[ax] = reinterpret_cast<const float2*>(row[ax] + d * PROW);
+                shell_terms(v, L, r, Lc, d, D, wlo, ext, rw, lane, s_anchor[w], lo, hi, amax, cnt);
+            }
+        }
+        // the coarse polynomial's Bernstein coefficients over the brick: the leaf's ancestor
+        // polynomial restricted to it (lane k < 27: coefficient k = 9i + 3j + l, through the
+        // blossom rows i, j, l of the three axes; the identity for a single-brick leaf) plus the
+        // shell part
+        const float* an = bix.anc + (i64)B.root * ANC_STRIDE;
+        __syncwarp();   // the previous brick's readers are done
+        if (lane < 27) s_coef[w][lane] = an[lane];
+        __syncwarp();
+        float cmin = INFINITY, cmax = -INFINITY;
+        if (lane < 27) {
+            float c = s_coef[w][lane];
+            if (nb > 1) {
+                float tx[3], ty[3], tz[3];
+                blossom_row(B.b[0] * E, (B.b[0] + 1) * E, S, lane / 9, tx);
+                blossom_row(B.b[1] * E, (B.b[1] + 1) * E, S, (lane / 3) % 3, ty);
+                blossom_row(B.b[2] * E, (B.b[2] + 1) * E, S, lane % 3, tz);
+                c = 0.f;
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        const float tij = tx[i] * ty[j];
+#pragma unroll
+                        for (int l = 0; l < 3; ++l) c = fmaf(s_coef[w][9 * i + 3 * j + l], tij * tz[l], c);
+                    }
+            }
+            c += coef;
+            cmin = cmax = c;
         }
         for (int o = 16; o; o >>= 1) {
             lo += __shfl_xor_sync(0xffffffffu, lo, o);
             hi += __shfl_xor_sync(0xffffffffu, hi, o);
             amax += __shfl_xor_sync(0xffffffffu, amax, o);
+            s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+            fit += __shfl_xor_sync(0xffffffffu, fit, o);
             cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            cmin = fminf(cmin, __shfl_xor_sync(0xffffffffu, cmin, o));
+            cmax = fmaxf(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
         }
-        // rounding of the evaluation's FMA chain, (cnt + 4) u sum|term|, plus that of this
-        // bound's own float products and sums, at most (cnt + 5) u sum|term| (factored
-        // ancestor rows) -- allowed (cnt + 2 BR_WEXT + 4)
-        if (lane == 0) sign[bi] = bound_sign(lo, hi, amax, cnt, v.iso);
+        if (lane == 0)
+            sign[bi] = ok ? bound_sign_poly(cmin + lo, cmax + hi, amax, s3 + an[27], fit + an[29], cnt + (int)an[28], v.iso)
+                          : (signed char)0;
     }
 }
 
@@ -2189,9 +2450,10 @@ void stage_mesh(Ctx& c) {
         i64* drpre = dpre + nr + 1;
         i64* dspre = dpre + 2 * (nr + 1);
         i64* dsrpre = dpre + 3 * (nr + 1);
-        float* rows = dalloc<float>(nrows * ROW_PER_DEPTH * (D + 1), s);
+        float* rows = dalloc<float>(nrows * PROW * (D + 1), s);
         float* xl = dalloc<float>((i64)nr * BR_LEVELS * 27, s);
-        BrickIndex bix{dbpre, drpre, nr, rows, xl, {}};
+        float* anc = dalloc<float>((i64)nr * ANC_STRIDE, s);
+        BrickIndex bix{dbpre, drpre, nr, rows, xl, anc, {}};
         for (int d = 0; d <= D; ++d) {
             bix.dl.first[d] = layout.first[d];
             bix.dl.lg[d] = std::max(D - d - 3, 0);          // bricks per edge 2^(D-d) / min(2^(D-d), 8)
@@ -2202,7 +2464,7 @@ void stage_mesh(Ctx& c) {
             bix.dl.sroff[d] = layout.off[3][d];
         }
         c.kend(kg);
-        const int kr = c.kbegin("brick_rows", (double)nrows * ROW_PER_DEPTH * (D + 1) * 4);
+        const int kr = c.kbegin("brick_rows", (double)nrows * PROW * (D + 1) * 4);
         k_brick_rows<<<grid_for(nrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nrows, 0, c.d_has_tri, rows);
         CK_LAUNCH();
         float* srows = nullptr;
@@ -2211,7 +2473,7 @@ void stage_mesh(Ctx& c) {
             k_brick_rows<<<grid_for(nsrows * (D + 1), 128), 128, 0, s>>>(va, bix.dl, nsrows, 1, c.d_has_tri, srows);
             CK_LAUNCH();
         }
-        k_brick_xl<<<grid_for((i64)nr * 32, 256), 256, 0, s>>>(va, nr, xl);
+        k_brick_xl<<<grid_for((i64)nr * 32, 32 * XL_WARPS), 32 * XL_WARPS, 0, s>>>(va, nr, c.d_has_tri, xl, anc);
         CK_LAUNCH();
         c.kend(kr);
         unsigned char* culled = dalloc<unsigned char>(nbricks, s);
@@ -2220,8 +2482,8 @@ void stage_mesh(Ctx& c) {
         CK(cudaMemsetAsync(root_of, 0xff, nCoarse * sizeof(int), s));
         k_root_of<<<grid_for(nr, 256), 256, 0, s>>>(droots, nr, root_of);
         CK_LAUNCH();
-        // compulsory: the range part of every brick row and the leaves' neighbour x once, the
-        // sign written and read, the culled flag written
+        // compulsory: every brick row and the leaves' ancestor polynomial (super-bricks: their
+        // rows and the neighbour x) once, the sign written and read, the culled flag written
         signed char* ssign = nullptr;
         if (nsuper > 0) {
             ssign = dalloc<signed char>(nsuper, s);
@@ -2241,8 +2503,8 @@ void stage_mesh(Ctx& c) {
             }
         }
         // bricks of leaves with lattice edge >= 16 come first (roots are in depth order)
-        const int kb = c.kbegin("brick_bound", (double)nrows * (6 + 2 * BR_WEXT) * (D + 1) * 4 +
-                                                   (double)nr * BR_LEVELS * 27 * 4 + (double)nbricks * 3);
+        const int kb = c.kbegin("brick_bound", (double)nrows * PROW * (D + 1) * 4 +
+                                                   (double)nr * ANC_STRIDE * 4 + (double)nbricks * 3);
         k_brick_bound<<<grid_for(nbig * 32, BB_BLOCK, (i64)c.sms * 8), BB_BLOCK, 0, s>>>(va, bix, 0, nbig, dspre,
                                                                                          ssign, c.d_has_tri, bsign);
         CK_LAUNCH();
@@ -2259,6 +2521,7 @@ void stage_mesh(Ctx& c) {
         dfree(bsign, s);
         dfree(ssign, s);
         dfree(srows, s);
+        dfree(anc, s);
         kg = c.kbegin("mesh_lists", 0.0);
         int* bf = dalloc<int>(nbricks, s);
         int* bp = dalloc<int>(nbricks + 1, s);
