@@ -1418,14 +1418,19 @@ __global__ void __launch_bounds__(256) k_super_bound(VArgs v, DepthLayout dl,
 // outside the leaf with a real node contributes x Qx Qy Qz, Q the cell's PW entries (Bernstein
 // form over the brick), to the brick's coarse polynomial.  The window spans at most PW = 4 cells
 // per axis there (the brick lies in one cell of depth d, and its first corner's owner may lie in
-// the cell below), so 4^3 cells, two per lane.  The lanes stage their terms in shared memory in
-// lane order, then lane k < 27 adds coefficient k = 9i + 3j + l of every term,
-// C_ijl += Qx_i (Qy_j (x Qz_l)).  s3 gains |x| Mx My Mz, fit |x| (dx My Mz + Mx dy Mz + Mx My dz)
-// (as k_brick_xl's), cnt the number of terms.
+// the cell below), so the terms form a 4^3 grid X of x (0: no node, or inside the leaf; two cells
+// per lane), contracted one axis at a time through shared memory:
+//   T1[n0 n1 l] = sum_n2 X Qz_l(n2),  T2[n0 j l] = sum_n1 T1 Qy_j(n1),  C_ijl += sum_n0 T2 Qx_i(n0)
+// (lane k < 27 holds coefficient k = 9i + 3j + l).  s3 gains |x| Mx My Mz, fit
+// |x| (dx My Mz + Mx dy Mz + Mx My dz) (as k_brick_xl's), cnt the number of terms.
+constexpr int SHELL_POLY_BUF = 64 + 48 + 36;   // floats of shared memory per warp
 __device__ __forceinline__ void shell_poly(const VArgs& v, int L, int r, const int Lc[3], int d, const int wlo[3],
                                            const int ext[3], const float4* const pw[3], int lane,
-                                           float2* __restrict__ stage, float& coef, float& s3, float& fit, int& cnt) {
-    int nst = 0;
+                                           float* __restrict__ buf, float& coef, float& s3, float& fit, int& cnt) {
+    float* X = buf;
+    float* T1 = buf + 64;
+    float* T2 = buf + 112;
+    bool any = false;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int g = lane + 32 * h, n0 = g >> 4, n1 = (g >> 2) & 3, n2 = g & 3;
@@ -1435,28 +1440,42 @@ __device__ __forceinline__ void shell_poly(const VArgs& v, int L, int r, const i
             const i64 node = shell_node(v, L, r, Lc, d, N);
             if (node >= 0) x = v.e.x[node];
         }
-        const unsigned m = __ballot_sync(0xffffffffu, x != 0.f);
+        X[g] = x;
         if (x != 0.f) {
-            const float4 X = pw[0][n0], Y = pw[1][n1], Z = pw[2][n2];
-            const float Mx = bern_m(X), My = bern_m(Y), Mz = bern_m(Z), ax = fabsf(x);
+            const float4 QX = pw[0][n0], QY = pw[1][n1], QZ = pw[2][n2];
+            const float Mx = bern_m(QX), My = bern_m(QY), Mz = bern_m(QZ), ax = fabsf(x);
             s3 += ax * Mx * My * Mz;
-            fit += ax * (X.w * My * Mz + Mx * Y.w * Mz + Mx * My * Z.w);
+            fit += ax * (QX.w * My * Mz + Mx * QY.w * Mz + Mx * My * QZ.w);
             ++cnt;
-            stage[nst + __popc(m & ((1u << lane) - 1u))] = make_float2(x, __int_as_float(g));
+            any = true;
         }
-        nst += __popc(m);
+    }
+    if (!__any_sync(0xffffffffu, any)) return;   // no real node near the brick at this depth
+    __syncwarp();
+    for (int e = lane; e < 48; e += 32) {
+        const int nn = e / 3, l = e - 3 * nn;   // nn = 4 n0 + n1
+        float t = 0.f;
+#pragma unroll
+        for (int n2 = 0; n2 < 4; ++n2) t = fmaf(X[4 * nn + n2], f4_at(pw[2][n2], l), t);
+        T1[e] = t;
+    }
+    __syncwarp();
+    for (int e = lane; e < 36; e += 32) {
+        const int n0 = e / 9, j = (e / 3) % 3, l = e % 3;
+        float t = 0.f;
+#pragma unroll
+        for (int n1 = 0; n1 < 4; ++n1) t = fmaf(T1[(4 * n0 + n1) * 3 + l], f4_at(pw[1][n1], j), t);
+        T2[e] = t;
     }
     __syncwarp();
     if (lane < 27) {
-        const int i = lane / 9, j = (lane / 3) % 3, l = lane % 3;
-        for (int q = 0; q < nst; ++q) {
-            const float2 t = stage[q];
-            const int g = __float_as_int(t.y);
-            const float xz = t.x * f4_at(pw[2][g & 3], l);
-            coef = fmaf(f4_at(pw[0][g >> 4], i), f4_at(pw[1][(g >> 2) & 3], j) * xz, coef);
-        }
+        const int i = lane / 9, jl = lane % 9;
+        float t = 0.f;
+#pragma unroll
+        for (int n0 = 0; n0 < 4; ++n0) t = fmaf(T2[9 * n0 + jl], f4_at(pw[0][n0], i), t);
+        coef += t;
     }
-    __syncwarp();   // the stage is reused by the next depth
+    __syncwarp();   // the buffer is reused by the next depth
 }
 
 // sign of a bound lo = min C + flo, hi = max C + fhi against iso: C the Bernstein coefficients over
@@ -1464,16 +1483,16 @@ __device__ __forceinline__ void shell_poly(const VArgs& v, int L, int r, const i
 // >= E; P lies within their range over the brick's box), [flo, fhi] the interval sum of the finer
 // shell terms.  The margin is bound_sign's over A = amax + s3 (the evaluation's FMA chain over all
 // the terms, and the interval part's own arithmetic), plus fit (the fits' residuals: the corner
-// values' coarse terms lie within fit of P), plus (cnt + 72) u s3 for P's coefficients,
-// s3 = sum |x| Mx My Mz over its terms: (cnt + 26)u for forming them (at most 9 roundings per
-// level and 16 levels for the ancestors, 4 per shell term and one per further term), 40u for the
+// values' coarse terms lie within fit of P), plus (cnt + 96) u s3 for P's coefficients,
+// s3 = sum |x| Mx My Mz over its terms: (cnt + 56)u for forming them (at most 9 roundings per
+// level and 16 levels for the ancestors, 12 per shell depth and one per further depth), 40u for the
 // restriction to the brick (3 rounded factors and 27 FMAs per coefficient; the blossom rows are
 // non-negative and sum to 1) and adding the two parts.
 __device__ __forceinline__ signed char bound_sign_poly(float lo, float hi, float amax, float s3, float fit, int cnt,
                                                        float iso) {
     const float u = 5.9604644775390625e-08f;   // 2^-24
     const float A = (amax + s3) * 1.01f;
-    const float m = ((2.0f * (float)cnt + (2.0f * BR_WEXT + 8.0f)) * u * A + ((float)cnt + 72.0f) * u * s3 * 1.01f +
+    const float m = ((2.0f * (float)cnt + (2.0f * BR_WEXT + 8.0f)) * u * A + ((float)cnt + 96.0f) * u * s3 * 1.01f +
                      fit * 1.01f + 6.0f * u * (fabsf(lo) + fabsf(hi) + 2.0f * fabsf(iso)) + 1e-30f) *
                     (1.0f + 1.52587890625e-05f);
     if (lo - iso > m) return 1;
@@ -1514,7 +1533,7 @@ __global__ void __launch_bounds__(BB_BLOCK, 4) k_brick_bound(VArgs v, BrickIndex
                                                           const int* __restrict__ has_tri,
                                                           signed char* __restrict__ sign) {
     __shared__ int s_anchor[BB_BLOCK / 32][SHELL_ANCHORS];
-    __shared__ float2 s_stage[BB_BLOCK / 32][PW * PW * PW];
+    __shared__ float s_stage[BB_BLOCK / 32][SHELL_POLY_BUF];
     __shared__ float s_coef[BB_BLOCK / 32][27];   // the leaf's ancestor polynomial
     const EvalArgs& a = v.e;
     const int D = a.D;
